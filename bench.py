@@ -1,0 +1,331 @@
+"""Benchmark of the SU(2) block-sparse H_eff*psi hot path on GB300.
+
+Workload (the reference's microbenchmark shape): one two-site effective
+Hamiltonian with D=2000 SU(2) multiplets per bond (sectors 2j=0..12, Gaussian
+counts), spin-1/2 sites (enlarged legs 2j=0..13, psi = 1,576,457 doubles), 18
+spin-1 operator pairs plus the two spin-0 block Hamiltonians (width 20),
+seeded synthetic data (workloads.synthetic_heff, seed 1234).  One "step" is
+one application y = H_eff psi.
+
+Printed JSON (rank 0, one line):
+  value  algorithmic FLOPs per application / device time, operators and psi
+         resident in HBM (the operators, ~1.3 GB, exceed the 129 MB L2, so no
+         flush is needed between iterations);
+  e2e    the same metric through the C ABI with host buffers: pinned-host psi
+         copied in, applied, y copied back, every step;
+  roofline, cpu_baseline, clocks, gpu_launches as documented in the design doc.
+--impl reference times the CPU restatement of the reference's hot path (the
+reference itself is not built on the GPU host) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "H_eff*psi TFLOP/s (FP64-equivalent), SU(2) D=2000 two-site step, width 20"
+UNIT = "TFLOP/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="su2g", choices=["su2g", "reference"])
+    ap.add_argument("--mode", default="f64", choices=["f64"])
+    ap.add_argument("--D", type=int, default=2000)
+    ap.add_argument("--nspin1", type=int, default=18)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank, world = 0, 1
+    if "RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+
+        rank = int(os.environ["RANK"])
+        world = int(os.environ["WORLD_SIZE"])
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 GEMM throughput (cuBLAS DGEMM 8192^3, best of 5): the
+    denominator of the FP64 roofline, which MEASURED_PEAKS.json does not hold."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b, out=c)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b, c
+    torch.cuda.empty_cache()
+    return 2.0 * n**3 / best / 1e12
+
+
+class CpuSample:
+    """Oracle (CPU restatement of the reference hot path, BLAS dgemm) on a
+    bounded sample of the workload: `nspin1_sample` of the spin-1 terms plus
+    the spin-0 terms at full D, all host cores."""
+
+    def __init__(self, D, nspin1_sample):
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle as o
+
+        from su2dmrg_gb300.workloads import synthetic_heff
+
+        self.o = o
+        self.cores = os.cpu_count() or 1
+        o.set_blas_threads(self.cores)
+        w = synthetic_heff(D=D, nspin1=nspin1_sample, seed=1234)
+        self.w = w
+        self.prob = o.HeffProblem(w.psi, w.terms, w.hl, w.hr)
+        self.flops = o.heff_flops(self.prob)
+        self.desc = (f"{nspin1_sample} of 18 spin-1 terms + both spin-0 terms at D={D} "
+                     f"(oracle C restatement of the reference, OpenBLAS dgemm, {self.cores} threads)")
+
+    def step(self):
+        t0 = time.perf_counter()
+        self.o.heff_apply(self.prob, self.w.psi_data)
+        return time.perf_counter() - t0
+
+    def measure(self, seconds=10.0, max_steps=20):
+        self.step()  # warm
+        ts = []
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds and len(ts) < max_steps:
+            ts.append(self.step())
+        dt = float(np.median(ts))
+        return {"value": self.flops / dt / 1e12, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "sample": f"{len(ts)} applications of {self.desc}; median time"}
+
+
+def run_reference(args):
+    rank, world = 0, 1
+    if args.gpus > 1 and "RANK" in os.environ:
+        rank = int(os.environ["RANK"])
+    if rank != 0:
+        return 0
+    cs = CpuSample(args.D, 2)
+    for _ in range(args.warmup):
+        cs.step()
+    ts = [cs.step() for _ in range(args.steps)]
+    dt = float(np.median(ts))
+    v = cs.flops / dt / 1e12
+    cb = {"value": v, "unit": UNIT, "cores": cs.cores, "kind": "port",
+          "sample": f"each step = one application of {cs.desc}; median of {args.steps}"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"synthetic SU(2) two-site H_eff, D={args.D}, width {args.nspin1 + 2}",
+                       "sample": cb["sample"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_su2g(args):
+    import torch
+
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300.su2 import HeffPlan
+    from su2dmrg_gb300.workloads import synthetic_heff
+
+    rank, world = dist_setup(args)
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)) if world > 1 else 0)
+    capi.lib()
+    w = synthetic_heff(D=args.D, nspin1=args.nspin1, seed=1234)
+    psi, terms, hl, hr = w.to_device()
+    plan = HeffPlan(w.psi, terms, hl, hr, mode=capi.MODE_F64)
+    info = plan.info()
+    flops = info["flops"]
+    y = torch.empty_like(psi)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        plan.apply(psi, y, stream)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing ----
+    barrier(world)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s, e in ev:
+            s.record(stream)
+            plan.apply(psi, y, stream)
+            e.record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    total = t0.elapsed_time(t1) / 1e3
+    total = max_over_ranks(total, world)
+    per_step = [s.elapsed_time(e) / 1e3 for s, e in ev]
+    ms_per_step = total / args.steps * 1e3
+    value = flops * world * args.steps / total / 1e12
+
+    # ---- end to end through the C ABI with host buffers ----
+    h_psi = torch.from_numpy(w.psi_data.copy()).pin_memory()
+    h_y = torch.empty_like(h_psi).pin_memory()
+    d_in = torch.empty_like(psi)
+    for _ in range(2):
+        d_in.copy_(h_psi, non_blocking=True)
+        plan.apply(d_in, y, stream)
+        h_y.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        d_in.copy_(h_psi, non_blocking=True)
+        plan.apply(d_in, y, stream)
+        h_y.copy_(y, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_total = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    e2e_value = flops * world * args.steps / e2e_total / 1e12
+    nbytes = psi.numel() * 8
+
+    if rank != 0:
+        return 0
+    # parity spot check of the measured output against the host copy path
+    assert torch.equal(h_y.cuda(), y), "e2e output differs from device-resident output"
+
+    peak64 = fp64_peak_tflops(torch)
+    kernel_time = float(np.mean(per_step))  # both launches of gemm_f64_tiles fill the step
+    achieved = flops / kernel_time / 1e12
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+            "frac": achieved / peak64, "traffic": None,
+            "kernel": "gemm_f64_tiles (FP64 DMMA), 2 launches per step",
+            "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 is not in MEASURED_PEAKS.json)"}
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = CpuSample(args.D, 2).measure(seconds=10.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"synthetic SU(2) two-site H_eff, D={args.D}, width {args.nspin1 + 2}",
+                   "mode": args.mode, "psi_doubles": int(psi.numel()), "flops_per_step": flops,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs (operators ~1.3 GB) larger than L2; no flush"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "path": "su2g_heff_apply via ctypes, pinned host psi -> device -> host y"},
+        "gpu_launches": 2 * args.steps,
+        "roofline": roof,
+        "cpu_baseline": cb,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_su2g(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

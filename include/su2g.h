@@ -1,0 +1,138 @@
+/*
+ * su2g: GB300-native (sm_103a) SU(2) block-sparse DMRG hot path, C ABI.
+ *
+ * This header is the drop-in boundary between an SU2DMRG-style host engine and
+ * the GPU library libsu2g.so.  Every entry point takes plain pointers and sizes
+ * and returns an int status (SU2G_OK = 0); on failure su2g_last_error() gives
+ * a one-line reason for the calling thread.  Nothing here calls exit().
+ *
+ * Block tensors (tensor_su2, tensor_su2.hpp:6-124) cross the boundary in the
+ * reference's own checkpoint layout (dmrg_su2_omp.cpp:864-941):
+ *   desc  int[]  = [nbond, locspin, {dir, n, angm[n], dim[n]} per leg]
+ *                  angm = 2j of each sector in ascending order (su2bond),
+ *                  dim  = multiplet count of the sector;
+ *   flag  int[nten] = 1 where the block is stored, in mixed-radix block order
+ *                  with leg 0 fastest (su2struct.cpp:243-261);
+ *   data  double[] = the stored blocks back to back in block order, each a
+ *                  column-major array of its multiplet dims (leg 0 fastest).
+ * Only the reduced (multiplet) blocks travel; the Clebsch-Gordan part of each
+ * block is the canonical one the reference engine uses (the singlet for 2-leg
+ * vectors, make_cgc(j0,j1,j2) for 3-leg operators, the identity for 2-leg
+ * scalar operators), so it is implied by the sector labels.
+ *
+ * "device" pointers are CUDA device addresses on the current device; "stream"
+ * is a cudaStream_t passed as void* (NULL = legacy default stream).
+ */
+#ifndef SU2G_H
+#define SU2G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SU2G_OK 0
+#define SU2G_EINVAL 1      /* inconsistent structures or arguments */
+#define SU2G_ENOMEM 2      /* device allocation refused */
+#define SU2G_ECUDA 3       /* a CUDA runtime call failed */
+#define SU2G_ETIMEOUT 4    /* a bounded device wait gave up */
+#define SU2G_EUNSUPPORTED 5
+
+#define SU2G_MODE_F64 0        /* plain FP64 contractions */
+#define SU2G_MODE_SPLIT_BF16 1 /* FP64 emulated with BF16 slices on the tensor cores */
+
+typedef struct su2g_heff_plan su2g_heff_plan;
+
+/* A block tensor: structure + presence flags (host) and packed data (device). */
+typedef struct {
+  const int* desc;
+  const int* flag;
+  const double* data;
+} su2g_tensor;
+
+/* One two-sided term  coef * op1 (x) op2  of the effective Hamiltonian. */
+typedef struct {
+  su2g_tensor op1; /* 3 legs: (left-in, operator spin, left-out)   */
+  su2g_tensor op2; /* 3 legs: (right-in, operator spin, right-out) */
+  double coef;
+} su2g_term;
+
+/* ---------------------------------------------------------------- meta -- */
+/* Library version (major*10000 + minor*100 + patch). */
+int su2g_version(void);
+/* One-line reason for the last failure on this thread. */
+const char* su2g_last_error(void);
+
+/* Number of blocks of a structure (su2struct::get_nten, su2struct.hpp:27). */
+int su2g_struct_nten(const int* desc);
+/* legal[i] = 1 for every block that passes the reference's legality test
+ * (su2struct::get_tensor_argument / check_angularmoments, su2struct.cpp:264-332).
+ * Returns nten, or -1 for a malformed desc. */
+int su2g_struct_legal(const int* desc, int* legal);
+/* offsets[i] (doubles) of every stored block in the packed layout, -1 where
+ * flag[i] == 0; returns the packed length, -1 for a malformed desc. */
+int64_t su2g_layout(const int* desc, const int* flag, int64_t* offsets);
+/* su2bond::fuse (su2bond.cpp:155-210): sectors of b1 (x) b2, ascending, 2j
+ * capped at 38.  aout/dout need room for 64 sectors. */
+int su2g_bond_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, const int* d2, int* nout,
+                   int* aout, int* dout);
+/* tensor::make_cgc (tensor.cpp:1353-1407), column-major (j1+1)(j2+1)(j3+1). */
+int su2g_make_cgc(int j1, int j2, int j3, double* out);
+/* fac_hamilt_vec[i][j][k] of dmrg_su2.cpp:759-766 at out[(i*m+j)*m+k]. */
+int su2g_fac_hamilt_vec(int max_angm, double* out);
+
+/* -------------------------------------------------------------- H_eff -- */
+/* Builds the device work list of one effective Hamiltonian
+ *   y = hl_coef*H_L^T psi + hr_coef*psi H_R + sum_t coef_t (op1_t, op2_t) psi
+ * for a two-site step.  Replaces the per-call term loop of
+ * dmrg_su2::hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664) and
+ * the block loops of tensor_su2::hamiltonian_vector_multiplication
+ * (tensor_su2_dmrg_src.cpp:893-1041) and tensor_su2::contract for the spin-0
+ * terms (tensor_su2.cpp:1255-1345, called at dmrg_su2.cpp:563-570).
+ * psi_desc/psi_flag describe psi and y (2 legs, locspin 0).  hl/hr may be
+ * NULL.  Operator data pointers are captured and must stay valid until the plan
+ * is destroyed.  Allocates the work list and its scratch on the device. */
+int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                          su2g_heff_plan** plan);
+/* flops: algorithmic FLOPs of one application; psi_len: packed length of psi
+ * and y (doubles); scratch_bytes: device scratch held by the plan; ntiles:
+ * output tiles of the two launch phases. */
+int su2g_heff_plan_info(const su2g_heff_plan* plan, double* flops, int64_t* psi_len, int64_t* scratch_bytes,
+                        int* ntiles);
+/* y = H_eff psi (device pointers, psi_len doubles each, no aliasing). */
+int su2g_heff_apply(su2g_heff_plan* plan, const double* psi, double* y, void* stream);
+int su2g_heff_plan_destroy(su2g_heff_plan* plan);
+
+/* One-shot form of tensor_su2::hamiltonian_vector_multiplication(vec, op1, op2)
+ * (tensor_su2_dmrg_src.cpp:893-1041): y = (op1, op2) vec with the recoupling
+ * factors of fac_hamilt_vec.  y (device) uses vec's layout: op1's last leg must
+ * equal vec's leg 0 and op2's last leg vec's leg 1, so the result can be added
+ * to vec-shaped accumulators as the reference does (dmrg_su2.cpp:606-608). */
+int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_flag, const double* vec,
+                                           su2g_tensor op1, su2g_tensor op2, double* y, void* stream);
+
+/* ------------------------------------------------------------ Lanczos -- */
+/* Ground state of the plan's H_eff by the reference's Lanczos scheme
+ * (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195, driven as in
+ * dmrg_su2::lanczos_solve_eigenvector_idmrg, dmrg_su2.cpp:527-540): at most
+ * mlanc Krylov vectors, full reorthogonalisation, tridiagonal eigenproblem,
+ * eigenvector check every 4 steps with early exit.  psi (device) is the start
+ * vector on entry and the normalised ground state on exit; *energy receives
+ * the eigenvalue (without the reference's -1000 print offset); *nmatvec, if
+ * not NULL, the number of H_eff applications. */
+int su2g_lanczos(su2g_heff_plan* plan, double* psi, int mlanc, double* energy, int* nmatvec, void* stream);
+
+/* -------------------------------------------------------------- BLAS-1 -- */
+/* tensor_su2 vector algebra (tensor_su2.cpp:106-260, 324-357, 663-685) on
+ * packed device vectors of n doubles.  Reductions are deterministic. */
+int su2g_vec_dot(const double* x, const double* y, int64_t n, double* result, void* stream);
+int su2g_vec_axpy(double alpha, const double* x, double* y, int64_t n, void* stream);
+int su2g_vec_scale(double alpha, double* x, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SU2G_H */

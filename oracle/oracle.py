@@ -1,0 +1,384 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY.
+
+Python side of the CPU oracle: loads oracle/liboracle.so (the C restatement of
+the reference hot path, su2_oracle.c) and offers numpy-level helpers.  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module; the GPU library never does.
+
+Block tensors use the reference checkpoint layout (dmrg_su2_omp.cpp:864-941):
+``desc`` = [nbond, locspin, {dir, n, angm..., dim...} per leg], ``flag`` = one
+int per block (mixed radix, leg 0 fastest), ``data`` = present blocks packed in
+block order, each column-major.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+MAX_ANGM = 25  # dmrg_su2.cpp:46
+
+_lib = None
+
+
+def build() -> str:
+    """Compile liboracle.so (gcc, a second or two)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def _capsule_ptr(capsule) -> int:
+    get_name = ctypes.pythonapi.PyCapsule_GetName
+    get_name.restype = ctypes.c_char_p
+    get_name.argtypes = [ctypes.py_object]
+    get_ptr = ctypes.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype = ctypes.c_void_p
+    get_ptr.argtypes = [ctypes.py_object, ctypes.c_char_p]
+    return get_ptr(capsule, get_name(capsule))
+
+
+def lib():
+    """The loaded oracle library, with SciPy's BLAS dgemm installed."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        import scipy.linalg.cython_blas as cb
+
+        L.or_set_dgemm(ctypes.c_void_p(_capsule_ptr(cb.__pyx_capi__["dgemm"])))
+        L.or_factorial.restype = ctypes.c_double
+        L.or_offsets.restype = ctypes.c_int64
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_blas_threads(n: int) -> None:
+    """Best effort: pin SciPy's bundled OpenBLAS to n threads (the oracle
+    parallelises above BLAS)."""
+    try:
+        import glob
+
+        import scipy
+
+        d = os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs")
+        for so in glob.glob(os.path.join(d, "libscipy_openblas*.so")):
+            ob = ctypes.CDLL(so)
+            for name in ("scipy_openblas_set_num_threads", "openblas_set_num_threads"):
+                if hasattr(ob, name):
+                    getattr(ob, name)(int(n))
+                    return
+    except OSError:
+        pass
+
+
+# --------------------------------------------------------------------------
+# structures
+# --------------------------------------------------------------------------
+@dataclass
+class Bond:
+    """su2bond (su2bond.hpp:3-29): direction, 2j per sector, multiplet dims."""
+
+    dir: int
+    angm: list
+    dim: list
+
+    def inverted(self) -> "Bond":
+        return Bond(-self.dir, list(self.angm), list(self.dim))
+
+
+@dataclass
+class Struct:
+    """su2struct (su2struct.hpp:4-40) plus the block presence flags."""
+
+    bonds: list
+    locspin: int = 0
+    flag: np.ndarray = field(default=None)
+
+    def desc(self) -> np.ndarray:
+        d = [len(self.bonds), self.locspin]
+        for b in self.bonds:
+            d += [b.dir, len(b.angm)] + list(b.angm) + list(b.dim)
+        return np.asarray(d, dtype=np.int32)
+
+    @property
+    def nten(self) -> int:
+        n = 1
+        for b in self.bonds:
+            n *= len(b.angm)
+        return n
+
+    def legal(self) -> np.ndarray:
+        out = np.zeros(self.nten, dtype=np.int32)
+        lib().or_legal_blocks(_p(self.desc()), _p(out))
+        return out
+
+    def with_legal_flags(self) -> "Struct":
+        self.flag = self.legal()
+        return self
+
+    def offsets(self):
+        off = np.zeros(self.nten, dtype=np.int64)
+        total = lib().or_offsets(_p(self.desc()), _p(self.flag.astype(np.int32)), _p(off))
+        return off, int(total)
+
+    def block_shape(self, idx: int):
+        shp = []
+        for b in self.bonds:
+            shp.append(b.dim[idx % len(b.angm)])
+            idx //= len(b.angm)
+        return tuple(shp)
+
+    def block_angm(self, idx: int):
+        out = []
+        for b in self.bonds:
+            out.append(b.angm[idx % len(b.angm)])
+            idx //= len(b.angm)
+        return tuple(out)
+
+
+def fuse(b1: Bond, b2: Bond) -> Bond:
+    """su2bond::fuse (su2bond.cpp:155-210): direction of the result is -b1.dir."""
+    aout = np.zeros(128, np.int32)
+    dout = np.zeros(128, np.int32)
+    a1 = np.asarray(b1.angm, np.int32)
+    d1 = np.asarray(b1.dim, np.int32)
+    a2 = np.asarray(b2.angm, np.int32)
+    d2 = np.asarray(b2.dim, np.int32)
+    n = lib().or_fuse(len(a1), _p(a1), _p(d1), len(a2), _p(a2), _p(d2), _p(aout), _p(dout))
+    return Bond(-b1.dir, aout[:n].tolist(), dout[:n].tolist())
+
+
+# --------------------------------------------------------------------------
+# tables
+# --------------------------------------------------------------------------
+def fac_hamilt_vec(max_angm: int = MAX_ANGM) -> np.ndarray:
+    out = np.zeros(max_angm**3, dtype=np.float64)
+    lib().or_fac_hamilt_vec(max_angm, _p(out))
+    return out.reshape(max_angm, max_angm, max_angm)
+
+
+def make_cgc(j1: int, j2: int, j3: int) -> np.ndarray:
+    out = np.zeros((j1 + 1) * (j2 + 1) * (j3 + 1), dtype=np.float64)
+    lib().or_make_cgc(j1, j2, j3, _p(out))
+    return out
+
+
+_FAC = None
+
+
+def fac_table() -> np.ndarray:
+    global _FAC
+    if _FAC is None:
+        _FAC = np.ascontiguousarray(fac_hamilt_vec(MAX_ANGM).ravel())
+    return _FAC
+
+
+# --------------------------------------------------------------------------
+# H_eff pieces
+# --------------------------------------------------------------------------
+def heff_term(vs: Struct, vx, s1: Struct, x1, s2: Struct, x2, ys: Struct, y, coef=1.0) -> None:
+    """y += coef * hamiltonian_vector_multiplication(vec, op1, op2)."""
+    fac = fac_table()
+    rc = lib().or_heff_term(
+        _p(vs.desc()), _p(vs.flag.astype(np.int32)), _p(vx),
+        _p(s1.desc()), _p(s1.flag.astype(np.int32)), _p(x1),
+        _p(s2.desc()), _p(s2.flag.astype(np.int32)), _p(x2),
+        _p(ys.desc()), _p(ys.flag.astype(np.int32)), _p(y),
+        ctypes.c_double(coef), _p(fac), MAX_ANGM)
+    if rc != 0:
+        raise RuntimeError(f"or_heff_term failed: {rc}")
+
+
+def heff_spin0(side: int, hs: Struct, hx, vs: Struct, vx, ys: Struct, y, coef=1.0) -> None:
+    """y += coef * (H^T vec) for side 0, y += coef * (vec H) for side 1."""
+    rc = lib().or_heff_spin0(
+        side, _p(hs.desc()), _p(hs.flag.astype(np.int32)), _p(hx),
+        _p(vs.desc()), _p(vs.flag.astype(np.int32)), _p(vx),
+        _p(ys.desc()), _p(ys.flag.astype(np.int32)), _p(y), ctypes.c_double(coef))
+    if rc != 0:
+        raise RuntimeError(f"or_heff_spin0 failed: {rc}")
+
+
+@dataclass
+class HeffProblem:
+    """One effective-Hamiltonian application: y = H_L^T psi + psi H_R
+    + sum_t coef_t * [L_t psi R_t] (the orchestration of dmrg_su2.cpp:543-664
+    with the complementary operators already combined)."""
+
+    psi: Struct
+    terms: list  # [(Struct op1, data1, Struct op2, data2, coef)]
+    hl: tuple = None  # (Struct, data[, coef]) or None
+    hr: tuple = None
+
+
+def heff_apply(prob: HeffProblem, psi: np.ndarray) -> np.ndarray:
+    y = np.zeros_like(psi)
+    for side, h in ((0, prob.hl), (1, prob.hr)):
+        if h is not None:
+            coef = h[2] if len(h) > 2 else 1.0
+            heff_spin0(side, h[0], h[1], prob.psi, psi, prob.psi, y, coef)
+    for (s1, x1, s2, x2, c) in prob.terms:
+        heff_term(prob.psi, psi, s1, x1, s2, x2, prob.psi, y, c)
+    return y
+
+
+def heff_flops(prob: HeffProblem) -> float:
+    """Algorithmic FLOPs of one application: 2*a*b*(m_s c) for step1 and
+    2*c*(b m_s)*d for the second product, per contributing block pair, plus
+    2*d^3-type products for the spin-0 terms."""
+    fac = fac_table().reshape(MAX_ANGM, MAX_ANGM, MAX_ANGM)
+    ps = prob.psi
+    total = 0.0
+    vblocks = [i for i in range(ps.nten) if ps.flag[i]]
+    for (s1, _x1, s2, _x2, _c) in prob.terms:
+        for k in vblocks:
+            ja, jb = ps.block_angm(k)
+            a, b = ps.block_shape(k)
+            for j in range(s1.nten):
+                if not s1.flag[j]:
+                    continue
+                a1 = s1.block_angm(j)
+                if a1[0] != ja:
+                    continue
+                _, ms, c = s1.block_shape(j)
+                used = False
+                for l in range(s2.nten):
+                    if not s2.flag[l]:
+                        continue
+                    a3 = s2.block_angm(l)
+                    if a3[0] != jb or a3[1] != a1[1] or a3[2] != a1[2]:
+                        continue
+                    if abs(fac[a1[0], a1[1], a1[2]]) < 1e-12:
+                        continue
+                    d = s2.block_shape(l)[2]
+                    total += 2.0 * c * (b * ms) * d
+                    used = True
+                if used:
+                    total += 2.0 * a * b * ms * c
+    for side, h in ((0, prob.hl), (1, prob.hr)):
+        if h is None:
+            continue
+        for k in vblocks:
+            a, b = ps.block_shape(k)
+            total += 2.0 * a * b * (a if side == 0 else b)
+    return total
+
+
+# --------------------------------------------------------------------------
+# Lanczos (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195)
+# --------------------------------------------------------------------------
+def _tridiag(aal, nnl, m):
+    from scipy.linalg import eigh_tridiagonal
+
+    d = np.asarray(aal[:m], float)
+    e = np.asarray(nnl[1:m], float)
+    if m == 1:
+        return d.copy(), np.ones((1, 1))
+    return eigh_tridiagonal(d, e)
+
+
+def lanczos1(matvec, psi: np.ndarray, mlanc: int = 5):
+    """Restatement of lanczos_su2::lanczos1 with the start-vector
+    normalisation of initialize_lanczos (lanczos_su2.cpp:36-47) and the mlanc
+    clamp of dmrg_su2.cpp:532.  Returns (eigenvalue, eigenvector, nmatvec)."""
+    n = psi.size
+    if mlanc > n:
+        mlanc = n + 1
+    tol = 1.0e-6
+    nmv = [0]
+
+    def H(v):
+        nmv[0] += 1
+        return matvec(v)
+
+    ff = [None] * (mlanc + 1)
+    ff[0] = psi / np.sqrt(psi @ psi)
+    aal = np.zeros(mlanc)
+    nnl = np.zeros(mlanc + 1)
+
+    def vout_of(z, m):
+        v = ff[0] * z[0]
+        for j in range(1, m):
+            v = v + ff[j] * z[j]
+        return v
+
+    def check(v):
+        v = v / np.sqrt(v @ v)
+        hv = H(v)
+        prod = np.sqrt(hv @ hv)
+        return v, prod, abs((hv @ v) / prod)
+
+    ff[1] = H(ff[0])
+    aal[0] = ff[0] @ ff[1]
+    ff[1] = ff[1] - aal[0] * ff[0]
+    nnl[1] = np.sqrt(ff[1] @ ff[1])
+    ff[1] = ff[1] / nnl[1]
+    if mlanc == 2:
+        if nnl[1] < tol:
+            w, z = _tridiag(aal, nnl, 1)
+            return w[0], vout_of(z[:, 0], 1), nmv[0]
+        ff[2] = H(ff[1])
+        aal[1] = ff[1] @ ff[2]
+        w, z = _tridiag(aal, nnl, 2)
+        return w[0], vout_of(z[:, 0], 2), nmv[0]
+    for m in range(2, mlanc):
+        ff[m] = H(ff[m - 1])
+        aal[m - 1] = ff[m - 1] @ ff[m]
+        ff[m] = ff[m] - aal[m - 1] * ff[m - 1]
+        ff[m] = ff[m] - nnl[m - 1] * ff[m - 2]
+        for j in range(m):
+            q = ff[m] @ ff[j]
+            ff[m] = ff[m] - q * ff[j]
+        nnl[m] = np.sqrt(ff[m] @ ff[m])
+        ff[m] = ff[m] / nnl[m]
+        w, z = _tridiag(aal, nnl, m)
+        if nnl[m] < tol:
+            v, _, _ = check(vout_of(z[:, 0], m))
+            return w[0], v, nmv[0]
+        if m % 4 == 0:
+            v, _, ov = check(vout_of(z[:, 0], m))
+            if abs(ov - 1.0) < 1.0e-8:
+                return w[0], v, nmv[0]
+    ff[mlanc] = H(ff[mlanc - 1])
+    aal[mlanc - 1] = ff[mlanc - 1] @ ff[mlanc]
+    w, z = _tridiag(aal, nnl, mlanc)
+    v, _, _ = check(vout_of(z[:, 0], mlanc))
+    return w[0], v, nmv[0]
+
+
+def struct_from_desc(desc, flag=None) -> Struct:
+    """Struct from the int desc array ([nbond, locspin, {dir, n, angm, dim}...])."""
+    d = [int(v) for v in desc]
+    nb, loc, p = d[0], d[1], 2
+    bonds = []
+    for _ in range(nb):
+        dr, n = d[p], d[p + 1]
+        bonds.append(Bond(dr, d[p + 2: p + 2 + n], d[p + 2 + n: p + 2 + 2 * n]))
+        p += 2 + 2 * n
+    s = Struct(bonds, loc)
+    s.flag = np.asarray(flag, np.int32) if flag is not None else s.legal()
+    return s
+
+
+def to_layout(src: Struct, x: np.ndarray, dst: Struct) -> np.ndarray:
+    """Re-pack block data of src's layout into dst's layout (same block space);
+    blocks absent from src become zeros, blocks absent from dst are dropped
+    (they must be zero for the caller's comparison to be meaningful)."""
+    so, _ = src.offsets()
+    do, dt = dst.offsets()
+    out = np.zeros(dt)
+    for i in range(dst.nten):
+        if dst.flag[i] and src.flag[i]:
+            n = int(np.prod(dst.block_shape(i)))
+            out[do[i]: do[i] + n] = x[so[i]: so[i] + n]
+    return out

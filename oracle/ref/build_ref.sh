@@ -1,0 +1,45 @@
+#!/usr/bin/env bash
+# ORACLE / TEST INFRASTRUCTURE ONLY.
+#
+# Builds the reference SU2DMRG (C++/OpenMP) from its own sources into
+# oracle/_ref/:
+#   oracle/_ref/main_omp       the reference driver, unmodified apart from the
+#                              missing-return patch (patch_ref.py)
+#   oracle/_ref/libsu2ref.so   the reference objects + harness.cpp, a C entry
+#                              layer used to generate golden fixtures
+# Sources are copied to a scratch directory under /tmp and patched there; the
+# reference tree is never written and no reference source enters the repo.
+# BLAS/LAPACK come from SciPy's bundled OpenBLAS (blas_shim.c), the Fortran
+# helpers from ../fhelpers.c, and mkl.h/mpi.h from shim/.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REPO="$(cd "$HERE/../.." && pwd)"
+SRC="${SU2REF_SRC:-/root/reference}"
+OUT="$REPO/oracle/_ref"
+if [ ! -f "$SRC/tensor_su2.cpp" ]; then
+  echo "build_ref.sh: reference sources not found at $SRC" >&2
+  exit 2
+fi
+WORK="$(mktemp -d /tmp/su2ref.XXXXXX)"
+trap 'rm -rf "$WORK"' EXIT
+cp "$SRC"/*.cpp "$SRC"/*.hpp "$WORK"/
+python3 "$HERE/patch_ref.py" "$WORK"
+OPENBLAS="$(python3 -c 'import scipy,os,glob; d=os.path.join(os.path.dirname(scipy.__file__),"..","scipy.libs"); print(os.path.realpath(sorted(glob.glob(os.path.join(d,"libscipy_openblas*.so")))[0]))')"
+OBDIR="$(dirname "$OPENBLAS")"
+mkdir -p "$OUT"
+CXXFLAGS="-O2 -fopenmp -fPIC -w -I$HERE/shim -I$WORK"
+OBJS=()
+for f in tensor tensor_dmrg_src tensor_su2 tensor_su2_dmrg_src tensor_su2_hamiltonian \
+         su2bond su2struct dmrg_su2 dmrg_su2_omp lanczos_su2; do
+  g++ $CXXFLAGS -c "$WORK/$f.cpp" -o "$WORK/$f.o" &
+  OBJS+=("$WORK/$f.o")
+done
+g++ $CXXFLAGS -c "$WORK/main_omp.cpp" -o "$WORK/main_omp.o" &
+g++ $CXXFLAGS -c "$HERE/harness.cpp" -o "$WORK/harness.o" &
+gcc -O2 -fPIC -c "$REPO/oracle/fhelpers.c" -o "$WORK/fhelpers.o" &
+gcc -O2 -fPIC -c "$HERE/blas_shim.c" -o "$WORK/blas_shim.o" &
+for job in $(jobs -p); do wait "$job"; done
+LIBS=("$WORK/fhelpers.o" "$WORK/blas_shim.o" "$OPENBLAS" -Wl,-rpath,"$OBDIR" -fopenmp)
+g++ -o "$OUT/main_omp" "$WORK/main_omp.o" "${OBJS[@]}" "${LIBS[@]}"
+g++ -shared -o "$OUT/libsu2ref.so" "$WORK/harness.o" "${OBJS[@]}" "${LIBS[@]}"
+echo "built $OUT/main_omp and $OUT/libsu2ref.so"

@@ -1,0 +1,199 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// A C entry layer over the reference's own objects, linked into
+// oracle/_ref/libsu2ref.so by build_ref.sh.  It exists to produce golden
+// fixtures (tests/golden/gen_golden.py) from the reference itself:
+//   * the recoupling table fac_hamilt_vec (dmrg_su2.cpp:759-775),
+//   * tensor_su2::hamiltonian_vector_multiplication on given block tensors
+//     (tensor_su2_dmrg_src.cpp:893-1041),
+//   * tensor_su2::contract for the spin-0 block-Hamiltonian terms
+//     (tensor_su2.cpp:1255-1345, used at dmrg_su2.cpp:563-570),
+//   * whole DMRG runs (do_idmrg + sweep, as main_omp.cpp:158-202 drives them).
+// Block tensors cross this boundary in the reference's own checkpoint layout
+// (dmrg_su2_omp.cpp:864-941): a presence flag per block, then the reduced
+// blocks in mixed-radix block order (leg 0 fastest), each column-major.
+// The structure travels as an int "desc":
+//   [nbond, locspin, {dir, n, angm[0..n), dim[0..n)} per leg].
+#include <omp.h>
+#include <mkl.h>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#define private public
+#include "dmrg_su2_omp.hpp"
+#undef private
+
+// Globals that main_omp.cpp:15-24 defines (main_omp.o is not linked here).
+int max_dcut = 8000, myrank = 0, myrk, psize = 12, mkl = 1, comm_rank = 0, comm_size, thread,
+    bdry = 2, jobid, memory_flag = 0;
+double delta = 0, qdelta = 1, alpha, tau;
+double t1, t2, preparetime = 0, svdtime = 0, lanczostime = 0;
+dmrg_su2* chain_ptr;
+tensor ***spin_op, ***cgc_coef_left, ***cgc_coef_rght, *cgc_coef_singlet, *identity;
+double **spin_op_trace, *****fac_operator_onsite_left, *****fac_operator_onsite_rght,
+    ******fac_operator_transformation_left, ******fac_operator_transformation_rght,
+    *****fac_operator_pairup_left, *****fac_operator_pairup_rght, ***fac_hamilt_vec,
+    *****fac_permutation_left, *****fac_permutation_rght, *fac_betadouble, *fac_comp_left,
+    *fac_comp_rght, *fac_init_left, *fac_init_rght;
+double cosk, coskminus;
+double pi = M_PI;
+double pi2 = pi * 2;
+int nkrylov = 0, disk = 0;
+
+namespace {
+dmrg_su2* g_tables = nullptr;  // owner of the recoupling tables
+tensor_su2 g_result;           // last result, read back by ref_result_*
+
+void desc_to_struct(const int* desc, su2struct& s) {
+  int nb = desc[0], locspin = desc[1], p = 2;
+  std::vector<su2bond> bb(nb);
+  for (int l = 0; l < nb; ++l) {
+    int dir = desc[p], n = desc[p + 1];
+    std::vector<int> ang(desc + p + 2, desc + p + 2 + n), dim(desc + p + 2 + n, desc + p + 2 + 2 * n);
+    bb[l].set_su2bond(n, dir, ang.data(), dim.data());
+    p += 2 + 2 * n;
+  }
+  s.set_su2struct(nb, locspin, bb.data());
+}
+
+// Builds a tensor_su2 from reduced blocks; the CG part of every block is the
+// canonical one the engine uses: make_cgc(a0,a1,a2) for 3-leg tensors, the
+// singlet for 2-leg vectors (dirs -1,-1), the identity for 2-leg scalar
+// operators (dirs +1,-1).
+void build_tensor(tensor_su2& t, const int* desc, const int* flag, const double* data) {
+  su2struct s;
+  desc_to_struct(desc, s);
+  int nb = s.get_nbond(), nten = s.get_nten();
+  std::vector<int> angm(nb), bdim(nb), cdim(nb);
+  std::vector<double> cg;
+  for (int i = 0; i < nten; ++i) {
+    if (!flag[i]) continue;
+    s.get_tensor_argument(i, angm.data(), bdim.data(), cdim.data());
+    tensor c;
+    if (nb == 3) c.make_cgc(angm[0], angm[1], angm[2]);
+    else if (s.get_bonddir(0) == 1) c.make_identity(angm[0]);
+    else c.make_singlet(angm[0]);
+    for (int e = 0; e < c.get_nelement(); ++e) cg.push_back(c.get_telement(e));
+  }
+  std::vector<int> f(flag, flag + nten);
+  t.set_tensor_su2(s, const_cast<double*>(data), cg.data(), f.data());
+}
+}  // namespace
+
+extern "C" {
+
+// Recoupling tables for 2j < max_angm, built exactly as the engine builds them.
+int ref_setup(int nthreads, int max_angm) {
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  if (!g_tables) {
+    g_tables = new dmrg_su2();
+    g_tables->physpn = 1;
+    g_tables->makeup_clebsch_gordan_coefficient_tensors(max_angm);
+  }
+  return 0;
+}
+
+void ref_fac_hamilt_vec(int max_angm, double* out) {
+  for (int i = 0; i < max_angm; ++i)
+    for (int j = 0; j < max_angm; ++j)
+      for (int k = 0; k < max_angm; ++k) out[(i * max_angm + j) * max_angm + k] = fac_hamilt_vec[i][j][k];
+}
+
+void ref_make_cgc(int j1, int j2, int j3, double* out) {
+  tensor c;
+  c.make_cgc(j1, j2, j3);
+  for (int e = 0; e < c.get_nelement(); ++e) out[e] = c.get_telement(e);
+}
+
+// result = hamiltonian_vector_multiplication(vec, op1, op2)
+int ref_heff_term(const int* vd, const int* vf, const double* vx, const int* d1, const int* f1,
+                  const double* x1, const int* d2, const int* f2, const double* x2) {
+  tensor_su2 vec, op1, op2;
+  build_tensor(vec, vd, vf, vx);
+  build_tensor(op1, d1, f1, x1);
+  build_tensor(op2, d2, f2, x2);
+  g_result.hamiltonian_vector_multiplication(vec, op1, op2);
+  return g_result.get_nten();
+}
+
+// result = contract(t1, i1, t2, i2)
+int ref_contract(const int* da, const int* fa, const double* xa, int ia, const int* db, const int* fb,
+                 const double* xb, int ib) {
+  tensor_su2 a, b;
+  build_tensor(a, da, fa, xa);
+  build_tensor(b, db, fb, xb);
+  g_result.contract(a, ia, b, ib);
+  return g_result.get_nten();
+}
+
+void ref_result_sizes(int* nten, int* nele1, int* nele2) {
+  *nten = g_result.get_nten();
+  g_result.get_nelement(*nele1, *nele2);
+}
+
+void ref_result_get(int* flag, double* tele1, double* tele2) { g_result.get_telement(tele1, tele2, flag); }
+
+// su2bond::fuse (su2bond.cpp:155-210); returns the sector count
+int ref_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, const int* d2, int* aout, int* dout) {
+  std::vector<int> x1(a1, a1 + n1), y1(d1, d1 + n1), x2(a2, a2 + n2), y2(d2, d2 + n2);
+  su2bond b1, b2, f;
+  b1.set_su2bond(n1, 1, x1.data(), y1.data());
+  b2.set_su2bond(n2, 1, x2.data(), y2.data());
+  f.fuse(b1, b2);
+  for (int i = 0; i < f.get_nmoment(); ++i) {
+    aout[i] = f.get_angularmoment(i);
+    dout[i] = f.get_bonddim(i);
+  }
+  return f.get_nmoment();
+}
+
+// su2struct::get_tensor_argument legality of every block
+int ref_legal(const int* desc, int* legal) {
+  su2struct s;
+  desc_to_struct(desc, s);
+  int nb = s.get_nbond();
+  std::vector<int> angm(nb), bdim(nb), cdim(nb);
+  for (int i = 0; i < s.get_nten(); ++i) legal[i] = s.get_tensor_argument(i, angm.data(), bdim.data(), cdim.data());
+  return s.get_nten();
+}
+
+// Runs the reference DMRG the way main_omp.cpp:158-202 does (without its
+// scratch-directory creation) and returns the per-sweep energies E0-1000.
+// Must be called from a scratch working directory: the engine writes its
+// checkpoint files (uu-*, ww-*, enr-*) into the current directory.
+int ref_run_dmrg(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
+                 int nthreads, double* energies) {
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  omp_set_nested(1);
+  omp_set_max_active_levels(2);
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* chain = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = chain;
+  chain->set_ky(0);
+  chain->do_idmrg();
+  double e1 = chain->get_enr();
+  energies[0] = e1;
+  int n = 1;
+  for (int i = 0; i < niter; ++i) {
+    chain->sweep();
+    double e2 = chain->get_enr();
+    energies[n++] = e2;
+    if (fabs(e1 - e2) < 1.e-6) break;
+    e1 = e2;
+  }
+  return n;
+}
+}

@@ -1,0 +1,389 @@
+// C ABI of libsu2g.so (declared in include/su2g.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "heff_plan.hpp"
+#include "kernels.hpp"
+#include "su2_meta.hpp"
+#include "su2g.h"
+#include "tridiag.hpp"
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? SU2G_ENOMEM : SU2G_ECUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define SU2G_CUDA(call)                                 \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+template <class T>
+cudaError_t upload(const std::vector<T>& v, T** dptr) {
+  *dptr = nullptr;
+  if (v.empty()) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)dptr, v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+}  // namespace
+
+struct su2g_heff_plan {
+  su2g::HeffWork work;
+  int mode = SU2G_MODE_F64;
+  su2g::GemmSeg* d_seg1 = nullptr;
+  su2g::GemmSeg* d_seg2 = nullptr;
+  su2g::GemmTile* d_tile1 = nullptr;
+  su2g::GemmTile* d_tile2 = nullptr;
+  double* d_scratch = nullptr;
+  // Lanczos workspace (allocated on first use)
+  double* d_krylov = nullptr;
+  int krylov_vectors = 0;
+  double* d_red = nullptr;
+
+  void release() {
+    cudaFree(d_seg1);
+    cudaFree(d_seg2);
+    cudaFree(d_tile1);
+    cudaFree(d_tile2);
+    cudaFree(d_scratch);
+    cudaFree(d_krylov);
+    cudaFree(d_red);
+    d_seg1 = d_seg2 = nullptr;
+    d_tile1 = d_tile2 = nullptr;
+    d_scratch = d_krylov = d_red = nullptr;
+  }
+};
+
+extern "C" {
+
+int su2g_version(void) { return 100; }
+
+const char* su2g_last_error(void) { return g_err.c_str(); }
+
+int su2g_struct_nten(const int* desc) {
+  su2g::Struct s;
+  std::string e;
+  if (!desc || !s.parse(desc, &e)) return -1;
+  return s.nten;
+}
+
+int su2g_struct_legal(const int* desc, int* legal) {
+  su2g::Struct s;
+  std::string e;
+  if (!desc || !legal || !s.parse(desc, &e)) return -1;
+  for (int i = 0; i < s.nten; ++i) legal[i] = s.legal_block(i) ? 1 : 0;
+  return s.nten;
+}
+
+int64_t su2g_layout(const int* desc, const int* flag, int64_t* offsets) {
+  su2g::Struct s;
+  std::string e;
+  if (!desc || !s.parse(desc, &e)) return -1;
+  s.set_layout(flag);
+  if (offsets) std::copy(s.offset.begin(), s.offset.end(), offsets);
+  return s.total;
+}
+
+int su2g_bond_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, const int* d2, int* nout,
+                   int* aout, int* dout) {
+  if (n1 < 0 || n2 < 0 || !nout || !aout || !dout) return fail(SU2G_EINVAL, "bond_fuse: bad arguments");
+  su2g::Bond b1, b2;
+  b1.angm.assign(a1, a1 + n1);
+  b1.dim.assign(d1, d1 + n1);
+  b2.angm.assign(a2, a2 + n2);
+  b2.dim.assign(d2, d2 + n2);
+  su2g::Bond f = su2g::fuse(b1, b2);
+  if (f.n() > 64) return fail(SU2G_EINVAL, "bond_fuse: more than 64 sectors");
+  *nout = f.n();
+  std::copy(f.angm.begin(), f.angm.end(), aout);
+  std::copy(f.dim.begin(), f.dim.end(), dout);
+  return SU2G_OK;
+}
+
+int su2g_make_cgc(int j1, int j2, int j3, double* out) {
+  if (j1 < 0 || j2 < 0 || j3 < 0 || !out) return fail(SU2G_EINVAL, "make_cgc: bad arguments");
+  su2g::make_cgc(j1, j2, j3, out);
+  return SU2G_OK;
+}
+
+int su2g_fac_hamilt_vec(int max_angm, double* out) {
+  if (max_angm <= 0 || max_angm > 64 || !out) return fail(SU2G_EINVAL, "fac_hamilt_vec: bad arguments");
+  su2g::fac_hamilt_vec(max_angm, out);
+  return SU2G_OK;
+}
+
+int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                          su2g_heff_plan** plan) {
+  if (!plan) return fail(SU2G_EINVAL, "plan_create: null output");
+  *plan = nullptr;
+  if (mode != SU2G_MODE_F64) return fail(SU2G_EUNSUPPORTED, "plan_create: mode not available in this build");
+  su2g_heff_plan* p = new su2g_heff_plan();
+  p->mode = mode;
+  std::string err;
+  int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &p->work, &err);
+  if (rc) {
+    delete p;
+    return fail(rc, err);
+  }
+  cudaError_t e = upload(p->work.seg1, &p->d_seg1);
+  if (e == cudaSuccess) e = upload(p->work.seg2, &p->d_seg2);
+  if (e == cudaSuccess) e = upload(p->work.tile1, &p->d_tile1);
+  if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
+  if (e == cudaSuccess && p->work.scratch_len > 0)
+    e = cudaMalloc((void**)&p->d_scratch, p->work.scratch_len * sizeof(double));
+  if (e != cudaSuccess) {
+    p->release();
+    delete p;
+    return cuda_fail(e, "plan_create");
+  }
+  *plan = p;
+  return SU2G_OK;
+}
+
+int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len, int64_t* scratch_bytes,
+                        int* ntiles) {
+  if (!p) return fail(SU2G_EINVAL, "plan_info: null plan");
+  if (flops) *flops = p->work.flops;
+  if (psi_len) *psi_len = p->work.psi.total;
+  if (scratch_bytes) *scratch_bytes = p->work.scratch_len * (int64_t)sizeof(double);
+  if (ntiles) *ntiles = (int)(p->work.tile1.size() + p->work.tile2.size());
+  return SU2G_OK;
+}
+
+int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* stream) {
+  if (!p) return fail(SU2G_EINVAL, "heff_apply: null plan");
+  if (p->work.psi.total > 0 && (!psi || !y)) return fail(SU2G_EINVAL, "heff_apply: null vector");
+  if (psi == y && psi) return fail(SU2G_EINVAL, "heff_apply: psi and y must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  su2g::Bases b;
+  b.p[su2g::kBufAbs] = 0;
+  b.p[su2g::kBufPsi] = reinterpret_cast<uintptr_t>(psi);
+  b.p[su2g::kBufY] = reinterpret_cast<uintptr_t>(y);
+  b.p[su2g::kBufScratch] = reinterpret_cast<uintptr_t>(p->d_scratch);
+  SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st));
+  SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st));
+  return SU2G_OK;
+}
+
+int su2g_heff_plan_destroy(su2g_heff_plan* p) {
+  if (!p) return SU2G_OK;
+  p->release();
+  delete p;
+  return SU2G_OK;
+}
+
+int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_flag, const double* vec,
+                                           su2g_tensor op1, su2g_tensor op2, double* y, void* stream) {
+  su2g_term term{op1, op2, 1.0};
+  su2g_heff_plan* p = nullptr;
+  int rc = su2g_heff_plan_create(vec_desc, vec_flag, 1, &term, nullptr, 0.0, nullptr, 0.0, SU2G_MODE_F64, &p);
+  if (rc) return rc;
+  rc = su2g_heff_apply(p, vec, y, stream);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  su2g_heff_plan_destroy(p);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "hamiltonian_vector_multiplication");
+  return SU2G_OK;
+}
+
+// ------------------------------------------------------------------ BLAS-1
+int su2g_vec_dot(const double* x, const double* y, int64_t n, double* result, void* stream) {
+  if (!result || n < 0) return fail(SU2G_EINVAL, "vec_dot: bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  double* scratch = nullptr;
+  const int ns = su2g::reduction_scratch_doubles();
+  SU2G_CUDA(cudaMallocAsync((void**)&scratch, ns * sizeof(double), st));
+  cudaError_t e = su2g::launch_dot(x, y, n, scratch, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(result, scratch + ns - 1, sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(scratch, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "vec_dot");
+  return SU2G_OK;
+}
+
+int su2g_vec_axpy(double alpha, const double* x, double* y, int64_t n, void* stream) {
+  if (n < 0) return fail(SU2G_EINVAL, "vec_axpy: bad arguments");
+  SU2G_CUDA(su2g::launch_axpy(alpha, x, y, n, (cudaStream_t)stream));
+  return SU2G_OK;
+}
+
+int su2g_vec_scale(double alpha, double* x, int64_t n, void* stream) {
+  if (n < 0) return fail(SU2G_EINVAL, "vec_scale: bad arguments");
+  SU2G_CUDA(su2g::launch_scale(alpha, x, n, (cudaStream_t)stream));
+  return SU2G_OK;
+}
+
+// ----------------------------------------------------------------- Lanczos
+namespace {
+
+struct LanczosCtx {
+  su2g_heff_plan* p;
+  cudaStream_t st;
+  int64_t n;
+  int nmatvec = 0;
+  double* ff(int i) { return p->d_krylov + (int64_t)i * n; }
+  double* tmp() { return p->d_krylov + (int64_t)(p->krylov_vectors - 1) * n; }
+
+  int dot(const double* x, const double* y, double* out) {
+    const int ns = su2g::reduction_scratch_doubles();
+    cudaError_t e = su2g::launch_dot(x, y, n, p->d_red, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, p->d_red + ns - 1, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "lanczos dot");
+    return SU2G_OK;
+  }
+  int matvec(const double* x, double* y) {
+    ++nmatvec;
+    return su2g_heff_apply(p, x, y, st);
+  }
+  int axpy(double a, const double* x, double* y) {
+    cudaError_t e = su2g::launch_axpy(a, x, y, n, st);
+    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos axpy");
+  }
+  int scale(double a, double* x) {
+    cudaError_t e = su2g::launch_scale(a, x, n, st);
+    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos scale");
+  }
+  int copy(const double* x, double* y) {
+    cudaError_t e = cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos copy");
+  }
+  // vout = sum_j z[j] ff[j]  (lanczos_su2::compute_eigenvector, lanczos_su2.cpp:262-279)
+  int combine(const std::vector<double>& z, int m, double* vout) {
+    int rc = copy(ff(0), vout);
+    if (!rc) rc = scale(z[0], vout);
+    for (int j = 1; j < m && !rc; ++j) rc = axpy(z[j], ff(j), vout);
+    return rc;
+  }
+  // lanczos_su2::check_eigenvector (lanczos_su2.cpp:320-332): normalises v,
+  // returns |Hv| and |<Hv,v>|/|Hv|
+  int check(double* v, double* eig, double* olap) {
+    double nn;
+    int rc = dot(v, v, &nn);
+    if (!rc) rc = scale(1.0 / std::sqrt(nn), v);
+    if (!rc) rc = matvec(v, tmp());
+    double pp = 0, ov = 0;
+    if (!rc) rc = dot(tmp(), tmp(), &pp);
+    if (!rc) rc = dot(tmp(), v, &ov);
+    if (rc) return rc;
+    const double prod = std::sqrt(pp);
+    *eig = prod;
+    *olap = std::fabs(ov / prod);
+    return SU2G_OK;
+  }
+};
+
+}  // namespace
+
+int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int* nmatvec, void* stream) {
+  if (!p || !psi || !energy || mlanc < 2) return fail(SU2G_EINVAL, "lanczos: bad arguments");
+  const int64_t n = p->work.psi.total;
+  if (n <= 0) return fail(SU2G_EINVAL, "lanczos: empty vector");
+  if (mlanc > n) mlanc = (int)n + 1;  // dmrg_su2.cpp:532
+  const int need = mlanc + 2;         // ff[0..mlanc] + one work vector
+  if (p->krylov_vectors < need) {
+    cudaFree(p->d_krylov);
+    p->d_krylov = nullptr;
+    p->krylov_vectors = 0;
+    SU2G_CUDA(cudaMalloc((void**)&p->d_krylov, (size_t)need * n * sizeof(double)));
+    p->krylov_vectors = need;
+  }
+  if (!p->d_red) SU2G_CUDA(cudaMalloc((void**)&p->d_red, su2g::reduction_scratch_doubles() * sizeof(double)));
+  LanczosCtx L{p, (cudaStream_t)stream, n};
+  const double tol = 1.e-6;  // lanczos_su2.cpp:128
+  std::vector<double> aal(mlanc, 0.0), nnl(mlanc + 1, 0.0), eig, z;
+  int rc;
+  auto tridiag = [&](int m) {  // lanczos_su2::diatridiag (lanczos_su2.cpp:237-259)
+    std::vector<double> d(aal.begin(), aal.begin() + m), e(m > 1 ? m - 1 : 0);
+    for (int i = 0; i + 1 < m; ++i) e[i] = nnl[i + 1];
+    su2g::tridiag_eigh(d, e, &eig, &z);
+  };
+  auto finish = [&](int m, bool do_check) -> int {
+    std::vector<double> z0(z.begin(), z.begin() + m);  // ground-state column
+    int r = L.combine(z0, m, psi);
+    if (r) return r;
+    if (do_check) {
+      double ee, ov;
+      r = L.check(psi, &ee, &ov);
+      if (r) return r;
+    }
+    *energy = eig[0];
+    if (nmatvec) *nmatvec = L.nmatvec;
+    cudaError_t e = cudaStreamSynchronize(L.st);
+    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos");
+  };
+
+  // ff[0] = normalised start vector (lanczos_su2.cpp:45-46)
+  if ((rc = L.copy(psi, L.ff(0)))) return rc;
+  double nn;
+  if ((rc = L.dot(L.ff(0), L.ff(0), &nn))) return rc;
+  if ((rc = L.scale(1.0 / std::sqrt(nn), L.ff(0)))) return rc;
+  // first step (lanczos_su2.cpp:136-142)
+  if ((rc = L.matvec(L.ff(0), L.ff(1)))) return rc;
+  if ((rc = L.dot(L.ff(0), L.ff(1), &aal[0]))) return rc;
+  if ((rc = L.axpy(-aal[0], L.ff(0), L.ff(1)))) return rc;
+  if ((rc = L.dot(L.ff(1), L.ff(1), &nn))) return rc;
+  nnl[1] = std::sqrt(nn);
+  if ((rc = L.scale(1.0 / nnl[1], L.ff(1)))) return rc;
+  if (mlanc == 2) {  // lanczos_su2.cpp:143-154
+    if (nnl[1] < tol) {
+      tridiag(1);
+      return finish(1, false);
+    }
+    if ((rc = L.matvec(L.ff(1), L.ff(2)))) return rc;
+    if ((rc = L.dot(L.ff(1), L.ff(2), &aal[1]))) return rc;
+    tridiag(2);
+    return finish(2, false);
+  }
+  for (int m = 2; m < mlanc; ++m) {  // lanczos_su2.cpp:155-188
+    if ((rc = L.matvec(L.ff(m - 1), L.ff(m)))) return rc;
+    if ((rc = L.dot(L.ff(m - 1), L.ff(m), &aal[m - 1]))) return rc;
+    if ((rc = L.axpy(-aal[m - 1], L.ff(m - 1), L.ff(m)))) return rc;
+    if ((rc = L.axpy(-nnl[m - 1], L.ff(m - 2), L.ff(m)))) return rc;
+    for (int j = 0; j < m; ++j) {  // full reorthogonalisation
+      double q;
+      if ((rc = L.dot(L.ff(m), L.ff(j), &q))) return rc;
+      if ((rc = L.axpy(-q, L.ff(j), L.ff(m)))) return rc;
+    }
+    if ((rc = L.dot(L.ff(m), L.ff(m), &nn))) return rc;
+    nnl[m] = std::sqrt(nn);
+    if ((rc = L.scale(1.0 / nnl[m], L.ff(m)))) return rc;
+    tridiag(m);
+    if (nnl[m] < tol) return finish(m, true);
+    if (m % 4 == 0) {
+      std::vector<double> z0(z.begin(), z.begin() + m);
+      if ((rc = L.combine(z0, m, psi))) return rc;
+      double ee, ov;
+      if ((rc = L.check(psi, &ee, &ov))) return rc;
+      if (std::fabs(ov - 1.) < 1.e-8) {
+        *energy = eig[0];
+        if (nmatvec) *nmatvec = L.nmatvec;
+        SU2G_CUDA(cudaStreamSynchronize(L.st));
+        return SU2G_OK;
+      }
+    }
+  }
+  // final step (lanczos_su2.cpp:189-194)
+  if ((rc = L.matvec(L.ff(mlanc - 1), L.ff(mlanc)))) return rc;
+  if ((rc = L.dot(L.ff(mlanc - 1), L.ff(mlanc), &aal[mlanc - 1]))) return rc;
+  tridiag(mlanc);
+  return finish(mlanc, true);
+}
+
+}  // extern "C"

@@ -1,0 +1,281 @@
+// Host-side construction of the H_eff work list; see heff_plan.hpp.
+#include "heff_plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+namespace su2g {
+namespace {
+
+bool same_sectors(const Bond& a, const Bond& b) { return a.angm == b.angm && a.dim == b.dim; }
+
+struct Op {
+  Struct s;
+  uintptr_t base = 0;  // device address of the packed data
+};
+
+int parse_tensor(const su2g_tensor& t, int want_legs, Op* op, const char* what, std::string* err) {
+  if (!t.desc) {
+    *err = std::string(what) + ": missing desc";
+    return SU2G_EINVAL;
+  }
+  std::string e;
+  if (!op->s.parse(t.desc, &e)) {
+    *err = std::string(what) + ": " + e;
+    return SU2G_EINVAL;
+  }
+  if (op->s.nbond != want_legs) {
+    *err = std::string(what) + ": wrong number of legs";
+    return SU2G_EINVAL;
+  }
+  op->s.set_layout(t.flag);
+  if (op->s.total > 0 && !t.data) {
+    *err = std::string(what) + ": missing data pointer";
+    return SU2G_EINVAL;
+  }
+  op->base = reinterpret_cast<uintptr_t>(t.data);
+  if (op->base % 8 != 0) {
+    *err = std::string(what) + ": data not 8-byte aligned";
+    return SU2G_EINVAL;
+  }
+  return SU2G_OK;
+}
+
+void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int c_buf, int ldc, int M, int N, int seg0, int nseg,
+               int64_t kwork) {
+  for (int m0 = 0; m0 < M; m0 += kTileM)
+    for (int n0 = 0; n0 < N; n0 += kTileN) {
+      GemmTile t;
+      t.c = c_off;
+      t.c_buf = c_buf;
+      t.ldc = ldc;
+      t.m0 = m0;
+      t.n0 = n0;
+      t.mlen = std::min(kTileM, M - m0);
+      t.nlen = std::min(kTileN, N - n0);
+      t.seg0 = seg0;
+      t.nseg = nseg;
+      t.kwork = kwork;
+      tiles.push_back(t);
+    }
+}
+
+int64_t abs_off(uintptr_t base, int64_t elem_off) { return (int64_t)(base / 8) + elem_off; }
+
+}  // namespace
+
+int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                    const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, HeffWork* out,
+                    std::string* err) {
+  HeffWork& w = *out;
+  w = HeffWork();
+  if (!psi_desc) {
+    *err = "psi: missing desc";
+    return SU2G_EINVAL;
+  }
+  if (!w.psi.parse(psi_desc, err)) return SU2G_EINVAL;
+  if (w.psi.nbond != 2 || w.psi.locspin != 0) {
+    *err = "psi must have 2 legs and locspin 0";
+    return SU2G_EINVAL;
+  }
+  w.psi.set_layout(psi_flag);
+  const Struct& P = w.psi;
+  if (nterms < 0 || (nterms > 0 && !terms)) {
+    *err = "bad term list";
+    return SU2G_EINVAL;
+  }
+
+  std::vector<Op> op1(nterms), op2(nterms);
+  for (int t = 0; t < nterms; ++t) {
+    int rc = parse_tensor(terms[t].op1, 3, &op1[t], "op1", err);
+    if (rc) return rc;
+    rc = parse_tensor(terms[t].op2, 3, &op2[t], "op2", err);
+    if (rc) return rc;
+    const Struct &s1 = op1[t].s, &s2 = op2[t].s;
+    // bond checks of tensor_su2_dmrg_src.cpp:908-921 plus the output legs
+    // matching psi (the result is accumulated into psi-shaped vectors)
+    if (!same_sectors(s1.legs[0], P.legs[0]) || s1.legs[0].dir != -P.legs[0].dir ||
+        !same_sectors(s2.legs[0], P.legs[1]) || s2.legs[0].dir != -P.legs[1].dir ||
+        !same_sectors(s1.legs[1], s2.legs[1]) || s1.legs[1].dir != s2.legs[1].dir) {
+      *err = "term " + std::to_string(t) + ": operator bonds do not match psi";
+      return SU2G_EINVAL;
+    }
+    if (!same_sectors(s1.legs[2], P.legs[0]) || s1.legs[2].dir != P.legs[0].dir ||
+        !same_sectors(s2.legs[2], P.legs[1]) || s2.legs[2].dir != P.legs[1].dir) {
+      *err = "term " + std::to_string(t) + ": output legs differ from psi's";
+      return SU2G_EINVAL;
+    }
+  }
+  Op h[2];
+  const su2g_tensor* hs[2] = {hl, hr};
+  for (int side = 0; side < 2; ++side) {
+    if (!hs[side]) continue;
+    int rc = parse_tensor(*hs[side], 2, &h[side], side ? "hr" : "hl", err);
+    if (rc) return rc;
+    const Struct& s = h[side].s;
+    const Bond& pb = P.legs[side];
+    if (!same_sectors(s.legs[0], pb) || s.legs[0].dir != -pb.dir || !same_sectors(s.legs[1], pb) ||
+        s.legs[1].dir != pb.dir) {
+      *err = std::string(side ? "hr" : "hl") + ": bonds do not match psi";
+      return SU2G_EINVAL;
+    }
+  }
+
+  const std::vector<double>& fac = fac_hamilt_vec_table();
+  auto fac_of = [&](int ja, int s, int jc, double* f) -> bool {
+    if (ja >= kMaxAngm || s >= kMaxAngm || jc >= kMaxAngm) return false;
+    *f = fac[(ja * kMaxAngm + s) * kMaxAngm + jc];
+    return true;
+  };
+
+  // ---- phase 1: intermediate blocks T = psi^T op1 ----
+  struct TBlock {
+    int t, k, j;
+    int64_t off;
+    int a, b, ms, c;
+    int ja, jb, s, jc;
+    double fac;
+  };
+  std::vector<TBlock> tb;
+  for (int t = 0; t < nterms; ++t) {
+    const Struct &s1 = op1[t].s, &s2 = op2[t].s;
+    for (int j = 0; j < s1.nten; ++j) {
+      if (!s1.flag[j]) continue;
+      const int ja = s1.block_angm(j, 0), s = s1.block_angm(j, 1), jc = s1.block_angm(j, 2);
+      const int a = s1.block_dim(j, 0), ms = s1.block_dim(j, 1), c = s1.block_dim(j, 2);
+      for (int k = 0; k < P.nten; ++k) {
+        if (!P.flag[k] || P.block_angm(k, 0) != ja) continue;
+        const int jb = P.block_angm(k, 1), b = P.block_dim(k, 1);
+        // does this step1 block reach a stored output block through op2?
+        bool used = false;
+        double f = 0;
+        for (int l = 0; l < s2.nten && !used; ++l) {
+          if (!s2.flag[l] || s2.block_angm(l, 0) != jb || s2.block_angm(l, 1) != s) continue;
+          const int jd = s2.block_angm(l, 2);
+          const int oa[2] = {jc, jd};
+          if (!legal_angm(oa, 2, 0)) continue;
+          if (!fac_of(ja, s, jc, &f)) {
+            *err = "angular momentum beyond the recoupling table (2j >= 25)";
+            return SU2G_EINVAL;
+          }
+          if (std::fabs(f) < 1.e-12) continue;
+          const int sec[2] = {P.legs[0].sector_of(jc), P.legs[1].sector_of(jd)};
+          if (sec[0] < 0 || sec[1] < 0 || !P.flag[P.index(sec)]) {
+            *err = "a term reaches an output block that psi's layout does not store";
+            return SU2G_EINVAL;
+          }
+          used = true;
+        }
+        if (!used) continue;
+        TBlock T{t, k, j, w.scratch_len, a, b, ms, c, ja, jb, s, jc, f};
+        tb.push_back(T);
+        GemmSeg g;
+        g.a = P.offset[k];
+        g.a_buf = kBufPsi;
+        g.b = abs_off(op1[t].base, s1.offset[j]);
+        g.b_buf = kBufAbs;
+        g.lda = a;
+        g.ldb = a;
+        g.K = a;
+        g.transA = 1;
+        g.alpha = 1.0;
+        const int seg0 = (int)w.seg1.size();
+        w.seg1.push_back(g);
+        add_tiles(w.tile1, T.off, kBufScratch, b, b, ms * c, seg0, 1, a);
+        w.scratch_len += (int64_t)b * ms * c;
+        w.flops += 2.0 * a * b * (double)ms * c;
+        w.max_k = std::max<int64_t>(w.max_k, a);
+      }
+    }
+  }
+
+  // ---- phase 2: output blocks ----
+  for (int m = 0; m < P.nten; ++m) {
+    if (!P.flag[m]) continue;
+    const int jc = P.block_angm(m, 0), jd = P.block_angm(m, 1);
+    const int c = P.block_dim(m, 0), d = P.block_dim(m, 1);
+    const int seg0 = (int)w.seg2.size();
+    int64_t kwork = 0;
+    if (hl) {  // Y(jc,jd) += hl_coef * H_L(ja,jc)^T psi(ja,jd)
+      const Struct& s = h[0].s;
+      for (int l = 0; l < s.nten; ++l) {
+        if (!s.flag[l] || s.block_angm(l, 1) != jc) continue;
+        const int ja = s.block_angm(l, 0), a = s.block_dim(l, 0);
+        const int sec[2] = {P.legs[0].sector_of(ja), P.legs[1].sector_of(jd)};
+        if (sec[0] < 0 || !P.flag[P.index(sec)]) continue;
+        const int k = P.index(sec);
+        GemmSeg g;
+        g.a = abs_off(h[0].base, s.offset[l]);
+        g.a_buf = kBufAbs;
+        g.b = P.offset[k];
+        g.b_buf = kBufPsi;
+        g.lda = a;
+        g.ldb = a;
+        g.K = a;
+        g.transA = 1;
+        g.alpha = hl_coef;
+        w.seg2.push_back(g);
+        kwork += a;
+        w.flops += 2.0 * c * (double)a * d;
+        w.max_k = std::max<int64_t>(w.max_k, a);
+      }
+    }
+    if (hr) {  // Y(jc,jd) += hr_coef * psi(jc,jb) H_R(jb,jd)
+      const Struct& s = h[1].s;
+      for (int l = 0; l < s.nten; ++l) {
+        if (!s.flag[l] || s.block_angm(l, 1) != jd) continue;
+        const int jb = s.block_angm(l, 0), b = s.block_dim(l, 0);
+        const int sec[2] = {P.legs[0].sector_of(jc), P.legs[1].sector_of(jb)};
+        if (sec[1] < 0 || !P.flag[P.index(sec)]) continue;
+        const int k = P.index(sec);
+        GemmSeg g;
+        g.a = P.offset[k];
+        g.a_buf = kBufPsi;
+        g.b = abs_off(h[1].base, s.offset[l]);
+        g.b_buf = kBufAbs;
+        g.lda = c;
+        g.ldb = b;
+        g.K = b;
+        g.transA = 0;
+        g.alpha = hr_coef;
+        w.seg2.push_back(g);
+        kwork += b;
+        w.flops += 2.0 * c * (double)b * d;
+        w.max_k = std::max<int64_t>(w.max_k, b);
+      }
+    }
+    // spin-1 (and any other operator-spin) terms, in term order
+    for (const TBlock& T : tb) {
+      if (T.jc != jc) continue;
+      const Struct& s2 = op2[T.t].s;
+      for (int l = 0; l < s2.nten; ++l) {
+        if (!s2.flag[l] || s2.block_angm(l, 0) != T.jb || s2.block_angm(l, 1) != T.s || s2.block_angm(l, 2) != jd)
+          continue;
+        GemmSeg g;
+        g.a = T.off;
+        g.a_buf = kBufScratch;
+        g.b = abs_off(op2[T.t].base, s2.offset[l]);
+        g.b_buf = kBufAbs;
+        g.lda = T.b * T.ms;
+        g.ldb = T.b * T.ms;
+        g.K = T.b * T.ms;
+        g.transA = 1;
+        g.alpha = terms[T.t].coef * T.fac;
+        w.seg2.push_back(g);
+        kwork += g.K;
+        w.flops += 2.0 * c * (double)g.K * d;
+        w.max_k = std::max<int64_t>(w.max_k, g.K);
+      }
+    }
+    add_tiles(w.tile2, P.offset[m], kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
+  }
+
+  // heaviest tiles first: the block scheduler then approximates LPT order
+  auto heavier = [](const GemmTile& x, const GemmTile& y) { return x.kwork > y.kwork; };
+  std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
+  std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
+  return SU2G_OK;
+}
+
+}  // namespace su2g

@@ -1,0 +1,21 @@
+// Launchers of the device kernels (kernels_f64.cu and friends).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gemm_work.hpp"
+
+namespace su2g {
+
+cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
+                            cudaStream_t stream);
+
+// deterministic dot product: partial sums in scratch[0..reduction_scratch_doubles()-1),
+// the result in scratch[reduction_scratch_doubles()-1]
+int reduction_scratch_doubles();
+cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* scratch, cudaStream_t stream);
+cudaError_t launch_axpy(double alpha, const double* x, double* y, int64_t n, cudaStream_t stream);
+cudaError_t launch_scale(double alpha, double* x, int64_t n, cudaStream_t stream);
+
+}  // namespace su2g

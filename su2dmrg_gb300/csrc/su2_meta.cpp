@@ -1,0 +1,205 @@
+// Host-side SU(2) bookkeeping; see su2_meta.hpp for the reference map.
+// Built with -ffp-contract=off: the table arithmetic must not be fused into
+// multiply-adds, so the same operation sequence gives the same bits on every
+// host architecture.
+#include "su2_meta.hpp"
+
+#include <cmath>
+#include <cstdlib>
+#include <mutex>
+
+namespace su2g {
+
+bool Struct::parse(const int* d, std::string* err) {
+  nbond = d[0];
+  locspin = d[1];
+  if (nbond < 1 || nbond > kMaxLegs) {
+    if (err) *err = "nbond out of range";
+    return false;
+  }
+  if (locspin < 0) {
+    if (err) *err = "negative locspin";
+    return false;
+  }
+  int p = 2;
+  nten = 1;
+  for (int l = 0; l < nbond; ++l) {
+    Bond& b = legs[l];
+    b.dir = d[p];
+    int n = d[p + 1];
+    if (n < 1 || n > 64) {
+      if (err) *err = "sector count out of range";
+      return false;
+    }
+    b.angm.assign(d + p + 2, d + p + 2 + n);
+    b.dim.assign(d + p + 2 + n, d + p + 2 + 2 * n);
+    for (int i = 0; i < n; ++i) {
+      if (b.angm[i] < 0 || b.dim[i] < 0 || (i > 0 && b.angm[i] <= b.angm[i - 1])) {
+        if (err) *err = "sector list must be ascending 2j with non-negative dims";
+        return false;
+      }
+    }
+    p += 2 + 2 * n;
+    nten *= n;
+  }
+  return true;
+}
+
+bool legal_angm(const int* angm, int n, int locspin) {
+  if (n == 1) return angm[0] == locspin;  // su2struct.cpp:279-280
+  // sequential fusion of single-sector bonds (su2struct.cpp:281-296)
+  int cur[kFuseCap + 2], nxt[kFuseCap + 2];
+  int ncur = 1;
+  cur[0] = angm[0];
+  for (int l = 1; l < n; ++l) {
+    int nn = 0;
+    for (int i = 0; i < ncur; ++i) {
+      int ks = std::abs(cur[i] - angm[l]), ke = std::abs(cur[i] + angm[l]);
+      if (ke > kFuseCap) ke = kFuseCap;
+      for (int k = ks; k <= ke; k += 2) {
+        bool seen = false;
+        for (int q = 0; q < nn; ++q)
+          if (nxt[q] == k) { seen = true; break; }
+        if (!seen) nxt[nn++] = k;
+      }
+    }
+    ncur = nn;
+    for (int i = 0; i < ncur; ++i) cur[i] = nxt[i];
+  }
+  for (int i = 0; i < ncur; ++i)
+    if (cur[i] == locspin) return true;
+  return false;
+}
+
+bool Struct::legal_block(int idx) const {
+  int sec[kMaxLegs], a[kMaxLegs];
+  sectors(idx, sec);
+  for (int l = 0; l < nbond; ++l) a[l] = legs[l].angm[sec[l]];
+  return legal_angm(a, nbond, locspin);
+}
+
+void Struct::set_layout(const int* flags) {
+  flag.assign(nten, 0);
+  offset.assign(nten, -1);
+  total = 0;
+  int sec[kMaxLegs];
+  for (int i = 0; i < nten; ++i) {
+    flag[i] = flags ? (flags[i] != 0) : (legal_block(i) ? 1 : 0);
+    if (!flag[i]) continue;
+    sectors(i, sec);
+    int64_t sz = 1;
+    for (int l = 0; l < nbond; ++l) sz *= legs[l].dim[sec[l]];
+    offset[i] = total;
+    total += sz;
+  }
+}
+
+Bond fuse(const Bond& b1, const Bond& b2) {
+  Bond out;
+  out.dir = -b1.dir;
+  for (int i = 0; i < b1.n(); ++i)
+    for (int j = 0; j < b2.n(); ++j) {
+      int ks = std::abs(b1.angm[i] - b2.angm[j]), ke = std::abs(b1.angm[i] + b2.angm[j]);
+      if (ke > kFuseCap) ke = kFuseCap;
+      for (int k = ks; k <= ke; k += 2) {
+        int s = out.sector_of(k);
+        if (s >= 0) {
+          out.dim[s] += b1.dim[i] * b2.dim[j];
+        } else {
+          out.angm.push_back(k);
+          out.dim.push_back(b1.dim[i] * b2.dim[j]);
+        }
+      }
+    }
+  // ascending by 2j (keys are distinct, so any correct sort gives isort2_'s order)
+  for (int i = 1; i < out.n(); ++i)
+    for (int j = i; j > 0 && out.angm[j - 1] > out.angm[j]; --j) {
+      std::swap(out.angm[j - 1], out.angm[j]);
+      std::swap(out.dim[j - 1], out.dim[j]);
+    }
+  return out;
+}
+
+double factorial(int n) {
+  double f = 1;
+  if (n == 0 || n == 1) return 1;
+  for (int i = 2; i <= n; ++i) f *= (double)i;
+  return f;
+}
+
+void make_cgc(int j1, int j2, int j3, double* out) {
+  const int n0 = j1 + 1, n1 = j2 + 1, n2 = j3 + 1;
+  for (int i = 0; i < n0 * n1 * n2; ++i) out[i] = 0;
+  const double fac1 = std::sqrt((double)(j3 + 1) * factorial((j3 + j1 - j2) / 2) * factorial((j3 - j1 + j2) / 2) *
+                                factorial((j1 + j2 - j3) / 2) / factorial((j1 + j2 + j3) / 2 + 1));
+  for (int i = 0; i < n0; ++i) {
+    const int m1 = 2 * i - j1;
+    const double f1 = factorial((j1 + m1) / 2) * factorial((j1 - m1) / 2);
+    for (int j = 0; j < n1; ++j) {
+      const int m2 = 2 * j - j2;
+      const double f2 = factorial((j2 + m2) / 2) * factorial((j2 - m2) / 2);
+      for (int k = 0; k < n2; ++k) {
+        const int m3 = 2 * k - j3;
+        if (m1 + m2 - m3 != 0) continue;
+        const double f3 = factorial((j3 + m3) / 2) * factorial((j3 - m3) / 2);
+        const double fac2 = std::sqrt(f1 * f2 * f3);
+        const int k1 = (j1 + j2 - j3) / 2, k2 = (j1 - m1) / 2, k3 = (j2 + m2) / 2;
+        const int k4 = (j3 - j2 + m1) / 2, k5 = (j3 - j1 - m2) / 2, kmax = (j1 + j2 + j3) / 2;
+        double sumk = 0;
+        for (int k0 = 0; k0 <= kmax; ++k0) {
+          if (k1 - k0 >= 0 && k2 - k0 >= 0 && k3 - k0 >= 0 && k4 + k0 >= 0 && k5 + k0 >= 0) {
+            const double sgn = (k0 % 2 == 0) ? 1 : -1;
+            sumk += sgn / (factorial(k0) * factorial(k1 - k0) * factorial(k2 - k0) * factorial(k3 - k0) *
+                           factorial(k4 + k0) * factorial(k5 + k0));
+          }
+        }
+        out[i + j * n0 + k * n0 * n1] = fac1 * fac2 * sumk;
+      }
+    }
+  }
+}
+
+// Singlet entry S_jj[row, m=-m_row] = (-1)^((jj - m_row)/2) / sqrt(jj+1)
+// (tensor.cpp:1339-1347); the integer sign is converted before the divide.
+static inline double singlet_entry(int jj, int row) {
+  const int m = 2 * row - jj;
+  const int sgn = (((jj - m) / 2) % 2 == 0) ? 1 : -1;
+  return sgn / std::sqrt((double)(jj + 1));
+}
+
+void fac_hamilt_vec(int m, double* out) {
+  for (int i = 0; i < m * m * m; ++i) out[i] = 0;
+  std::vector<double> c;
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j)
+      for (int k = 0; k < m; ++k) {
+        if (!(k >= std::abs(i - j) && k <= std::abs(i + j) && (i % 2 == k % 2))) continue;
+        const int n0 = i + 1, n1 = j + 1, n2 = k + 1, ne = n0 * n1 * n2;
+        c.assign(ne, 0.0);
+        make_cgc(i, j, k, c.data());
+        // <C, C contracted with the singlet on every leg> * sqrt(j+1); each
+        // contracted entry is the product chain ((C*S_i)*S_j)*S_k.
+        double prod = 0;
+        for (int e = 0; e < ne; ++e) {
+          const int a = e % n0, b = (e / n0) % n1, cc = e / (n0 * n1);
+          const int abar = n0 - 1 - a, bbar = n1 - 1 - b, cbar = n2 - 1 - cc;
+          double t = c[abar + bbar * n0 + cbar * n0 * n1] * singlet_entry(i, a);
+          t = t * singlet_entry(j, b);
+          t = t * singlet_entry(k, cc);
+          prod += c[e] * t;
+        }
+        out[(i * m + j) * m + k] = prod * std::sqrt((double)(j + 1));
+      }
+}
+
+const std::vector<double>& fac_hamilt_vec_table() {
+  static std::vector<double> table;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    table.assign(kMaxAngm * kMaxAngm * kMaxAngm, 0.0);
+    fac_hamilt_vec(kMaxAngm, table.data());
+  });
+  return table;
+}
+
+}  // namespace su2g

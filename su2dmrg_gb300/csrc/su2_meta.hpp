@@ -1,0 +1,81 @@
+// Host-side SU(2) symmetry bookkeeping: bonds, block structures, block
+// layout, Clebsch-Gordan tensors and recoupling tables.
+//
+// Integer metadata follows the reference exactly (bit-exact by construction):
+//   su2bond::fuse                      su2bond.cpp:155-210 (2j capped at 38)
+//   su2struct block index (mixed radix, leg 0 fastest)  su2struct.cpp:243-302
+//   block legality (sequential fusion contains locspin) su2struct.cpp:305-332
+// FP64 tables follow the reference's operation sequence:
+//   tensor::make_cgc                   tensor.cpp:1353-1407
+//   fac_hamilt_vec                     dmrg_su2.cpp:759-766
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace su2g {
+
+constexpr int kMaxLegs = 4;
+constexpr int kFuseCap = 38;   // su2bond.cpp:177
+constexpr int kMaxAngm = 25;   // dmrg_su2.cpp:46 (tables hold 2j < 25)
+
+struct Bond {
+  int dir = 1;
+  std::vector<int> angm;  // 2j per sector, ascending
+  std::vector<int> dim;   // multiplet count per sector
+  int n() const { return (int)angm.size(); }
+  int sector_of(int a) const {
+    for (int i = 0; i < n(); ++i)
+      if (angm[i] == a) return i;
+    return -1;
+  }
+};
+
+// The block structure of one tensor (su2struct) with its presence flags and
+// the packed layout of the present blocks.
+struct Struct {
+  int nbond = 0, locspin = 0, nten = 0;
+  Bond legs[kMaxLegs];
+  std::vector<int> flag;        // 1 = block stored
+  std::vector<int64_t> offset;  // doubles from the start of the packed data, -1 if absent
+  int64_t total = 0;            // doubles in the packed data
+
+  // desc = [nbond, locspin, {dir, n, angm[n], dim[n]} per leg]
+  bool parse(const int* desc, std::string* err);
+  // flags + offsets; flag == nullptr means "every legal block is present"
+  void set_layout(const int* flags);
+  void sectors(int idx, int* sec) const {
+    for (int l = 0; l < nbond; ++l) {
+      sec[l] = idx % legs[l].n();
+      idx /= legs[l].n();
+    }
+  }
+  int index(const int* sec) const {
+    int i0 = 0;
+    for (int l = nbond - 1; l >= 0; --l) i0 = i0 * legs[l].n() + sec[l];
+    return i0;
+  }
+  bool legal_block(int idx) const;
+  int block_sector(int idx, int leg) const {
+    for (int l = 0; l < leg; ++l) idx /= legs[l].n();
+    return idx % legs[leg].n();
+  }
+  int block_dim(int idx, int leg) const { return legs[leg].dim[block_sector(idx, leg)]; }
+  int block_angm(int idx, int leg) const { return legs[leg].angm[block_sector(idx, leg)]; }
+};
+
+// true when `locspin` is reachable by fusing angm[0..n) left to right
+bool legal_angm(const int* angm, int n, int locspin);
+
+// su2bond::fuse with multiplicities; the result is sorted ascending and has
+// direction -b1.dir (su2bond.cpp:207).
+Bond fuse(const Bond& b1, const Bond& b2);
+
+double factorial(int n);
+void make_cgc(int j1, int j2, int j3, double* out);
+// fac_hamilt_vec[i][j][k] stored at (i*m + j)*m + k, m = max_angm
+void fac_hamilt_vec(int max_angm, double* out);
+// the table for kMaxAngm, computed once and cached
+const std::vector<double>& fac_hamilt_vec_table();
+
+}  // namespace su2g

@@ -1,0 +1,213 @@
+"""Host-side mirror of the reference's SU(2) tensor interface for the hot path.
+
+Names follow the reference so that callers read the same:
+  Su2Bond    ~ su2bond   (su2bond.hpp:3-29)
+  Su2Struct  ~ su2struct (su2struct.hpp:4-40) + the block presence flags
+  HeffPlan   ~ dmrg_su2::hamiltonian_vector_multiplication_idmrg
+               (dmrg_su2.cpp:543-664) with its term list fixed per two-site
+               step; .lanczos() ~ lanczos_su2::lanczos1 (lanczos_su2.cpp:125-195)
+  hamiltonian_vector_multiplication ~ tensor_su2::hamiltonian_vector_multiplication
+               (tensor_su2_dmrg_src.cpp:893-1041)
+All metadata work (legality, layout, fusion) is done by libsu2g.so's host
+entry points; all arithmetic runs on the GPU through the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from .capi import check, lib, ptr, stream_handle
+
+
+@dataclass
+class Su2Bond:
+    dir: int
+    angm: list
+    dim: list
+
+    def inverted(self) -> "Su2Bond":
+        return Su2Bond(-self.dir, list(self.angm), list(self.dim))
+
+    def fuse(self, other: "Su2Bond") -> "Su2Bond":
+        """su2bond::fuse: direction -self.dir, 2j capped at 38."""
+        a1 = np.asarray(self.angm, np.int32)
+        d1 = np.asarray(self.dim, np.int32)
+        a2 = np.asarray(other.angm, np.int32)
+        d2 = np.asarray(other.dim, np.int32)
+        n = ctypes.c_int(0)
+        ao = np.zeros(64, np.int32)
+        do = np.zeros(64, np.int32)
+        check(lib().su2g_bond_fuse(len(a1), ptr(a1), ptr(d1), len(a2), ptr(a2), ptr(d2), ctypes.addressof(n),
+                                   ptr(ao), ptr(do)))
+        return Su2Bond(-self.dir, ao[: n.value].tolist(), do[: n.value].tolist())
+
+
+@dataclass
+class Su2Struct:
+    bonds: list
+    locspin: int = 0
+    flag: np.ndarray = field(default=None)
+
+    def desc(self) -> np.ndarray:
+        d = [len(self.bonds), self.locspin]
+        for b in self.bonds:
+            d += [b.dir, len(b.angm)] + list(b.angm) + list(b.dim)
+        return np.asarray(d, dtype=np.int32)
+
+    @property
+    def nten(self) -> int:
+        n = 1
+        for b in self.bonds:
+            n *= len(b.angm)
+        return n
+
+    def legal(self) -> np.ndarray:
+        out = np.zeros(self.nten, np.int32)
+        n = lib().su2g_struct_legal(ptr(self.desc()), ptr(out))
+        if n < 0:
+            raise capi.Su2gError(capi.SU2G_EINVAL, "malformed structure")
+        return out
+
+    def with_legal_flags(self) -> "Su2Struct":
+        self.flag = self.legal()
+        return self
+
+    def offsets(self):
+        off = np.zeros(self.nten, np.int64)
+        total = lib().su2g_layout(ptr(self.desc()), ptr(np.ascontiguousarray(self.flag, np.int32)), ptr(off))
+        if total < 0:
+            raise capi.Su2gError(capi.SU2G_EINVAL, "malformed structure")
+        return off, int(total)
+
+    def size(self) -> int:
+        return self.offsets()[1]
+
+    def block_angm(self, idx: int):
+        out = []
+        for b in self.bonds:
+            out.append(b.angm[idx % len(b.angm)])
+            idx //= len(b.angm)
+        return tuple(out)
+
+    def block_shape(self, idx: int):
+        out = []
+        for b in self.bonds:
+            out.append(b.dim[idx % len(b.angm)])
+            idx //= len(b.angm)
+        return tuple(out)
+
+    def flag_array(self) -> np.ndarray:
+        return np.ascontiguousarray(self.flag, np.int32)
+
+
+def fac_hamilt_vec(max_angm: int = 25) -> np.ndarray:
+    out = np.zeros(max_angm**3, np.float64)
+    check(lib().su2g_fac_hamilt_vec(max_angm, ptr(out)))
+    return out.reshape(max_angm, max_angm, max_angm)
+
+
+def make_cgc(j1: int, j2: int, j3: int) -> np.ndarray:
+    out = np.zeros((j1 + 1) * (j2 + 1) * (j3 + 1), np.float64)
+    check(lib().su2g_make_cgc(j1, j2, j3, ptr(out)))
+    return out
+
+
+class _Pinned:
+    """Keeps the host arrays a plan was built from alive (the library copies
+    them, but the ctypes structures point at them during creation)."""
+
+    def __init__(self, struct: Su2Struct):
+        self.desc = struct.desc()
+        self.flag = struct.flag_array()
+
+
+def _tensor(struct: Su2Struct, data, keep: list) -> capi.Tensor:
+    p = _Pinned(struct)
+    keep.append(p)
+    return capi.Tensor(ptr(p.desc), ptr(p.flag), ptr(data))
+
+
+class HeffPlan:
+    """Device work list of one effective Hamiltonian (see su2g_heff_plan_create).
+
+    terms: list of (Su2Struct op1, device data1, Su2Struct op2, device data2, coef)
+    hl, hr: (Su2Struct, device data, coef) or None.
+    Device data are torch CUDA tensors (float64) or raw device addresses; they
+    must outlive the plan (the plan holds references to torch tensors).
+    """
+
+    def __init__(self, psi: Su2Struct, terms, hl=None, hr=None, mode: int = capi.MODE_F64):
+        self.psi = psi
+        keep = []
+        self._data_refs = []
+        tarr = (capi.Term * max(1, len(terms)))()
+        for i, (s1, x1, s2, x2, c) in enumerate(terms):
+            tarr[i] = capi.Term(_tensor(s1, x1, keep), _tensor(s2, x2, keep), float(c))
+            self._data_refs += [x1, x2]
+        hl_t = hr_t = None
+        hl_c = hr_c = 0.0
+        if hl is not None:
+            hl_t = _tensor(hl[0], hl[1], keep)
+            hl_c = float(hl[2])
+            self._data_refs.append(hl[1])
+        if hr is not None:
+            hr_t = _tensor(hr[0], hr[1], keep)
+            hr_c = float(hr[2])
+            self._data_refs.append(hr[1])
+        pd = psi.desc()
+        pf = psi.flag_array()
+        handle = ctypes.c_void_p()
+        check(lib().su2g_heff_plan_create(
+            ptr(pd), ptr(pf), len(terms), ctypes.addressof(tarr),
+            ctypes.addressof(hl_t) if hl_t is not None else None, hl_c,
+            ctypes.addressof(hr_t) if hr_t is not None else None, hr_c, int(mode), ctypes.addressof(handle)))
+        self._h = handle
+        self.mode = mode
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        fl = ctypes.c_double()
+        n = ctypes.c_int64()
+        sb = ctypes.c_int64()
+        nt = ctypes.c_int()
+        check(lib().su2g_heff_plan_info(self._h, ctypes.addressof(fl), ctypes.addressof(n), ctypes.addressof(sb),
+                                        ctypes.addressof(nt)))
+        return {"flops": fl.value, "psi_len": n.value, "scratch_bytes": sb.value, "ntiles": nt.value}
+
+    def apply(self, psi, y, stream=None) -> None:
+        check(lib().su2g_heff_apply(self._h, ptr(psi), ptr(y), stream_handle(stream)))
+
+    def lanczos(self, psi, mlanc: int = 5, stream=None):
+        e = ctypes.c_double()
+        nmv = ctypes.c_int()
+        check(lib().su2g_lanczos(self._h, ptr(psi), int(mlanc), ctypes.addressof(e), ctypes.addressof(nmv),
+                                 stream_handle(stream)))
+        return e.value, nmv.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().su2g_heff_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hamiltonian_vector_multiplication(vec: Su2Struct, vec_data, op1: Su2Struct, x1, op2: Su2Struct, x2, y,
+                                      stream=None) -> None:
+    keep = []
+    t1 = _tensor(op1, x1, keep)
+    t2 = _tensor(op2, x2, keep)
+    vd = vec.desc()
+    vf = vec.flag_array()
+    check(lib().su2g_hamiltonian_vector_multiplication(ptr(vd), ptr(vf), ptr(vec_data), t1, t2, ptr(y),
+                                                       stream_handle(stream)))

@@ -1,0 +1,232 @@
+"""Generates the golden fixtures of tests/golden/ from the reference itself.
+
+Runs only where the reference sources exist (they are compiled by
+oracle/ref/build_ref.sh into oracle/_ref/libsu2ref.so); the fixtures it writes
+are committed and are what the tests read on every other machine.
+
+    python oracle/ref/build_ref.sh && python tests/golden/gen_golden.py
+
+Fixtures:
+  fac_hamilt_vec.npy   fac_hamilt_vec[25][25][25] (dmrg_su2.cpp:759-766)
+  cgc.npz              tensor::make_cgc for a spread of (j1,j2,j3)
+  meta.npz             su2bond::fuse and su2struct block legality cases
+  heff_term_*.npz      tensor_su2::hamiltonian_vector_multiplication cases
+  spin0_*.npz          tensor_su2::contract cases of the spin-0 terms
+  dmrg_energies.json   whole reference DMRG runs (E0 - 1000 per sweep)
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REFLIB = os.path.join(REPO, "oracle", "_ref", "libsu2ref.so")
+
+
+def p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def desc_of(bonds, locspin=0):
+    d = [len(bonds), locspin]
+    for (dr, angm, dim) in bonds:
+        d += [dr, len(angm)] + list(angm) + list(dim)
+    return np.asarray(d, np.int32)
+
+
+def nten_of(bonds):
+    n = 1
+    for b in bonds:
+        n *= len(b[1])
+    return n
+
+
+def block_shape(bonds, idx):
+    shp = []
+    for (_, angm, dim) in bonds:
+        shp.append(dim[idx % len(angm)])
+        idx //= len(angm)
+    return shp
+
+
+def random_data(bonds, flag, rng):
+    n = 0
+    for i in range(nten_of(bonds)):
+        if flag[i]:
+            n += int(np.prod(block_shape(bonds, i)))
+    return rng.standard_normal(n)
+
+
+def legal_flags(L, desc):
+    out = np.zeros(4096, np.int32)
+    n = L.ref_legal(p(desc), p(out))
+    return out[:n].copy()
+
+
+def read_result(L):
+    nten = ctypes.c_int()
+    n1 = ctypes.c_int()
+    n2 = ctypes.c_int()
+    L.ref_result_sizes(ctypes.byref(nten), ctypes.byref(n1), ctypes.byref(n2))
+    flag = np.zeros(nten.value, np.int32)
+    x1 = np.zeros(max(1, n1.value))
+    x2 = np.zeros(max(1, n2.value))
+    L.ref_result_get(p(flag), p(x1), p(x2))
+    return flag, x1[: n1.value], x2[: n2.value]
+
+
+def heff_cases(L, rng):
+    cases = []
+    specs = [
+        # (left sectors, right sectors, spin sectors(2j), spin dims, dropout)
+        ([0, 1, 2, 3, 4], [0, 1, 2, 3, 4], [2], [1], 0.0),
+        ([0, 2, 4], [0, 2, 4, 6], [2], [1], 0.0),
+        ([1, 3, 5], [1, 3, 5], [2], [1], 0.25),
+        ([0, 1, 2, 3, 4, 5, 6], [0, 1, 2, 3, 4, 5, 6], [0, 2], [2, 1], 0.2),
+        ([0, 2, 4, 6, 8], [0, 2, 4, 6, 8], [2, 4], [1, 2], 0.1),
+    ]
+    for ci, (la, ra, sa, sd, drop) in enumerate(specs):
+        common = sorted(set(la) & set(ra))
+        ld = [int(rng.integers(1, 7)) for _ in la]
+        rd = [int(rng.integers(1, 7)) for _ in ra]
+        # psi/y legs must carry exactly the sectors the operators map onto
+        EL = (-1, la, ld)
+        ER = (-1, ra, rd)
+        S = (1, sa, sd)
+        vb = [EL, ER]
+        o1b = [(1, la, ld), S, EL]
+        o2b = [(1, ra, rd), S, ER]
+        vdesc, d1, d2 = desc_of(vb), desc_of(o1b), desc_of(o2b)
+        vflag = legal_flags(L, vdesc)
+        f1 = legal_flags(L, d1) * (rng.random(nten_of(o1b)) >= drop)
+        f2 = legal_flags(L, d2) * (rng.random(nten_of(o2b)) >= drop)
+        f1 = f1.astype(np.int32)
+        f2 = f2.astype(np.int32)
+        vx = random_data(vb, vflag, rng)
+        x1 = random_data(o1b, f1, rng)
+        x2 = random_data(o2b, f2, rng)
+        L.ref_heff_term(p(vdesc), p(vflag), p(vx), p(d1), p(f1), p(x1), p(d2), p(f2), p(x2))
+        rflag, rx, rcg = read_result(L)
+        cases.append(dict(name=f"heff_term_{ci}", vdesc=vdesc, vflag=vflag, vx=vx, d1=d1, f1=f1, x1=x1, d2=d2,
+                          f2=f2, x2=x2, rflag=rflag, rx=rx, rcg=rcg, common=np.asarray(common, np.int32)))
+    return cases
+
+
+def spin0_cases(L, rng):
+    cases = []
+    for ci, (la, ra) in enumerate([([0, 1, 2, 3], [0, 1, 2, 3]), ([0, 2, 4, 6], [0, 2, 4, 6])]):
+        ld = [int(rng.integers(1, 8)) for _ in la]
+        rd = [int(rng.integers(1, 8)) for _ in ra]
+        vb = [(-1, la, ld), (-1, ra, rd)]
+        vdesc = desc_of(vb)
+        vflag = legal_flags(L, vdesc)
+        vx = random_data(vb, vflag, rng)
+        for side in (0, 1):
+            sec, dim = (la, ld) if side == 0 else (ra, rd)
+            hb = [(1, sec, dim), (-1, sec, dim)]
+            hdesc = desc_of(hb)
+            hflag = legal_flags(L, hdesc)
+            hx = random_data(hb, hflag, rng)
+            if side == 0:  # contract(hh[il],0,vec1,0)
+                L.ref_contract(p(hdesc), p(hflag), p(hx), 0, p(vdesc), p(vflag), p(vx), 0)
+            else:  # contract(vec1,1,hh[ir],0)
+                L.ref_contract(p(vdesc), p(vflag), p(vx), 1, p(hdesc), p(hflag), p(hx), 0)
+            rflag, rx, rcg = read_result(L)
+            cases.append(dict(name=f"spin0_{ci}_{side}", side=np.int32(side), vdesc=vdesc, vflag=vflag, vx=vx,
+                              hdesc=hdesc, hflag=hflag, hx=hx, rflag=rflag, rx=rx, rcg=rcg))
+    return cases
+
+
+def meta_cases(L, rng):
+    fa, fd, fo_a, fo_d, fn = [], [], [], [], []
+    for _ in range(40):
+        n1 = int(rng.integers(1, 6))
+        n2 = int(rng.integers(1, 4))
+        a1 = sorted(rng.choice(np.arange(0, 30), n1, replace=False).tolist())
+        a2 = sorted(rng.choice(np.arange(0, 12), n2, replace=False).tolist())
+        d1 = rng.integers(1, 50, n1).tolist()
+        d2 = rng.integers(1, 5, n2).tolist()
+        ao = np.zeros(128, np.int32)
+        do = np.zeros(128, np.int32)
+        A1, D1, A2, D2 = (np.asarray(v, np.int32) for v in (a1, d1, a2, d2))
+        n = L.ref_fuse(n1, p(A1), p(D1), n2, p(A2), p(D2), p(ao), p(do))
+        fa.append(np.concatenate([[n1], a1, d1, [n2], a2, d2]).astype(np.int32))
+        fo_a.append(ao[:n].copy())
+        fo_d.append(do[:n].copy())
+        fn.append(n)
+    # legality of random 2-, 3- and 4-leg structures with several locspins
+    ldesc, lflag = [], []
+    for _ in range(30):
+        nb = int(rng.integers(2, 5))
+        bonds = []
+        for _l in range(nb):
+            k = int(rng.integers(1, 5))
+            bonds.append((1, sorted(rng.choice(np.arange(0, 16), k, replace=False).tolist()), [1] * k))
+        desc = desc_of(bonds, int(rng.integers(0, 5)))
+        ldesc.append(desc)
+        lflag.append(legal_flags(L, desc))
+    pack = lambda arrs: (np.concatenate(arrs).astype(np.int32), np.cumsum([0] + [len(a) for a in arrs]))
+    fin, fin_idx = pack(fa)
+    foa, foa_idx = pack(fo_a)
+    fod, _ = pack(fo_d)
+    ld, ld_idx = pack(ldesc)
+    lf, lf_idx = pack(lflag)
+    return dict(fuse_in=fin, fuse_in_idx=fin_idx, fuse_out_a=foa, fuse_out_d=fod, fuse_out_idx=foa_idx,
+                legal_desc=ld, legal_desc_idx=ld_idx, legal_flag=lf, legal_flag_idx=lf_idx)
+
+
+def dmrg_runs(L):
+    runs = [
+        # (lx, ly, sec, D, niter, jcoup, qcoup, boundary)
+        (4, 2, 0, 64, 4, 0.5, 0.0, 2),
+        (3, 4, 0, 64, 4, 0.5, 0.0, 2),
+        (3, 4, 0, 64, 4, 0.5, 1.0, 2),
+        (6, 4, 0, 200, 4, 2.0, 0.0, 2),
+    ]
+    out = []
+    cwd = os.getcwd()
+    for (lx, ly, sec, d, niter, jc, qc, bd) in runs:
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            e = np.zeros(64)
+            n = L.ref_run_dmrg(lx, ly, sec, d, niter, ctypes.c_double(jc), ctypes.c_double(qc), bd, 1, p(e))
+            os.chdir(cwd)
+        out.append(dict(lx=lx, ly=ly, sec=sec, d=d, niter=niter, jcoup=jc, qcoup=qc, boundary=bd,
+                        energies_minus_1000=[float(v) for v in e[:n]]))
+        print("dmrg", lx, ly, d, jc, qc, out[-1]["energies_minus_1000"], file=sys.stderr)
+    return out
+
+
+def main():
+    L = ctypes.CDLL(REFLIB)
+    L.ref_setup(1, 25)
+    rng = np.random.Generator(np.random.PCG64(20241203))
+    fac = np.zeros(25**3)
+    L.ref_fac_hamilt_vec(25, p(fac))
+    np.save(os.path.join(HERE, "fac_hamilt_vec.npy"), fac.reshape(25, 25, 25))
+    trip, vals = [], []
+    for (j1, j2, j3) in [(0, 0, 0), (1, 1, 0), (1, 1, 2), (2, 2, 2), (3, 2, 1), (4, 2, 6), (5, 3, 4), (6, 6, 0),
+                         (7, 2, 9), (12, 2, 12), (13, 1, 12), (24, 2, 22), (24, 24, 24), (9, 8, 7)]:
+        c = np.zeros((j1 + 1) * (j2 + 1) * (j3 + 1))
+        L.ref_make_cgc(j1, j2, j3, p(c))
+        trip.append((j1, j2, j3))
+        vals.append(c)
+    np.savez(os.path.join(HERE, "cgc.npz"), triples=np.asarray(trip, np.int32), values=np.concatenate(vals),
+             idx=np.cumsum([0] + [len(v) for v in vals]))
+    np.savez(os.path.join(HERE, "meta.npz"), **meta_cases(L, rng))
+    for c in heff_cases(L, rng) + spin0_cases(L, rng):
+        name = c.pop("name")
+        np.savez(os.path.join(HERE, name + ".npz"), **c)
+    if "--no-dmrg" not in sys.argv:
+        with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
+            json.dump(dmrg_runs(L), f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,102 @@
+"""libsu2g.so host entry points (no GPU needed): integer bookkeeping and the
+recoupling tables must be bit-exact with the reference; the C ABI exports
+every symbol include/su2g.h declares."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REPO
+
+
+def test_exports_match_header(su2lib):
+    hdr = open(os.path.join(REPO, "include", "su2g.h")).read()
+    declared = sorted(set(re.findall(r"\b(su2g_[a-z0-9_]+)\s*\(", hdr)))
+    so = os.path.join(REPO, "su2dmrg_gb300", "libsu2g.so")
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (su2g_[a-z0-9_]+)$", out, re.M))
+    missing = [d for d in declared if d not in exported]
+    assert not missing, missing
+    for d in declared:
+        assert hasattr(su2lib, d)
+    from su2dmrg_gb300 import capi
+
+    assert sorted(capi.EXPORTED) == declared
+
+
+def test_fac_table_bit_exact(su2lib):
+    from su2dmrg_gb300.su2 import fac_hamilt_vec
+
+    ref = np.load(os.path.join(GOLDEN, "fac_hamilt_vec.npy"))
+    assert np.array_equal(fac_hamilt_vec(25), ref)
+
+
+def test_cgc_bit_exact(su2lib):
+    from su2dmrg_gb300.su2 import make_cgc
+
+    g = np.load(os.path.join(GOLDEN, "cgc.npz"))
+    for n, (j1, j2, j3) in enumerate(g["triples"]):
+        assert np.array_equal(make_cgc(int(j1), int(j2), int(j3)), g["values"][g["idx"][n]: g["idx"][n + 1]])
+
+
+def test_fuse_and_legality(su2lib):
+    from su2dmrg_gb300.su2 import Su2Bond, Su2Struct
+
+    g = np.load(os.path.join(GOLDEN, "meta.npz"))
+    fin, idx = g["fuse_in"], g["fuse_in_idx"]
+    for c in range(len(idx) - 1):
+        v = fin[idx[c]: idx[c + 1]].tolist()
+        n1 = v[0]
+        a1, d1 = v[1: 1 + n1], v[1 + n1: 1 + 2 * n1]
+        n2 = v[1 + 2 * n1]
+        a2, d2 = v[2 + 2 * n1: 2 + 2 * n1 + n2], v[2 + 2 * n1 + n2:]
+        f = Su2Bond(1, a1, d1).fuse(Su2Bond(1, a2, d2))
+        assert f.angm == g["fuse_out_a"][g["fuse_out_idx"][c]: g["fuse_out_idx"][c + 1]].tolist()
+        assert f.dim == g["fuse_out_d"][g["fuse_out_idx"][c]: g["fuse_out_idx"][c + 1]].tolist()
+        assert f.dir == -1
+    d, di, fl, fi = g["legal_desc"], g["legal_desc_idx"], g["legal_flag"], g["legal_flag_idx"]
+    for c in range(len(di) - 1):
+        desc = np.ascontiguousarray(d[di[c]: di[c + 1]], np.int32)
+        out = np.zeros(fi[c + 1] - fi[c], np.int32)
+        assert su2lib.su2g_struct_legal(desc.ctypes.data, out.ctypes.data) == len(out)
+        assert out.tolist() == fl[fi[c]: fi[c + 1]].tolist()
+
+
+def test_layout_offsets(su2lib):
+    from su2dmrg_gb300.su2 import Su2Bond, Su2Struct
+
+    s = Su2Struct([Su2Bond(-1, [0, 1, 2], [3, 4, 5]), Su2Bond(-1, [0, 1, 2], [2, 6, 7])], 0).with_legal_flags()
+    assert s.flag.tolist() == [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    off, total = s.offsets()
+    assert off.tolist() == [0, -1, -1, -1, 6, -1, -1, -1, 30]
+    assert total == 6 + 24 + 35
+
+
+def test_malformed_inputs_rejected(su2lib):
+    bad = np.asarray([7, 0], np.int32)  # 7 legs
+    assert su2lib.su2g_struct_nten(bad.ctypes.data) == -1
+    unsorted = np.asarray([1, 0, -1, 2, 3, 1, 5, 5], np.int32)
+    assert su2lib.su2g_struct_nten(unsorted.ctypes.data) == -1
+    from su2dmrg_gb300 import capi
+
+    out = np.zeros(8)
+    assert su2lib.su2g_make_cgc(-1, 0, 0, out.ctypes.data) == capi.SU2G_EINVAL
+    assert b"make_cgc" in su2lib.su2g_last_error()
+
+
+def test_plan_validation_without_gpu(su2lib):
+    """Structure mismatches are reported as SU2G_EINVAL before any device work."""
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300.su2 import HeffPlan, Su2Bond, Su2Struct
+
+    e = Su2Bond(-1, [0, 1, 2], [2, 3, 2])
+    psi = Su2Struct([e, e], 0).with_legal_flags()
+    other = Su2Bond(1, [0, 1, 2], [2, 9, 2])  # wrong dims
+    op = Su2Struct([other, Su2Bond(1, [2], [1]), e], 0).with_legal_flags()
+    x = np.zeros(op.size())
+    with pytest.raises(capi.Su2gError) as ei:
+        HeffPlan(psi, [(op, x, op, x, 1.0)])
+    assert ei.value.code == capi.SU2G_EINVAL

@@ -1,0 +1,136 @@
+"""The CPU oracle (oracle/su2_oracle.c) against fixtures produced by the
+reference itself (tests/golden/gen_golden.py).  These pin the oracle before any
+GPU result is compared with it."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def test_fac_hamilt_vec_bit_exact(oracle):
+    ref = np.load(os.path.join(GOLDEN, "fac_hamilt_vec.npy"))
+    got = oracle.fac_hamilt_vec(25)
+    assert np.array_equal(got, ref), np.abs(got - ref).max()
+    assert np.count_nonzero(ref) > 1000
+
+
+def test_make_cgc_bit_exact(oracle):
+    g = np.load(os.path.join(GOLDEN, "cgc.npz"))
+    for n, (j1, j2, j3) in enumerate(g["triples"]):
+        ref = g["values"][g["idx"][n]: g["idx"][n + 1]]
+        got = oracle.make_cgc(int(j1), int(j2), int(j3))
+        assert np.array_equal(got, ref), (j1, j2, j3)
+
+
+def test_fuse_matches_reference(oracle):
+    g = np.load(os.path.join(GOLDEN, "meta.npz"))
+    fin, idx = g["fuse_in"], g["fuse_in_idx"]
+    oa, od, oidx = g["fuse_out_a"], g["fuse_out_d"], g["fuse_out_idx"]
+    for c in range(len(idx) - 1):
+        v = fin[idx[c]: idx[c + 1]].tolist()
+        n1 = v[0]
+        a1, d1 = v[1: 1 + n1], v[1 + n1: 1 + 2 * n1]
+        n2 = v[1 + 2 * n1]
+        a2, d2 = v[2 + 2 * n1: 2 + 2 * n1 + n2], v[2 + 2 * n1 + n2:]
+        f = oracle.fuse(oracle.Bond(1, a1, d1), oracle.Bond(1, a2, d2))
+        assert f.angm == oa[oidx[c]: oidx[c + 1]].tolist()
+        assert f.dim == od[oidx[c]: oidx[c + 1]].tolist()
+
+
+def test_legality_matches_reference(oracle):
+    g = np.load(os.path.join(GOLDEN, "meta.npz"))
+    d, di, f, fi = g["legal_desc"], g["legal_desc_idx"], g["legal_flag"], g["legal_flag_idx"]
+    for c in range(len(di) - 1):
+        s = oracle.struct_from_desc(d[di[c]: di[c + 1]])
+        assert s.legal().tolist() == f[fi[c]: fi[c + 1]].tolist()
+
+
+def _singlet_cg_ok(oracle, s, rflag, rcg):
+    """Every result block carries the canonical singlet CG (so comparing the
+    reduced blocks alone is comparing the tensors)."""
+    pos = 0
+    for i in range(s.nten):
+        if not rflag[i]:
+            continue
+        ja, jb = s.block_angm(i)
+        n = (ja + 1) * (jb + 1)
+        cg = rcg[pos: pos + n].reshape(ja + 1, jb + 1, order="F")
+        pos += n
+        sing = np.zeros((ja + 1, ja + 1))
+        for r in range(ja + 1):
+            m = 2 * r - ja
+            sing[r, ja - r] = (1 if ((ja - m) // 2) % 2 == 0 else -1) / np.sqrt(ja + 1)
+        assert ja == jb and np.allclose(cg, sing, atol=1e-14)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "heff_term_*.npz"))))
+def test_heff_term_matches_reference(oracle, path):
+    g = np.load(path)
+    vs = oracle.struct_from_desc(g["vdesc"], g["vflag"])
+    s1 = oracle.struct_from_desc(g["d1"], g["f1"])
+    s2 = oracle.struct_from_desc(g["d2"], g["f2"])
+    y = np.zeros_like(g["vx"])
+    oracle.heff_term(vs, g["vx"], s1, g["x1"], s2, g["x2"], vs, y)
+    rs = oracle.struct_from_desc(g["vdesc"], g["rflag"])
+    _singlet_cg_ok(oracle, rs, g["rflag"], g["rcg"])
+    ref = oracle.to_layout(rs, g["rx"], vs)
+    assert np.linalg.norm(ref) > 0
+    assert np.linalg.norm(y - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "spin0_*.npz"))))
+def test_spin0_matches_reference(oracle, path):
+    g = np.load(path)
+    vs = oracle.struct_from_desc(g["vdesc"], g["vflag"])
+    hs = oracle.struct_from_desc(g["hdesc"], g["hflag"])
+    y = np.zeros_like(g["vx"])
+    oracle.heff_spin0(int(g["side"]), hs, g["hx"], vs, g["vx"], vs, y)
+    rs = oracle.struct_from_desc(g["vdesc"], g["rflag"])
+    _singlet_cg_ok(oracle, rs, g["rflag"], g["rcg"])
+    ref = oracle.to_layout(rs, g["rx"], vs)
+    assert np.linalg.norm(y - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+def test_dsort2_and_ran_restatement(oracle):
+    """The C restatement of sort2.f / ran.f90 (oracle/fhelpers.c): ascending
+    order with the companion array permuted alongside, and a deterministic
+    LCG stream in (0,1)."""
+    import ctypes
+
+    L = oracle.lib()
+    a = np.array([3.0, 1.0, 2.0, 1.0, 5.0, 0.5], np.float64)
+    b = np.arange(6, dtype=np.int32)
+    n = ctypes.c_int(6)
+    L.dsort2_(ctypes.byref(n), a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p))
+    assert a.tolist() == sorted([3.0, 1.0, 2.0, 1.0, 5.0, 0.5])
+    assert sorted(b.tolist()) == list(range(6))
+    assert all(np.array([3.0, 1.0, 2.0, 1.0, 5.0, 0.5])[b] == a)
+    L.ran_.restype = ctypes.c_double
+    seed = ctypes.c_int(12345)
+    L.initran_(ctypes.byref(seed))
+    xs = [L.ran_() for _ in range(1000)]
+    L.initran_(ctypes.byref(seed))
+    assert xs == [L.ran_() for _ in range(1000)]
+    assert 0 < min(xs) and max(xs) < 1 and abs(np.mean(xs) - 0.5) < 0.05
+
+
+def test_dmrg_energies_match_exact_diagonalisation():
+    """The reference runs recorded in the fixtures converge to the exact ground
+    states of the small lattices (E0 - 1000 is what the reference prints)."""
+    path = os.path.join(GOLDEN, "dmrg_energies.json")
+    if not os.path.exists(path):
+        pytest.skip("dmrg_energies.json not generated")
+    runs = json.load(open(path))
+    exact = {(4, 2, 0.5, 0.0): -3.296960690549784, (3, 4, 0.5, 0.0): -6.762720424674632,
+             (3, 4, 0.5, 1.0): -10.228711857181608}
+    seen = 0
+    for r in runs:
+        key = (r["lx"], r["ly"], r["jcoup"], r["qcoup"])
+        if key in exact:
+            assert abs(r["energies_minus_1000"][-1] + 1000 - exact[key]) < 1e-8
+            seen += 1
+    assert seen == 3
