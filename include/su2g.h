@@ -96,6 +96,13 @@ int su2g_fac_hamilt_vec(int max_angm, double* out);
 int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                           const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
                           su2g_heff_plan** plan);
+/* Host-only dry run of su2g_heff_plan_create: builds the work list and checks
+ * every element access its kernels would make against the extent of the block
+ * it reads or writes, without touching a GPU.  Same arguments; outputs the
+ * algorithmic FLOPs of one application and the scratch length (doubles). */
+int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef,
+                            double* flops, int64_t* scratch_len);
 /* flops: algorithmic FLOPs of one application; psi_len: packed length of psi
  * and y (doubles); scratch_bytes: device scratch held by the plan; ntiles:
  * output tiles of the two launch phases. */

@@ -56,6 +56,7 @@ _PROTOS = {
     "su2g_make_cgc": (_i, [_i, _i, _i, _vp]),
     "su2g_fac_hamilt_vec": (_i, [_i, _vp]),
     "su2g_heff_plan_create": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp]),
+    "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _vp, _vp]),
     "su2g_heff_plan_info": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_apply": (_i, [_vp, _vp, _vp, _vp]),
     "su2g_heff_plan_destroy": (_i, [_vp]),

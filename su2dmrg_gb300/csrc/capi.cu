@@ -156,6 +156,18 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
   return SU2G_OK;
 }
 
+int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef,
+                            double* flops, int64_t* scratch_len) {
+  su2g::HeffWork w;
+  std::string err;
+  int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err);
+  if (rc) return fail(rc, err);
+  if (flops) *flops = w.flops;
+  if (scratch_len) *scratch_len = w.scratch_len;
+  return SU2G_OK;
+}
+
 int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len, int64_t* scratch_bytes,
                         int* ntiles) {
   if (!p) return fail(SU2G_EINVAL, "plan_info: null plan");

@@ -24,6 +24,7 @@ enum BufId : int { kBufAbs = 0, kBufPsi = 1, kBufY = 2, kBufScratch = 3, kNumBuf
 
 struct GemmSeg {
   int64_t a, b;   // element offsets of the A / B block origins
+  int64_t a_len, b_len;  // elements of the A / B blocks (host-side bounds check)
   int a_buf, b_buf;
   int lda, ldb;
   int K;
@@ -33,6 +34,7 @@ struct GemmSeg {
 
 struct GemmTile {
   int64_t c;      // element offset of the C block origin
+  int64_t c_len;  // elements of the C block (host-side bounds check)
   int c_buf;
   int ldc;
   int m0, n0;     // tile origin inside the block

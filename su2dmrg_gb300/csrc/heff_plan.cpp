@@ -42,12 +42,13 @@ int parse_tensor(const su2g_tensor& t, int want_legs, Op* op, const char* what, 
   return SU2G_OK;
 }
 
-void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int c_buf, int ldc, int M, int N, int seg0, int nseg,
-               int64_t kwork) {
+void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int64_t c_len, int c_buf, int ldc, int M, int N,
+               int seg0, int nseg, int64_t kwork) {
   for (int m0 = 0; m0 < M; m0 += kTileM)
     for (int n0 = 0; n0 < N; n0 += kTileN) {
       GemmTile t;
       t.c = c_off;
+      t.c_len = c_len;
       t.c_buf = c_buf;
       t.ldc = ldc;
       t.m0 = m0;
@@ -167,7 +168,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
           }
           used = true;
         }
-        if (!used) continue;
+        if (!used || a == 0 || b == 0 || ms == 0 || c == 0) continue;  // zero-size products add nothing
         TBlock T{t, k, j, w.scratch_len, a, b, ms, c, ja, jb, s, jc, f};
         tb.push_back(T);
         GemmSeg g;
@@ -175,6 +176,8 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         g.a_buf = kBufPsi;
         g.b = abs_off(op1[t].base, s1.offset[j]);
         g.b_buf = kBufAbs;
+        g.a_len = (int64_t)a * b;
+        g.b_len = (int64_t)a * ms * c;
         g.lda = a;
         g.ldb = a;
         g.K = a;
@@ -182,7 +185,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         g.alpha = 1.0;
         const int seg0 = (int)w.seg1.size();
         w.seg1.push_back(g);
-        add_tiles(w.tile1, T.off, kBufScratch, b, b, ms * c, seg0, 1, a);
+        add_tiles(w.tile1, T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1, a);
         w.scratch_len += (int64_t)b * ms * c;
         w.flops += 2.0 * a * b * (double)ms * c;
         w.max_k = std::max<int64_t>(w.max_k, a);
@@ -203,13 +206,15 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         if (!s.flag[l] || s.block_angm(l, 1) != jc) continue;
         const int ja = s.block_angm(l, 0), a = s.block_dim(l, 0);
         const int sec[2] = {P.legs[0].sector_of(ja), P.legs[1].sector_of(jd)};
-        if (sec[0] < 0 || !P.flag[P.index(sec)]) continue;
+        if (sec[0] < 0 || !P.flag[P.index(sec)] || a == 0) continue;
         const int k = P.index(sec);
         GemmSeg g;
         g.a = abs_off(h[0].base, s.offset[l]);
         g.a_buf = kBufAbs;
         g.b = P.offset[k];
         g.b_buf = kBufPsi;
+        g.a_len = (int64_t)a * c;
+        g.b_len = (int64_t)a * d;
         g.lda = a;
         g.ldb = a;
         g.K = a;
@@ -227,13 +232,15 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         if (!s.flag[l] || s.block_angm(l, 1) != jd) continue;
         const int jb = s.block_angm(l, 0), b = s.block_dim(l, 0);
         const int sec[2] = {P.legs[0].sector_of(jc), P.legs[1].sector_of(jb)};
-        if (sec[1] < 0 || !P.flag[P.index(sec)]) continue;
+        if (sec[1] < 0 || !P.flag[P.index(sec)] || b == 0) continue;
         const int k = P.index(sec);
         GemmSeg g;
         g.a = P.offset[k];
         g.a_buf = kBufPsi;
         g.b = abs_off(h[1].base, s.offset[l]);
         g.b_buf = kBufAbs;
+        g.a_len = (int64_t)c * b;
+        g.b_len = (int64_t)b * d;
         g.lda = c;
         g.ldb = b;
         g.K = b;
@@ -257,6 +264,8 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         g.a_buf = kBufScratch;
         g.b = abs_off(op2[T.t].base, s2.offset[l]);
         g.b_buf = kBufAbs;
+        g.a_len = (int64_t)T.b * T.ms * T.c;
+        g.b_len = (int64_t)T.b * T.ms * d;
         g.lda = T.b * T.ms;
         g.ldb = T.b * T.ms;
         g.K = T.b * T.ms;
@@ -268,13 +277,70 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         w.max_k = std::max<int64_t>(w.max_k, g.K);
       }
     }
-    add_tiles(w.tile2, P.offset[m], kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
+    add_tiles(w.tile2, P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
   }
 
   // heaviest tiles first: the block scheduler then approximates LPT order
   auto heavier = [](const GemmTile& x, const GemmTile& y) { return x.kwork > y.kwork; };
   std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
   std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
+  return validate_heff_work(w, err);
+}
+
+namespace {
+bool within(int64_t off, int64_t len, int buf, const HeffWork& w) {
+  if (off < 0 || len < 0) return false;
+  if (buf == kBufPsi || buf == kBufY) return off + len <= w.psi.total;
+  if (buf == kBufScratch) return off + len <= w.scratch_len;
+  return buf == kBufAbs;
+}
+
+// largest element index read from an operand stored with leading dimension
+// ld: rows [r0, r0+nr) x columns [c0, c0+nc)
+int64_t last_index(int64_t r0, int64_t nr, int64_t c0, int64_t nc, int64_t ld) {
+  return (r0 + nr - 1) + (c0 + nc - 1) * ld;
+}
+
+int check_list(const std::vector<GemmTile>& tiles, const std::vector<GemmSeg>& segs, const HeffWork& w,
+               const char* phase, std::string* err) {
+  for (const GemmTile& t : tiles) {
+    if (t.mlen <= 0 || t.nlen <= 0 || t.mlen > kTileM || t.nlen > kTileN || t.m0 < 0 || t.n0 < 0 ||
+        !within(t.c, t.c_len, t.c_buf, w) || last_index(t.m0, t.mlen, t.n0, t.nlen, t.ldc) >= t.c_len ||
+        t.ldc < t.m0 + t.mlen || t.seg0 < 0 || t.nseg < 0 || t.seg0 + t.nseg > (int)segs.size()) {
+      *err = std::string(phase) + ": tile out of bounds";
+      return SU2G_EINVAL;
+    }
+    for (int s = t.seg0; s < t.seg0 + t.nseg; ++s) {
+      const GemmSeg& g = segs[s];
+      if (g.K <= 0 || !within(g.a, g.a_len, g.a_buf, w) || !within(g.b, g.b_len, g.b_buf, w)) {
+        *err = std::string(phase) + ": segment out of bounds";
+        return SU2G_EINVAL;
+      }
+      const int64_t alast = g.transA ? last_index(0, g.K, t.m0, t.mlen, g.lda) : last_index(t.m0, t.mlen, 0, g.K, g.lda);
+      const int64_t blast = last_index(0, g.K, t.n0, t.nlen, g.ldb);
+      const bool lda_ok = g.transA ? g.lda >= g.K : g.lda >= t.m0 + t.mlen;
+      if (alast >= g.a_len || blast >= g.b_len || !lda_ok || g.ldb < g.K) {
+        *err = std::string(phase) + ": operand access beyond its block";
+        return SU2G_EINVAL;
+      }
+    }
+  }
+  return SU2G_OK;
+}
+}  // namespace
+
+int validate_heff_work(const HeffWork& w, std::string* err) {
+  int rc = check_list(w.tile1, w.seg1, w, "phase 1", err);
+  if (rc) return rc;
+  rc = check_list(w.tile2, w.seg2, w, "phase 2", err);
+  if (rc) return rc;
+  // the output tiles cover y exactly (each element written once)
+  int64_t written = 0;
+  for (const GemmTile& t : w.tile2) written += (int64_t)t.mlen * t.nlen;
+  if (written != w.psi.total) {
+    *err = "phase 2 tiles do not cover y exactly";
+    return SU2G_EINVAL;
+  }
   return SU2G_OK;
 }
 

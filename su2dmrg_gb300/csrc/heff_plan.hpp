@@ -36,4 +36,9 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
                     const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, HeffWork* out,
                     std::string* err);
 
+// Checks every element access the kernels will make against the extent of
+// the block it belongs to (and the block against its buffer for psi, y and
+// scratch).  Returns SU2G_OK or SU2G_EINVAL with *err set.
+int validate_heff_work(const HeffWork& w, std::string* err);
+
 }  // namespace su2g

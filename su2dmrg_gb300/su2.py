@@ -130,6 +130,35 @@ def _tensor(struct: Su2Struct, data, keep: list) -> capi.Tensor:
     return capi.Tensor(ptr(p.desc), ptr(p.flag), ptr(data))
 
 
+class _PlanArgs:
+    """Packs (psi, terms, hl, hr) into the C structures of su2g_heff_plan_*;
+    the host arrays stay referenced while the call runs."""
+
+    def __init__(self, psi, terms, hl, hr):
+        self.keep = []
+        self.tarr = (capi.Term * max(1, len(terms)))()
+        for i, (s1, x1, s2, x2, c) in enumerate(terms):
+            self.tarr[i] = capi.Term(_tensor(s1, x1, self.keep), _tensor(s2, x2, self.keep), float(c))
+        self.h = []
+        for h in (hl, hr):
+            if h is None:
+                self.h.append((None, 0.0))
+            else:
+                t = _tensor(h[0], h[1], self.keep)
+                self.keep.append(t)
+                self.h.append((ctypes.addressof(t), float(h[2])))
+        self.pd = psi.desc()
+        self.pf = psi.flag_array()
+        self.args = (ptr(self.pd), ptr(self.pf), len(terms), ctypes.addressof(self.tarr),
+                     self.h[0][0], self.h[0][1], self.h[1][0], self.h[1][1])
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.keep.clear()
+
+
 class HeffPlan:
     """Device work list of one effective Hamiltonian (see su2g_heff_plan_create).
 
@@ -141,31 +170,23 @@ class HeffPlan:
 
     def __init__(self, psi: Su2Struct, terms, hl=None, hr=None, mode: int = capi.MODE_F64):
         self.psi = psi
-        keep = []
-        self._data_refs = []
-        tarr = (capi.Term * max(1, len(terms)))()
-        for i, (s1, x1, s2, x2, c) in enumerate(terms):
-            tarr[i] = capi.Term(_tensor(s1, x1, keep), _tensor(s2, x2, keep), float(c))
-            self._data_refs += [x1, x2]
-        hl_t = hr_t = None
-        hl_c = hr_c = 0.0
-        if hl is not None:
-            hl_t = _tensor(hl[0], hl[1], keep)
-            hl_c = float(hl[2])
-            self._data_refs.append(hl[1])
-        if hr is not None:
-            hr_t = _tensor(hr[0], hr[1], keep)
-            hr_c = float(hr[2])
-            self._data_refs.append(hr[1])
-        pd = psi.desc()
-        pf = psi.flag_array()
+        self._data_refs = [x for (_s1, x1, _s2, x2, _c) in terms for x in (x1, x2)]
+        self._data_refs += [h[1] for h in (hl, hr) if h is not None]
         handle = ctypes.c_void_p()
-        check(lib().su2g_heff_plan_create(
-            ptr(pd), ptr(pf), len(terms), ctypes.addressof(tarr),
-            ctypes.addressof(hl_t) if hl_t is not None else None, hl_c,
-            ctypes.addressof(hr_t) if hr_t is not None else None, hr_c, int(mode), ctypes.addressof(handle)))
+        with _PlanArgs(psi, terms, hl, hr) as a:
+            check(lib().su2g_heff_plan_create(*a.args, int(mode), ctypes.addressof(handle)))
         self._h = handle
         self.mode = mode
+
+    @staticmethod
+    def validate(psi: Su2Struct, terms, hl=None, hr=None) -> dict:
+        """Host-only dry run: builds the work list and bounds-checks every
+        access (su2g_heff_plan_validate).  Data may be host arrays."""
+        fl = ctypes.c_double()
+        sl = ctypes.c_int64()
+        with _PlanArgs(psi, terms, hl, hr) as a:
+            check(lib().su2g_heff_plan_validate(*a.args, ctypes.addressof(fl), ctypes.addressof(sl)))
+        return {"flops": fl.value, "scratch_len": sl.value}
 
     @property
     def handle(self):

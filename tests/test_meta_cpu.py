@@ -100,3 +100,18 @@ def test_plan_validation_without_gpu(su2lib):
     with pytest.raises(capi.Su2gError) as ei:
         HeffPlan(psi, [(op, x, op, x, 1.0)])
     assert ei.value.code == capi.SU2G_EINVAL
+
+
+@pytest.mark.parametrize("D,nspin1", [(60, 3), (2000, 18)])
+def test_work_list_bounds_on_cpu(su2lib, D, nspin1):
+    """Every element access of the H_eff kernels, at the benchmark shape,
+    checked against the blocks it belongs to before anything runs on a GPU."""
+    from su2dmrg_gb300.su2 import HeffPlan
+    from su2dmrg_gb300.workloads import synthetic_heff
+
+    w = synthetic_heff(D=D, nspin1=nspin1, seed=1234)
+    r = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr)
+    assert r["flops"] > 0 and r["scratch_len"] > 0
+    if D == 2000:
+        # algorithmic FLOPs of the width-20 D=2000 step (18 spin-1 pairs + 2 spin-0)
+        assert 1.0e11 < r["flops"] < 2.0e11
