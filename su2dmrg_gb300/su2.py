@@ -119,9 +119,9 @@ class _Pinned:
     """Keeps the host arrays a plan was built from alive (the library copies
     them, but the ctypes structures point at them during creation)."""
 
-    def __init__(self, struct: Su2Struct):
-        self.desc = struct.desc()
-        self.flag = struct.flag_array()
+    def __init__(self, struct):
+        self.desc = np.ascontiguousarray(struct.desc(), np.int32)
+        self.flag = np.ascontiguousarray(struct.flag, np.int32)
 
 
 def _tensor(struct: Su2Struct, data, keep: list) -> capi.Tensor:
@@ -147,8 +147,8 @@ class _PlanArgs:
                 t = _tensor(h[0], h[1], self.keep)
                 self.keep.append(t)
                 self.h.append((ctypes.addressof(t), float(h[2])))
-        self.pd = psi.desc()
-        self.pf = psi.flag_array()
+        self.pd = np.ascontiguousarray(psi.desc(), np.int32)
+        self.pf = np.ascontiguousarray(psi.flag, np.int32)
         self.args = (ptr(self.pd), ptr(self.pf), len(terms), ctypes.addressof(self.tarr),
                      self.h[0][0], self.h[0][1], self.h[1][0], self.h[1][1])
 
@@ -228,7 +228,7 @@ def hamiltonian_vector_multiplication(vec: Su2Struct, vec_data, op1: Su2Struct, 
     keep = []
     t1 = _tensor(op1, x1, keep)
     t2 = _tensor(op2, x2, keep)
-    vd = vec.desc()
-    vf = vec.flag_array()
+    vd = np.ascontiguousarray(vec.desc(), np.int32)
+    vf = np.ascontiguousarray(vec.flag, np.int32)
     check(lib().su2g_hamiltonian_vector_multiplication(ptr(vd), ptr(vf), ptr(vec_data), t1, t2, ptr(y),
                                                        stream_handle(stream)))

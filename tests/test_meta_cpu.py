@@ -115,3 +115,20 @@ def test_work_list_bounds_on_cpu(su2lib, D, nspin1):
     if D == 2000:
         # algorithmic FLOPs of the width-20 D=2000 step (18 spin-1 pairs + 2 spin-0)
         assert 1.0e11 < r["flops"] < 2.0e11
+
+
+def test_golden_cases_build_valid_work_lists(su2lib, oracle):
+    """The reference's golden H_eff inputs produce bounds-checked work lists
+    (host dry run), with the oracle's structures passed straight through."""
+    import glob
+
+    from su2dmrg_gb300.su2 import HeffPlan
+
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "heff_term_*.npz"))):
+        g = np.load(path)
+        vs = oracle.struct_from_desc(g["vdesc"], g["vflag"])
+        s1 = oracle.struct_from_desc(g["d1"], g["f1"])
+        s2 = oracle.struct_from_desc(g["d2"], g["f2"])
+        r = HeffPlan.validate(vs, [(s1, g["x1"], s2, g["x2"], 1.0)])
+        prob = oracle.HeffProblem(vs, [(s1, g["x1"], s2, g["x2"], 1.0)])
+        assert r["flops"] == oracle.heff_flops(prob)
