@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="su2g", choices=["su2g", "reference"])
-    ap.add_argument("--mode", default="f64", choices=["f64"])
+    ap.add_argument("--mode", default="split", choices=["f64", "split", "split-fast"])
     ap.add_argument("--D", type=int, default=2000)
     ap.add_argument("--nspin1", type=int, default=18)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -135,6 +135,21 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+MODES = {"f64": 0, "split": 1, "split-fast": 2}
+SLICES = {"f64": 0, "split": 7, "split-fast": 6}
+
+
+def bf16_peak():
+    """Dense BF16 peak measured on this machine (MEASURED_PEAKS.json), else the
+    documented fallback."""
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops, burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback 1.9 PFLOP/s"
 
 
 def fp64_peak_tflops(torch):
@@ -232,7 +247,7 @@ def run_su2g(args):
     capi.lib()
     w = synthetic_heff(D=args.D, nspin1=args.nspin1, seed=1234)
     psi, terms, hl, hr = w.to_device()
-    plan = HeffPlan(w.psi, terms, hl, hr, mode=capi.MODE_F64)
+    plan = HeffPlan(w.psi, terms, hl, hr, mode=MODES[args.mode])
     info = plan.info()
     flops = info["flops"]
     y = torch.empty_like(psi)
@@ -259,7 +274,6 @@ def run_su2g(args):
     barrier(world)
     total = t0.elapsed_time(t1) / 1e3
     total = max_over_ranks(total, world)
-    per_step = [s.elapsed_time(e) / 1e3 for s, e in ev]
     ms_per_step = total / args.steps * 1e3
     value = flops * world * args.steps / total / 1e12
 
@@ -291,28 +305,59 @@ def run_su2g(args):
     # parity spot check of the measured output against the host copy path
     assert torch.equal(h_y.cuda(), y), "e2e output differs from device-resident output"
 
-    peak64 = fp64_peak_tflops(torch)
-    kernel_time = float(np.mean(per_step))  # both launches of gemm_f64_tiles fill the step
-    achieved = flops / kernel_time / 1e12
-    roof = {"bound": "tensor", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-            "frac": achieved / peak64, "traffic": None,
-            "kernel": "gemm_f64_tiles (FP64 DMMA), 2 launches per step",
-            "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 is not in MEASURED_PEAKS.json)"}
+    # per-launch times of one application (events between the launches)
+    prof = [plan.apply_profile(psi, y, stream) for _ in range(3)]
+    prof = [float(np.median([p[i] for p in prof])) for i in range(len(prof[0]))]
+    S = SLICES[args.mode]
+    if S == 0:
+        peak = fp64_peak_tflops(torch)
+        t_kernel = (prof[0] + prof[1]) / 1e3
+        achieved = flops / t_kernel / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "gemm_f64_tiles (FP64 DMMA m8n8k4), 2 launches per step",
+                "launch_ms": prof,
+                "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 is not in MEASURED_PEAKS.json)"}
+        accuracy = {"mode": "FP64", "rel_err_vs_fp64_path": 0.0}
+    else:
+        peak, src = bf16_peak()
+        pairs = S * (S + 1) // 2
+        t_kernel = (prof[1] + prof[3]) / 1e3
+        achieved = pairs * flops / t_kernel / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None,
+                "kernel": f"ozaki_gemm<{S}> (tcgen05 BF16, {pairs} digit-pair products per FP64 product), "
+                          "2 launches per step",
+                "achieved_definition": f"{pairs} x algorithmic FP64 FLOPs of the two GEMM launches / their time",
+                "launch_ms": {"pack_psi": prof[0], "gemm_phase1": prof[1], "pack_intermediates": prof[2],
+                              "gemm_phase2": prof[3]},
+                "peak_source": src}
+        ref_plan = HeffPlan(w.psi, terms, hl, hr, mode=capi.MODE_F64)
+        y64 = torch.empty_like(psi)
+        ref_plan.apply(psi, y64, stream)
+        plan.apply(psi, y, stream)
+        torch.cuda.synchronize()
+        rel = float((y - y64).norm() / y64.norm())
+        ref_plan.close()
+        accuracy = {"mode": f"BF16 x {S} slices", "rel_err_vs_fp64_path": rel,
+                    "tolerance": 1e-12 if S == 7 else 1e-10}
+        assert plan.status() == 0
     cb = None
     if not args.no_cpu_baseline:
         cb = CpuSample(args.D, 2).measure(seconds=10.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if S == 0 else f"f64 emulated by bf16 x{S} (fp32 accumulate)",
+        "data": "synthetic",
         "config": {"workload": f"synthetic SU(2) two-site H_eff, D={args.D}, width {args.nspin1 + 2}",
                    "mode": args.mode, "psi_doubles": int(psi.numel()), "flops_per_step": flops,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs (operators ~1.3 GB) larger than L2; no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                "path": "su2g_heff_apply via ctypes, pinned host psi -> device -> host y"},
-        "gpu_launches": 2 * args.steps,
+                "path": "su2g_heff_apply via ctypes, pinned host psi -> device -> host y; operators resident"},
+        "gpu_launches": (2 if S == 0 else 4) * args.steps,
         "roofline": roof,
+        "accuracy": accuracy,
         "cpu_baseline": cb,
         "clocks": clk.summary(),
     }

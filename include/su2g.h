@@ -39,8 +39,9 @@ extern "C" {
 #define SU2G_ETIMEOUT 4    /* a bounded device wait gave up */
 #define SU2G_EUNSUPPORTED 5
 
-#define SU2G_MODE_F64 0        /* plain FP64 contractions */
-#define SU2G_MODE_SPLIT_BF16 1 /* FP64 emulated with BF16 slices on the tensor cores */
+#define SU2G_MODE_F64 0             /* plain FP64 contractions (FP64 tensor-core MMA) */
+#define SU2G_MODE_SPLIT_BF16 1      /* FP64 emulated with 7 BF16 digit slices on the tcgen05 tensor cores */
+#define SU2G_MODE_SPLIT_BF16_FAST 2 /* the same with 6 slices: fewer products, about 2^-40 relative error */
 
 typedef struct su2g_heff_plan su2g_heff_plan;
 
@@ -96,13 +97,17 @@ int su2g_fac_hamilt_vec(int max_angm, double* out);
 int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                           const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
                           su2g_heff_plan** plan);
-/* Host-only dry run of su2g_heff_plan_create: builds the work list and checks
- * every element access its kernels would make against the extent of the block
- * it reads or writes, without touching a GPU.  Same arguments; outputs the
- * algorithmic FLOPs of one application and the scratch length (doubles). */
+/* Host-only dry run of su2g_heff_plan_create: builds the work lists of the
+ * given mode and checks every element access their kernels would make against
+ * the extent of the block it reads or writes, without touching a GPU.  Same
+ * arguments; outputs the algorithmic FLOPs of one application and the device
+ * bytes the plan would hold beyond its work lists. */
 int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
-                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef,
-                            double* flops, int64_t* scratch_len);
+                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                            double* flops, int64_t* scratch_bytes);
+/* Reads and clears the plan's device error word (the split-precision kernels
+ * record a bounded wait that gave up there).  SU2G_ETIMEOUT if one did. */
+int su2g_heff_plan_status(su2g_heff_plan* plan, int* code);
 /* flops: algorithmic FLOPs of one application; psi_len: packed length of psi
  * and y (doubles); scratch_bytes: device scratch held by the plan; ntiles:
  * output tiles of the two launch phases. */
@@ -110,6 +115,12 @@ int su2g_heff_plan_info(const su2g_heff_plan* plan, double* flops, int64_t* psi_
                         int* ntiles);
 /* y = H_eff psi (device pointers, psi_len doubles each, no aliasing). */
 int su2g_heff_apply(su2g_heff_plan* plan, const double* psi, double* y, void* stream);
+/* su2g_heff_apply with a CUDA event between its launches; waits for the
+ * result and writes the duration (ms) of each launch to ms[0..*nlaunch):
+ * FP64 mode: phase 1, phase 2; split modes: pack psi, phase 1, pack the
+ * intermediates, phase 2. */
+int su2g_heff_apply_profile(su2g_heff_plan* plan, const double* psi, double* y, void* stream, double* ms,
+                            int* nlaunch);
 int su2g_heff_plan_destroy(su2g_heff_plan* plan);
 
 /* One-shot form of tensor_su2::hamiltonian_vector_multiplication(vec, op1, op2)

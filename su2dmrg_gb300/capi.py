@@ -23,6 +23,7 @@ SU2G_EUNSUPPORTED = 5
 
 MODE_F64 = 0
 MODE_SPLIT_BF16 = 1
+MODE_SPLIT_BF16_FAST = 2
 
 
 class Su2gError(RuntimeError):
@@ -56,9 +57,11 @@ _PROTOS = {
     "su2g_make_cgc": (_i, [_i, _i, _i, _vp]),
     "su2g_fac_hamilt_vec": (_i, [_i, _vp]),
     "su2g_heff_plan_create": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp]),
-    "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _vp, _vp]),
+    "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp, _vp]),
+    "su2g_heff_plan_status": (_i, [_vp, _vp]),
     "su2g_heff_plan_info": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "su2g_heff_apply_profile": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_plan_destroy": (_i, [_vp]),
     "su2g_hamiltonian_vector_multiplication": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_lanczos": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),

@@ -9,6 +9,7 @@
 
 #include "heff_plan.hpp"
 #include "kernels.hpp"
+#include "ozaki_plan.hpp"
 #include "su2_meta.hpp"
 #include "su2g.h"
 #include "tridiag.hpp"
@@ -50,6 +51,18 @@ struct su2g_heff_plan {
   su2g::GemmTile* d_tile1 = nullptr;
   su2g::GemmTile* d_tile2 = nullptr;
   double* d_scratch = nullptr;
+  // split-precision work (S > 0)
+  int S = 0;
+  su2g::oz::OzWork oz;
+  uint8_t* d_packed = nullptr;
+  int* d_exps = nullptr;
+  su2g::oz::PackJob* d_jobs[3] = {nullptr, nullptr, nullptr};
+  int2* d_units[3] = {nullptr, nullptr, nullptr};
+  su2g::oz::OzSeg* d_oseg1 = nullptr;
+  su2g::oz::OzSeg* d_oseg2 = nullptr;
+  su2g::oz::OzTile* d_otile1 = nullptr;
+  su2g::oz::OzTile* d_otile2 = nullptr;
+  int* d_err = nullptr;
   // Lanczos workspace (allocated on first use)
   double* d_krylov = nullptr;
   int krylov_vectors = 0;
@@ -63,11 +76,74 @@ struct su2g_heff_plan {
     cudaFree(d_scratch);
     cudaFree(d_krylov);
     cudaFree(d_red);
+    cudaFree(d_packed);
+    cudaFree(d_exps);
+    for (int c = 0; c < 3; ++c) {
+      cudaFree(d_jobs[c]);
+      cudaFree(d_units[c]);
+      d_jobs[c] = nullptr;
+      d_units[c] = nullptr;
+    }
+    cudaFree(d_oseg1);
+    cudaFree(d_oseg2);
+    cudaFree(d_otile1);
+    cudaFree(d_otile2);
+    cudaFree(d_err);
     d_seg1 = d_seg2 = nullptr;
     d_tile1 = d_tile2 = nullptr;
     d_scratch = d_krylov = d_red = nullptr;
+    d_packed = nullptr;
+    d_exps = d_err = nullptr;
+    d_oseg1 = d_oseg2 = nullptr;
+    d_otile1 = d_otile2 = nullptr;
   }
 };
+
+namespace {
+int slices_of_mode(int mode) {
+  if (mode == SU2G_MODE_F64) return 0;
+  if (mode == SU2G_MODE_SPLIT_BF16) return 7;
+  if (mode == SU2G_MODE_SPLIT_BF16_FAST) return 6;
+  return -1;
+}
+
+su2g::Bases make_bases(const su2g_heff_plan* p, const double* psi, double* y) {
+  su2g::Bases b;
+  b.p[su2g::kBufAbs] = 0;
+  b.p[su2g::kBufPsi] = reinterpret_cast<uintptr_t>(psi);
+  b.p[su2g::kBufY] = reinterpret_cast<uintptr_t>(y);
+  b.p[su2g::kBufScratch] = reinterpret_cast<uintptr_t>(p->d_scratch);
+  return b;
+}
+
+// device buffers of the split-precision work, and the one-time packing of
+// the operators (they stay fixed for the lifetime of the plan)
+cudaError_t setup_split(su2g_heff_plan* p) {
+  su2g::oz::OzWork& w = p->oz;
+  cudaError_t e = cudaMalloc((void**)&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
+  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+    e = upload(w.jobs[c], &p->d_jobs[c]);
+    if (e == cudaSuccess) {
+      std::vector<int2> u(w.units[c].size());
+      for (size_t i = 0; i < u.size(); ++i) u[i] = make_int2(w.units[c][i].job, w.units[c][i].rt);
+      e = upload(u, &p->d_units[c]);
+    }
+  }
+  if (e == cudaSuccess) e = upload(w.seg1, &p->d_oseg1);
+  if (e == cudaSuccess) e = upload(w.seg2, &p->d_oseg2);
+  if (e == cudaSuccess) e = upload(w.tile1, &p->d_otile1);
+  if (e == cudaSuccess) e = upload(w.tile2, &p->d_otile2);
+  if (e != cudaSuccess) return e;
+  const su2g::Bases b = make_bases(p, nullptr, nullptr);
+  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), b, p->d_packed, p->d_exps,
+                            nullptr);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  return e;
+}
+}  // namespace
 
 extern "C" {
 
@@ -132,9 +208,11 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
                           su2g_heff_plan** plan) {
   if (!plan) return fail(SU2G_EINVAL, "plan_create: null output");
   *plan = nullptr;
-  if (mode != SU2G_MODE_F64) return fail(SU2G_EUNSUPPORTED, "plan_create: mode not available in this build");
+  const int S = slices_of_mode(mode);
+  if (S < 0) return fail(SU2G_EINVAL, "plan_create: unknown mode");
   su2g_heff_plan* p = new su2g_heff_plan();
   p->mode = mode;
+  p->S = S;
   std::string err;
   int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &p->work, &err);
   if (rc) {
@@ -147,6 +225,15 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
   if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
   if (e == cudaSuccess && p->work.scratch_len > 0)
     e = cudaMalloc((void**)&p->d_scratch, p->work.scratch_len * sizeof(double));
+  if (e == cudaSuccess && S > 0) {
+    rc = su2g::oz::build_ozaki_work(p->work, S, &p->oz, &err);
+    if (rc) {
+      p->release();
+      delete p;
+      return fail(rc, err);
+    }
+    e = setup_split(p);
+  }
   if (e != cudaSuccess) {
     p->release();
     delete p;
@@ -157,14 +244,33 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
 }
 
 int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
-                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef,
-                            double* flops, int64_t* scratch_len) {
+                            const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                            double* flops, int64_t* scratch_bytes) {
+  const int S = slices_of_mode(mode);
+  if (S < 0) return fail(SU2G_EINVAL, "plan_validate: unknown mode");
   su2g::HeffWork w;
   std::string err;
   int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err);
   if (rc) return fail(rc, err);
+  int64_t bytes = w.scratch_len * (int64_t)sizeof(double);
+  if (S > 0) {
+    su2g::oz::OzWork oz;
+    rc = su2g::oz::build_ozaki_work(w, S, &oz, &err);
+    if (rc) return fail(rc, err);
+    bytes += oz.packed_bytes + oz.exp_len * (int64_t)sizeof(int);
+  }
   if (flops) *flops = w.flops;
-  if (scratch_len) *scratch_len = w.scratch_len;
+  if (scratch_bytes) *scratch_bytes = bytes;
+  return SU2G_OK;
+}
+
+int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
+  if (!p || !code) return fail(SU2G_EINVAL, "plan_status: bad arguments");
+  *code = 0;
+  if (!p->d_err) return SU2G_OK;
+  SU2G_CUDA(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  SU2G_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+  if (*code) return fail(SU2G_ETIMEOUT, "a bounded device wait gave up (code " + std::to_string(*code) + ")");
   return SU2G_OK;
 }
 
@@ -173,8 +279,12 @@ int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len
   if (!p) return fail(SU2G_EINVAL, "plan_info: null plan");
   if (flops) *flops = p->work.flops;
   if (psi_len) *psi_len = p->work.psi.total;
-  if (scratch_bytes) *scratch_bytes = p->work.scratch_len * (int64_t)sizeof(double);
-  if (ntiles) *ntiles = (int)(p->work.tile1.size() + p->work.tile2.size());
+  if (scratch_bytes)
+    *scratch_bytes = p->work.scratch_len * (int64_t)sizeof(double) + p->oz.packed_bytes +
+                     p->oz.exp_len * (int64_t)sizeof(int);
+  if (ntiles)
+    *ntiles = p->S > 0 ? (int)(p->oz.tile1.size() + p->oz.tile2.size())
+                       : (int)(p->work.tile1.size() + p->work.tile2.size());
   return SU2G_OK;
 }
 
@@ -183,13 +293,69 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
   if (p->work.psi.total > 0 && (!psi || !y)) return fail(SU2G_EINVAL, "heff_apply: null vector");
   if (psi == y && psi) return fail(SU2G_EINVAL, "heff_apply: psi and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
-  su2g::Bases b;
-  b.p[su2g::kBufAbs] = 0;
-  b.p[su2g::kBufPsi] = reinterpret_cast<uintptr_t>(psi);
-  b.p[su2g::kBufY] = reinterpret_cast<uintptr_t>(y);
-  b.p[su2g::kBufScratch] = reinterpret_cast<uintptr_t>(p->d_scratch);
-  SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st));
-  SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st));
+  const su2g::Bases b = make_bases(p, psi, y);
+  if (p->S == 0) {
+    SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st));
+    SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st));
+    return SU2G_OK;
+  }
+  const su2g::oz::OzWork& w = p->oz;
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), b, p->d_packed,
+                                  p->d_exps, st));
+  SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile1, (int)w.tile1.size(), p->d_oseg1, p->d_packed, p->d_exps, b,
+                                        p->d_err, st));
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), b, p->d_packed,
+                                  p->d_exps, st));
+  SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
+                                        p->d_err, st));
+  return SU2G_OK;
+}
+
+int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, void* stream, double* ms,
+                            int* nlaunch) {
+  if (!p || !ms || !nlaunch) return fail(SU2G_EINVAL, "apply_profile: bad arguments");
+  if (psi == y && psi) return fail(SU2G_EINVAL, "apply_profile: psi and y must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  const su2g::Bases b = make_bases(p, psi, y);
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i) SU2G_CUDA(cudaEventCreate(&ev[i]));
+  cudaError_t e = cudaEventRecord(ev[0], st);
+  int n = 0;
+  if (p->S == 0) {
+    if (e == cudaSuccess) e = su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess) e = su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
+    n = 2;
+  } else {
+    const su2g::oz::OzWork& w = p->oz;
+    if (e == cudaSuccess)
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), b, p->d_packed, p->d_exps,
+                                st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess)
+      e = su2g::oz::launch_ozaki_gemm(p->S, p->d_otile1, (int)w.tile1.size(), p->d_oseg1, p->d_packed, p->d_exps, b,
+                                      p->d_err, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
+    if (e == cudaSuccess)
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), b, p->d_packed, p->d_exps,
+                                st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
+    if (e == cudaSuccess)
+      e = su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
+                                      p->d_err, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
+    n = 4;
+  }
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    float t = 0;
+    e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+    ms[i] = t;
+  }
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  if (e != cudaSuccess) return cuda_fail(e, "apply_profile");
+  *nlaunch = n;
   return SU2G_OK;
 }
 

@@ -186,6 +186,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         const int seg0 = (int)w.seg1.size();
         w.seg1.push_back(g);
         add_tiles(w.tile1, T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1, a);
+        w.blk1.push_back(OutBlock{T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1});
         w.scratch_len += (int64_t)b * ms * c;
         w.flops += 2.0 * a * b * (double)ms * c;
         w.max_k = std::max<int64_t>(w.max_k, a);
@@ -278,6 +279,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
       }
     }
     add_tiles(w.tile2, P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
+    w.blk2.push_back(OutBlock{P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0});
   }
 
   // heaviest tiles first: the block scheduler then approximates LPT order

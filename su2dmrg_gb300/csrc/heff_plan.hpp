@@ -22,9 +22,21 @@
 
 namespace su2g {
 
+// One output block of a phase and the contiguous run of block products
+// (GemmSeg, each over its full K) that feed it.
+struct OutBlock {
+  int64_t c;
+  int64_t c_len;
+  int c_buf;
+  int ldc;
+  int M, N;
+  int seg0, nseg;
+};
+
 struct HeffWork {
   Struct psi;  // layout of psi and y
   std::vector<GemmSeg> seg1, seg2;
+  std::vector<OutBlock> blk1, blk2;
   std::vector<GemmTile> tile1, tile2;
   int64_t scratch_len = 0;  // doubles of intermediate blocks
   double flops = 0;         // algorithmic FLOPs of one application

@@ -18,4 +18,15 @@ cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* scra
 cudaError_t launch_axpy(double alpha, const double* x, double* y, int64_t n, cudaStream_t stream);
 cudaError_t launch_scale(double alpha, double* x, int64_t n, cudaStream_t stream);
 
+namespace oz {
+struct PackJob;
+struct OzSeg;
+struct OzTile;
+cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, const Bases& bases,
+                        uint8_t* packed, int* exps, cudaStream_t stream);
+cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
+                              const int* exps, const Bases& bases, int* err, cudaStream_t stream);
+int gemm_smem_bytes(int S);
+}  // namespace oz
+
 }  // namespace su2g

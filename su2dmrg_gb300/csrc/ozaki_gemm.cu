@@ -1,0 +1,353 @@
+// Split-precision tile GEMM on the tcgen05 tensor cores (representation in
+// ozaki.hpp).  One CTA computes one 128 x 64 output tile:
+//
+//   warp 4, lane 0  producer + MMA issuer: bulk-copies the packed A (S slices
+//                   x 128 x 32) and B (S slices x 64 x 32) units of each K
+//                   stage into a two-stage shared-memory ring
+//                   (cp.async.bulk + mbarrier transaction counts) and issues
+//                   the BF16 MMAs: for every digit pair (p, q) with
+//                   p + q <= S + 1, D[g = p+q] += A_p B_q^T, one FP32 TMEM
+//                   accumulator of 128 lanes x 64 columns per group g;
+//   warps 0-3       epilogue: after every K chunk of 128 (or segment end) they
+//                   read the S group sums from TMEM (tcgen05.ld, lane = tile
+//                   row), convert them exactly to integers, weight them by
+//                   2^(49 - 7g) and add them, aligned to the tile's largest
+//                   exponents, into 64 int64 accumulators per thread; at the
+//                   end each thread scales its row to FP64 and stores it.
+//
+// Every mbarrier wait is bounded; on time-out the CTA records an error code
+// in *err, drains its outstanding tensor-core work (bounded) and returns.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.hpp"
+#include "ozaki.hpp"
+
+namespace su2g {
+namespace oz {
+namespace {
+
+constexpr int kThreads = 160;  // 4 epilogue warps + 1 producer/MMA warp
+constexpr long long kWaitIters = 1ll << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
+  for (long long i = 0; i < kWaitIters; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+// K-major, no swizzle: core matrices 8 rows x 16 B; LBO = 128 B between
+// K-adjacent cores, SBO = 512 B between 8-row groups (32 k per stage).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)(128 >> 4) << 16;
+  d |= (uint64_t)(512 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// kind::f16, BF16 x BF16 -> FP32, both K-major, M = 128, N = 64
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) |
+                            ((uint32_t)(kTM >> 4) << 24);
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// exact FP32 integer (|v| < 2^22) to int32: 1.5*2^23 + v keeps v in the low mantissa bits
+__device__ __forceinline__ int f32_to_int_exact(uint32_t bits) {
+  const float v = __uint_as_float(bits) + 12582912.0f;
+  return (int)(__float_as_uint(v) - 0x4B400000u);
+}
+
+__device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
+
+template <int S>
+struct Smem {
+  static constexpr int kA = a_unit_bytes(S);
+  static constexpr int kB = b_unit_bytes(S);
+  static constexpr int kStage = kA + kB;
+  static constexpr int kBytes = 2 * kStage + 1024;  // + alignment slack
+};
+
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restrict__ tiles, const OzSeg* __restrict__ segs,
+                                                          const uint8_t* __restrict__ packed,
+                                                          const int* __restrict__ exps, Bases bases, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_accf, bar_acce, bar_drain;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int fmax_sh[kTN];
+  __shared__ int abort_sh;
+
+  const OzTile t = tiles[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(&bar_full[i]), 1);
+      mbar_init(smem_u32(&bar_empty[i]), 1);
+    }
+    mbar_init(smem_u32(&bar_accf), 1);
+    mbar_init(smem_u32(&bar_acce), 4);
+    mbar_init(smem_u32(&bar_drain), 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp == 4) {
+    // ===================== producer + MMA issuer =====================
+    if (lane == 0) {
+      int total = 0;
+      for (int s = 0; s < t.nseg; ++s) total += segs[t.seg0 + s].nks;
+      const uint32_t sA[2] = {smem_u32(smem), smem_u32(smem + Smem<S>::kStage)};
+      const uint32_t sB[2] = {sA[0] + Smem<S>::kA, sA[1] + Smem<S>::kA};
+      // load cursor
+      int ls = 0, lks = 0;
+      auto load = [&](int it) -> bool {
+        const int st = it & 1;
+        if (it >= 2 && !mbar_wait(smem_u32(&bar_empty[st]), ((it >> 1) - 1) & 1)) return false;
+        const OzSeg g = segs[t.seg0 + ls];
+        const uint8_t* a = packed + g.a_unit + (int64_t)lks * a_unit_bytes(S) * 1;
+        const uint8_t* b = packed + g.b_unit + (int64_t)lks * b_unit_bytes(S) * 1;
+        mbar_expect_tx(smem_u32(&bar_full[st]), Smem<S>::kStage);
+        bulk_g2s(sA[st], a, Smem<S>::kA, smem_u32(&bar_full[st]));
+        bulk_g2s(sB[st], b, Smem<S>::kB, smem_u32(&bar_full[st]));
+        if (++lks == g.nks) {
+          lks = 0;
+          ++ls;
+        }
+        return true;
+      };
+      bool ok = true;
+      int loaded = 0;
+      if (total > 0) ok = load(loaded++);
+      if (ok && total > 1) ok = load(loaded++);
+      int it = 0, chunk = 0;
+      for (int s = 0; s < t.nseg && ok; ++s) {
+        const int nks = segs[t.seg0 + s].nks;
+        for (int ks = 0; ks < nks && ok; ++ks, ++it) {
+          const int st = it & 1;
+          if (!mbar_wait(smem_u32(&bar_full[st]), (it >> 1) & 1)) { ok = false; break; }
+          const bool first = (ks % kChunkStages) == 0;
+          if (first && chunk > 0 && !mbar_wait(smem_u32(&bar_acce), (chunk - 1) & 1)) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int kk = 0; kk < kKS / 16; ++kk) {
+#pragma unroll
+            for (int g = 2; g <= S + 1; ++g) {
+              const int p0 = (g - S > 1) ? g - S : 1;
+              const int p1 = (g - 1 < S) ? g - 1 : S;
+#pragma unroll
+              for (int p = p0; p <= p1; ++p) {
+                const int q = g - p;
+                const uint64_t ad = smem_desc(sA[st] + (p - 1) * (kTM * kKS * 2) + kk * 256);
+                const uint64_t bd = smem_desc(sB[st] + (q - 1) * (kTN * kKS * 2) + kk * 256);
+                const uint32_t acc = (first && kk == 0 && p == p0) ? 0u : 1u;
+                mma(tmem + (uint32_t)((g - 2) * kTN), ad, bd, acc);
+              }
+            }
+          }
+          mma_commit(smem_u32(&bar_empty[st]));
+          const bool last = ((ks % kChunkStages) == kChunkStages - 1) || ks == nks - 1;
+          if (last) {
+            mma_commit(smem_u32(&bar_accf));
+            ++chunk;
+          }
+          if (loaded < total) {
+            if (!load(loaded)) { ok = false; break; }
+            ++loaded;
+          }
+        }
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        atomicExch(&abort_sh, 1);
+      }
+      // drain: every MMA issued so far has completed once this commit arrives
+      mma_commit(smem_u32(&bar_drain));
+      if (!mbar_wait(smem_u32(&bar_drain), 0)) atomicExch(err, 2);
+      // bulk copies still in flight (possible only after an abort) must land
+      // before the CTA exits: wait for every issued load's transaction count
+      if (!ok) {
+        for (int i = it; i < loaded; ++i) mbar_wait(smem_u32(&bar_full[i & 1]), (i >> 1) & 1);
+      }
+    }
+  } else {
+    // ============================ epilogue ============================
+    const int row = warp * 32 + lane;  // TMEM lane == tile row
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    // largest exponents over the tile's segments: rows here, columns shared
+    int emax = kExpZero;
+    for (int s = 0; s < t.nseg; ++s) emax = max(emax, exps[segs[t.seg0 + s].a_exp + row]);
+    if (tid < kTN) {
+      int f = kExpZero;
+      for (int s = 0; s < t.nseg; ++s) f = max(f, exps[segs[t.seg0 + s].b_exp + tid]);
+      fmax_sh[tid] = f;
+    }
+    // the only block-wide barrier of the epilogue, taken before any bounded
+    // wait so that a time-out can never leave a warp stranded in it
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    long long acc[kTN];
+#pragma unroll
+    for (int j = 0; j < kTN; ++j) acc[j] = 0;
+    int chunk = 0;
+    bool ok = true;
+    for (int s = 0; s < t.nseg && ok; ++s) {
+      const OzSeg g = segs[t.seg0 + s];
+      const int ea = exps[g.a_exp + row];
+      const int sha = (ea == kExpZero) ? 1000 : emax - ea;
+      const int* __restrict__ fb = exps + g.b_exp;
+      const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
+      for (int c = 0; c < nchunks; ++c, ++chunk) {
+        if (!mbar_wait(smem_u32(&bar_accf), chunk & 1)) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int cb = 0; cb < kTN / 16; ++cb) {
+          long long v[16];
+#pragma unroll
+          for (int x = 0; x < 16; ++x) v[x] = 0;
+#pragma unroll
+          for (int gg = 2; gg <= S + 1; ++gg) {
+            uint32_t r[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)((gg - 2) * kTN + cb * 16), r);
+            tmem_wait_ld();
+#pragma unroll
+            for (int x = 0; x < 16; ++x) v[x] += shl_signed((long long)f32_to_int_exact(r[x]), 49 - 7 * gg);
+          }
+#pragma unroll
+          for (int x = 0; x < 16; ++x) {
+            const int j = cb * 16 + x;
+            const int fj = fb[j];
+            const int sh = (fj == kExpZero) ? 1000 : sha + fmax_sh[j] - fj;
+            if (sh == 0) {
+              acc[j] += v[x];
+            } else if (sh < 63) {
+              acc[j] += (v[x] + (1ll << (sh - 1))) >> sh;  // round to nearest
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&bar_acce));
+      }
+    }
+    if (!ok) {
+      atomicExch(err, 3);
+      atomicExch(&abort_sh, 1);
+    }
+    // ---- store the row: C = acc * 2^(emax + fmax - 7(S+1) + drop) ----
+    double* C = resolve(bases, t.c_buf, t.c);
+    if (row < t.mlen) {
+      const int ebase = emax - kBits * (S + 1) + fixed_drop(S);
+#pragma unroll
+      for (int j = 0; j < kTN; ++j) {
+        if (j < t.nlen) {
+          const int f = fmax_sh[j];
+          double out = 0.0;
+          if (ok && emax != kExpZero && f != kExpZero && acc[j] != 0) out = ldexp((double)acc[j], ebase + f);
+          C[(int64_t)(t.m0 + row) + (int64_t)(t.n0 + j) * t.ldc] = out;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+}  // namespace
+
+int gemm_smem_bytes(int S) {
+  switch (S) {
+    case 6: return Smem<6>::kBytes;
+    case 7: return Smem<7>::kBytes;
+    case 8: return Smem<8>::kBytes;
+  }
+  return 0;
+}
+
+cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
+                              const int* exps, const Bases& bases, int* err, cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  const int smem = gemm_smem_bytes(S);
+  cudaError_t e = cudaSuccess;
+  switch (S) {
+    case 6:
+      e = cudaFuncSetAttribute(ozaki_gemm<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e == cudaSuccess) ozaki_gemm<6><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, bases, err);
+      break;
+    case 7:
+      e = cudaFuncSetAttribute(ozaki_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e == cudaSuccess) ozaki_gemm<7><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, bases, err);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+}  // namespace oz
+}  // namespace su2g

@@ -1,0 +1,178 @@
+// Host-side construction of the split-precision work: pack jobs (one per
+// distinct operand view, deduplicated) and the 128 x 64 output tiles with their
+// segments, derived from the block-level products of the H_eff work list.
+#include "ozaki_plan.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+namespace su2g {
+namespace oz {
+namespace {
+
+using Key = std::tuple<int, int64_t, int64_t, int64_t, int, int, int, uint64_t>;
+
+struct Builder {
+  int S;
+  OzWork* w;
+  std::map<Key, std::pair<int, int>> index;  // key -> (class, job index)
+  std::vector<PackJob>* lists[3];
+
+  // class 0 = operator (packed once), 1 = from psi, 2 = from the phase-1 intermediates
+  int job(int src_buf, int64_t src, int64_t ld_r, int64_t ld_k, int R, int K, int rt, double alpha) {
+    uint64_t abits;
+    std::memcpy(&abits, &alpha, 8);
+    const Key key{src_buf, src, ld_r, ld_k, R, K, rt, abits};
+    auto it = index.find(key);
+    const int cls = src_buf == kBufAbs ? 0 : (src_buf == kBufPsi ? 1 : 2);
+    if (it != index.end()) return it->second.second;
+    PackJob j;
+    j.src = src;
+    j.src_buf = src_buf;
+    j.R = R;
+    j.K = K;
+    j.ld_r = ld_r;
+    j.ld_k = ld_k;
+    j.rt = rt;
+    j.nrt = (R + rt - 1) / rt;
+    j.nkt = (K + kKS - 1) / kKS;
+    j.alpha = alpha;
+    j.dst = w->packed_bytes;
+    j.exp = w->exp_len;
+    w->packed_bytes += (int64_t)j.nrt * j.nkt * S * rt * kKS * 2;
+    w->exp_len += (int64_t)j.nrt * rt;
+    lists[cls]->push_back(j);
+    const int id = (int)lists[cls]->size() - 1;
+    index[key] = {cls, id};
+    return id;
+  }
+  const PackJob& get(int src_buf, int id) {
+    const int cls = src_buf == kBufAbs ? 0 : (src_buf == kBufPsi ? 1 : 2);
+    return (*lists[cls])[id];
+  }
+};
+
+int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<OutBlock>& blks,
+                std::vector<OzSeg>* oseg, std::vector<OzTile>* otile, std::string* err) {
+  const int S = B.S;
+  for (const OutBlock& ob : blks) {
+    // pack jobs of every product of this block
+    std::vector<std::pair<int, int>> ids;  // (A job, B job) indices
+    std::vector<std::pair<int, int>> bufs;
+    for (int s = ob.seg0; s < ob.seg0 + ob.nseg; ++s) {
+      const GemmSeg& g = segs[s];
+      double aa = 1.0, ab = 1.0;
+      if (g.alpha != 1.0) {
+        if (g.b_buf == kBufAbs) ab = g.alpha;
+        else if (g.a_buf == kBufAbs) aa = g.alpha;
+        else {
+          *err = "split mode: a scaled product needs one operator operand";
+          return SU2G_EUNSUPPORTED;
+        }
+      }
+      const int64_t a_ldr = g.transA ? g.lda : 1, a_ldk = g.transA ? 1 : g.lda;
+      const int ja = B.job(g.a_buf, g.a, a_ldr, a_ldk, ob.M, g.K, kTM, aa);
+      const int jb = B.job(g.b_buf, g.b, g.ldb, 1, ob.N, g.K, kTN, ab);
+      ids.push_back({ja, jb});
+      bufs.push_back({g.a_buf, g.b_buf});
+    }
+    int64_t ktot = 0;
+    for (int s = 0; s < ob.nseg; ++s) ktot += (int64_t)segs[ob.seg0 + s].K;
+    if (ktot >= (int64_t)1 << 17) {
+      *err = "split mode: more than 2^17 contracted values feed one output block";
+      return SU2G_EUNSUPPORTED;
+    }
+    for (int m0 = 0; m0 < ob.M; m0 += kTM)
+      for (int n0 = 0; n0 < ob.N; n0 += kTN) {
+        OzTile t;
+        t.c = ob.c;
+        t.c_buf = ob.c_buf;
+        t.ldc = ob.ldc;
+        t.m0 = m0;
+        t.n0 = n0;
+        t.mlen = std::min(kTM, ob.M - m0);
+        t.nlen = std::min(kTN, ob.N - n0);
+        t.seg0 = (int)oseg->size();
+        t.nseg = ob.nseg;
+        t.work = 0;
+        for (int s = 0; s < ob.nseg; ++s) {
+          const PackJob& a = B.get(bufs[s].first, ids[s].first);
+          const PackJob& b = B.get(bufs[s].second, ids[s].second);
+          OzSeg z;
+          z.a_unit = a.dst + (int64_t)(m0 / kTM) * a.nkt * a_unit_bytes(S);
+          z.b_unit = b.dst + (int64_t)(n0 / kTN) * b.nkt * b_unit_bytes(S);
+          z.a_exp = a.exp + m0;
+          z.b_exp = b.exp + n0;
+          z.nks = a.nkt;
+          z.pad = 0;
+          t.work += z.nks;
+          oseg->push_back(z);
+        }
+        otile->push_back(t);
+      }
+  }
+  std::stable_sort(otile->begin(), otile->end(), [](const OzTile& x, const OzTile& y) { return x.work > y.work; });
+  return SU2G_OK;
+}
+
+}  // namespace
+
+int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
+  OzWork& w = *out;
+  w = OzWork();
+  w.S = S;
+  Builder B;
+  B.S = S;
+  B.w = &w;
+  B.lists[0] = &w.jobs[0];
+  B.lists[1] = &w.jobs[1];
+  B.lists[2] = &w.jobs[2];
+  int rc = build_phase(B, hw.seg1, hw.blk1, &w.seg1, &w.tile1, err);
+  if (rc) return rc;
+  rc = build_phase(B, hw.seg2, hw.blk2, &w.seg2, &w.tile2, err);
+  if (rc) return rc;
+  for (int c = 0; c < 3; ++c) {
+    w.units[c].clear();
+    for (int j = 0; j < (int)w.jobs[c].size(); ++j)
+      for (int r = 0; r < w.jobs[c][j].nrt; ++r) w.units[c].push_back(Unit{j, r});
+  }
+  return validate_ozaki_work(w, err);
+}
+
+int validate_ozaki_work(const OzWork& w, std::string* err) {
+  for (int c = 0; c < 3; ++c)
+    for (const PackJob& j : w.jobs[c]) {
+      const int64_t bytes = (int64_t)j.nrt * j.nkt * w.S * j.rt * kKS * 2;
+      if (j.dst < 0 || j.dst % 1024 || j.dst + bytes > w.packed_bytes || j.exp < 0 ||
+          j.exp + (int64_t)j.nrt * j.rt > w.exp_len || j.R <= 0 || j.K <= 0 || (j.rt != kTM && j.rt != kTN)) {
+        *err = "split mode: pack job out of bounds";
+        return SU2G_EINVAL;
+      }
+    }
+  auto check = [&](const std::vector<OzTile>& tiles, const std::vector<OzSeg>& segs) -> bool {
+    for (const OzTile& t : tiles) {
+      if (t.seg0 < 0 || t.nseg < 0 || t.seg0 + t.nseg > (int)segs.size() || t.mlen <= 0 || t.mlen > kTM ||
+          t.nlen <= 0 || t.nlen > kTN || t.ldc < t.m0 + t.mlen)
+        return false;
+      for (int s = t.seg0; s < t.seg0 + t.nseg; ++s) {
+        const OzSeg& z = segs[s];
+        if (z.nks <= 0 || z.a_unit < 0 || z.b_unit < 0 ||
+            z.a_unit + (int64_t)z.nks * a_unit_bytes(w.S) > w.packed_bytes ||
+            z.b_unit + (int64_t)z.nks * b_unit_bytes(w.S) > w.packed_bytes || z.a_unit % 1024 || z.b_unit % 1024 ||
+            z.a_exp < 0 || z.a_exp + kTM > w.exp_len || z.b_exp < 0 || z.b_exp + kTN > w.exp_len)
+          return false;
+      }
+    }
+    return true;
+  };
+  if (!check(w.tile1, w.seg1) || !check(w.tile2, w.seg2)) {
+    *err = "split mode: tile segment out of bounds";
+    return SU2G_EINVAL;
+  }
+  return SU2G_OK;
+}
+
+}  // namespace oz
+}  // namespace su2g

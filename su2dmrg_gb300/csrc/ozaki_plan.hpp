@@ -1,0 +1,35 @@
+// Split-precision work list (see ozaki.hpp for the representation).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "heff_plan.hpp"
+#include "ozaki.hpp"
+
+namespace su2g {
+namespace oz {
+
+struct Unit {  // one CTA of the pack kernel; same layout as int2
+  int job, rt;
+};
+
+struct OzWork {
+  int S = 7;
+  // pack jobs by source: 0 = operators (packed once at plan creation),
+  // 1 = blocks of psi (packed at the start of every application),
+  // 2 = phase-1 intermediates (packed between the two phases)
+  std::vector<PackJob> jobs[3];
+  std::vector<Unit> units[3];
+  std::vector<OzSeg> seg1, seg2;
+  std::vector<OzTile> tile1, tile2;
+  int64_t packed_bytes = 0;  // bytes of all packed operands
+  int64_t exp_len = 0;       // int32 row exponents of all packed operands
+};
+
+// The operand that is not an operator (psi or an intermediate) carries no
+// scale factor: a product's alpha is folded into its operator operand.
+int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err);
+int validate_ozaki_work(const OzWork& w, std::string* err);
+
+}  // namespace oz
+}  // namespace su2g

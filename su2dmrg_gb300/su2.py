@@ -179,14 +179,20 @@ class HeffPlan:
         self.mode = mode
 
     @staticmethod
-    def validate(psi: Su2Struct, terms, hl=None, hr=None) -> dict:
-        """Host-only dry run: builds the work list and bounds-checks every
-        access (su2g_heff_plan_validate).  Data may be host arrays."""
+    def validate(psi: Su2Struct, terms, hl=None, hr=None, mode: int = capi.MODE_F64) -> dict:
+        """Host-only dry run: builds the work lists of `mode` and bounds-checks
+        every access (su2g_heff_plan_validate).  Data may be host arrays."""
         fl = ctypes.c_double()
-        sl = ctypes.c_int64()
+        sb = ctypes.c_int64()
         with _PlanArgs(psi, terms, hl, hr) as a:
-            check(lib().su2g_heff_plan_validate(*a.args, ctypes.addressof(fl), ctypes.addressof(sl)))
-        return {"flops": fl.value, "scratch_len": sl.value}
+            check(lib().su2g_heff_plan_validate(*a.args, int(mode), ctypes.addressof(fl), ctypes.addressof(sb)))
+        return {"flops": fl.value, "scratch_bytes": sb.value}
+
+    def status(self) -> int:
+        """Device error word (0 = no bounded wait gave up); raises on time-out."""
+        code = ctypes.c_int()
+        check(lib().su2g_heff_plan_status(self._h, ctypes.addressof(code)))
+        return code.value
 
     @property
     def handle(self):
@@ -203,6 +209,15 @@ class HeffPlan:
 
     def apply(self, psi, y, stream=None) -> None:
         check(lib().su2g_heff_apply(self._h, ptr(psi), ptr(y), stream_handle(stream)))
+
+    def apply_profile(self, psi, y, stream=None) -> list:
+        """One application with per-launch device times in ms (see
+        su2g_heff_apply_profile)."""
+        ms = (ctypes.c_double * 8)()
+        n = ctypes.c_int()
+        check(lib().su2g_heff_apply_profile(self._h, ptr(psi), ptr(y), stream_handle(stream), ctypes.addressof(ms),
+                                            ctypes.addressof(n)))
+        return [ms[i] for i in range(n.value)]
 
     def lanczos(self, psi, mlanc: int = 5, stream=None):
         e = ctypes.c_double()

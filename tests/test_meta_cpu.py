@@ -111,7 +111,7 @@ def test_work_list_bounds_on_cpu(su2lib, D, nspin1):
 
     w = synthetic_heff(D=D, nspin1=nspin1, seed=1234)
     r = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr)
-    assert r["flops"] > 0 and r["scratch_len"] > 0
+    assert r["flops"] > 0 and r["scratch_bytes"] > 0
     if D == 2000:
         # algorithmic FLOPs of the width-20 D=2000 step (18 spin-1 pairs + 2 spin-0)
         assert 1.0e11 < r["flops"] < 2.0e11
@@ -132,3 +132,15 @@ def test_golden_cases_build_valid_work_lists(su2lib, oracle):
         r = HeffPlan.validate(vs, [(s1, g["x1"], s2, g["x2"], 1.0)])
         prob = oracle.HeffProblem(vs, [(s1, g["x1"], s2, g["x2"], 1.0)])
         assert r["flops"] == oracle.heff_flops(prob)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_split_work_lists_on_cpu(su2lib, mode):
+    """Split-precision pack jobs and tiles at the benchmark shape, bounds
+    checked on the host (no GPU)."""
+    from su2dmrg_gb300.su2 import HeffPlan
+    from su2dmrg_gb300.workloads import synthetic_heff
+
+    w = synthetic_heff(D=2000, nspin1=18, seed=1234)
+    r = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr, mode=mode)
+    assert r["scratch_bytes"] > 2e9  # packed operator slices + intermediates
