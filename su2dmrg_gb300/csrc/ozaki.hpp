@@ -6,18 +6,21 @@
 // FP32 group sums).
 //
 // Representation.  Every operand X (R rows x K, the contraction index K) is
-// scaled per row by 2^-e_r so that |X_rk| 2^-e_r < 1/4, rounded to the
+// scaled per row by 2^-e_r so that |X_rk| 2^-e_r < 1/2, rounded to the
 // integer N_rk = rint(X_rk 2^(7S - e_r)) and written as S balanced base-128
-// digits  N = sum_p d_p 2^(7(S-p)),  |d_p| <= 64,  each exact in BF16.
+// digits  N = sum_p d_p 2^(7(S-p)),  |d_p| <= 64 (65 for the leading digit),
+// each exact in BF16.
 // A product C = A B^T then is
 //     C_ij = 2^(e_i + f_j - 7(S+1)) sum_{g=2}^{S+1} 2^(7(S+1-g)) G_g(i,j),
 //     G_g  = sum_{p+q=g} sum_k dA_p(i,k) dB_q(j,k)
 // (pairs with p+q > S+1 are dropped: they weigh below 2^-7(S+2)).  With
-// |d| <= 64 and at most S pairs per group, a group summed over 128 values of
+// |d| <= 65 and at most S pairs per group, a group summed over 128 values of
 // k stays below 2^22 in magnitude, so the FP32 tensor-core accumulation of
 // one group over one K chunk of 128 is exact, and the chunk sums are combined
-// in 64-bit integers.  The only rounding is in forming N (2^-47 relative to
-// the row maximum for S = 7) and in the dropped pairs.
+// in 64-bit integers, C = 2^(e_i + f_j - 48) sum_g 2^(48 - 7g) G_g.  The only
+// rounding is in forming N (2^-48 relative to the row maximum for S = 7), in
+// the dropped pairs, and in aligning products of different exponents to the
+// tile's common fixed point (2^-46 of the tile's largest product).
 //
 // Packed operand layout (bytes), built by the pack kernel:
 //   [row tile rt][k tile kt][slice p][rows RT x 32 k, tcgen05 canonical
@@ -45,12 +48,12 @@ constexpr int kTN = 64;             // tile columns (MMA N)
 constexpr int kKS = 32;             // K per shared-memory stage
 constexpr int kChunkStages = 4;     // exact FP32 group sums over 4 stages = 128 k
 constexpr int kExpZero = -(1 << 20);  // exponent of an all-zero row
+constexpr int kFixedTop = 48;         // fixed point: group g weighs 2^(kFixedTop - 7g)
+constexpr int kMaxSegs = 1024;        // segments feeding one output tile
 
 SU2G_HD constexpr int pairs(int S) { return S * (S + 1) / 2; }
 SU2G_HD constexpr int a_unit_bytes(int S) { return S * kTM * kKS * 2; }
 SU2G_HD constexpr int b_unit_bytes(int S) { return S * kTN * kKS * 2; }
-// fixed-point shift applied to the sum of chunks: see ozaki_gemm.cu
-SU2G_HD constexpr int fixed_drop(int S) { return kBits * S - 42; }
 
 // One FP64 operand to split: X(r, k) = alpha * src[r*ld_r + k*ld_k].
 struct PackJob {

@@ -11,9 +11,9 @@
 //   warps 0-3       epilogue: after every K chunk of 128 (or segment end) they
 //                   read the S group sums from TMEM (tcgen05.ld, lane = tile
 //                   row), convert them exactly to integers, weight them by
-//                   2^(49 - 7g) and add them, aligned to the tile's largest
-//                   exponents, into 64 int64 accumulators per thread; at the
-//                   end each thread scales its row to FP64 and stores it.
+//                   2^(48 - 7g) and add them, aligned to the tile's largest
+//                   product exponents, into 64 int64 accumulators per thread;
+//                   at the end each thread scales its row to FP64 and stores it.
 //
 // Every mbarrier wait is bounded; on time-out the CTA records an error code
 // in *err, drains its outstanding tensor-core work (bounded) and returns.
@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_accf, bar_acce, bar_drain;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int fmax_sh[kTN];
+  __shared__ int cshift_sh[kMaxSegs];
   __shared__ int abort_sh;
 
   const OzTile t = tiles[blockIdx.x];
@@ -235,12 +236,34 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     // ============================ epilogue ============================
     const int row = warp * 32 + lane;  // TMEM lane == tile row
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    // largest exponents over the tile's segments: rows here, columns shared
+    // Exponent bookkeeping.  Segment s contributes 2^(eA_s(i) + eB_s(j)) times
+    // its digit sums; moving c_s = max_i eA_s(i) (over the tile rows) from the
+    // A side to the B side leaves every product unchanged but makes the
+    // tile's reference exponents emax(i) = max_s (eA_s(i) - c_s) and
+    // fmax(j) = max_s (eB_s(j) + c_s) track the largest actual product scale
+    // (otherwise an O(1) x O(1e-3) segment and an O(1e-3) x O(1) segment would
+    // set a reference 2^10 above both).
+    for (int s = tid; s < t.nseg; s += 128) cshift_sh[s] = kExpZero;
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    for (int s = 0; s < t.nseg; ++s) {
+      const int m = __reduce_max_sync(0xffffffffu, exps[segs[t.seg0 + s].a_exp + row]);
+      if (lane == 0) atomicMax(&cshift_sh[s], m);
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    for (int s = tid; s < t.nseg; s += 128)
+      if (cshift_sh[s] == kExpZero) cshift_sh[s] = 0;
+    asm volatile("bar.sync 1, 128;" ::: "memory");
     int emax = kExpZero;
-    for (int s = 0; s < t.nseg; ++s) emax = max(emax, exps[segs[t.seg0 + s].a_exp + row]);
+    for (int s = 0; s < t.nseg; ++s) {
+      const int e = exps[segs[t.seg0 + s].a_exp + row];
+      if (e != kExpZero) emax = max(emax, e - cshift_sh[s]);
+    }
     if (tid < kTN) {
       int f = kExpZero;
-      for (int s = 0; s < t.nseg; ++s) f = max(f, exps[segs[t.seg0 + s].b_exp + tid]);
+      for (int s = 0; s < t.nseg; ++s) {
+        const int fb = exps[segs[t.seg0 + s].b_exp + tid];
+        if (fb != kExpZero) f = max(f, fb + cshift_sh[s]);
+      }
       fmax_sh[tid] = f;
     }
     // the only block-wide barrier of the epilogue, taken before any bounded
@@ -254,7 +277,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     for (int s = 0; s < t.nseg && ok; ++s) {
       const OzSeg g = segs[t.seg0 + s];
       const int ea = exps[g.a_exp + row];
-      const int sha = (ea == kExpZero) ? 1000 : emax - ea;
+      const int cs = cshift_sh[s];
+      const int sha = (ea == kExpZero) ? 1000 : emax - (ea - cs);
       const int* __restrict__ fb = exps + g.b_exp;
       const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
       for (int c = 0; c < nchunks; ++c, ++chunk) {
@@ -271,13 +295,13 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
             tmem_ld16(tmem + lane_base + (uint32_t)((gg - 2) * kTN + cb * 16), r);
             tmem_wait_ld();
 #pragma unroll
-            for (int x = 0; x < 16; ++x) v[x] += shl_signed((long long)f32_to_int_exact(r[x]), 49 - 7 * gg);
+            for (int x = 0; x < 16; ++x) v[x] += shl_signed((long long)f32_to_int_exact(r[x]), kFixedTop - kBits * gg);
           }
 #pragma unroll
           for (int x = 0; x < 16; ++x) {
             const int j = cb * 16 + x;
             const int fj = fb[j];
-            const int sh = (fj == kExpZero) ? 1000 : sha + fmax_sh[j] - fj;
+            const int sh = (fj == kExpZero) ? 1000 : sha + fmax_sh[j] - (fj + cs);
             if (sh == 0) {
               acc[j] += v[x];
             } else if (sh < 63) {
@@ -294,10 +318,10 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       atomicExch(err, 3);
       atomicExch(&abort_sh, 1);
     }
-    // ---- store the row: C = acc * 2^(emax + fmax - 7(S+1) + drop) ----
+    // ---- store the row: C = acc * 2^(emax + fmax - kFixedTop) ----
     double* C = resolve(bases, t.c_buf, t.c);
     if (row < t.mlen) {
-      const int ebase = emax - kBits * (S + 1) + fixed_drop(S);
+      const int ebase = emax - kFixedTop;
 #pragma unroll
       for (int j = 0; j < kTN; ++j) {
         if (j < t.nlen) {

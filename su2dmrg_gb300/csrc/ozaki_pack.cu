@@ -43,8 +43,8 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
     double mm = rmax[tid];
     for (int q = 1; q < parts; ++q) mm = fmax(mm, rmax[tid + q * RT]);
     mm *= fabs(job.alpha);
-    // |X| 2^-e < 1/4 : e = ilogb(max) + 3
-    const int e = (mm > 0.0) ? ilogb(mm) + 3 : kExpZero;
+    // |X| 2^-e < 1/2 : e = ilogb(max) + 2
+    const int e = (mm > 0.0) ? ilogb(mm) + 2 : kExpZero;
     rexp[tid] = e;
     exps[job.exp + r0 + tid] = e;
   }

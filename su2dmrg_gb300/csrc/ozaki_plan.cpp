@@ -84,6 +84,10 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
       *err = "split mode: more than 2^17 contracted values feed one output block";
       return SU2G_EUNSUPPORTED;
     }
+    if (ob.nseg > kMaxSegs) {
+      *err = "split mode: more than 1024 products feed one output block";
+      return SU2G_EUNSUPPORTED;
+    }
     for (int m0 = 0; m0 < ob.M; m0 += kTM)
       for (int n0 = 0; n0 < ob.N; n0 += kTN) {
         OzTile t;
