@@ -131,6 +131,25 @@ int su2g_heff_plan_destroy(su2g_heff_plan* plan);
 int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_flag, const double* vec,
                                            su2g_tensor op1, su2g_tensor op2, double* y, void* stream);
 
+/* Allocation-free form of su2g_hamiltonian_vector_multiplication, for callers
+ * that may not allocate device memory when they apply a term: engines that
+ * reserve their whole HBM budget up front, per-term calls from many host
+ * threads where cudaMalloc/cudaFree would synchronise the device, code running
+ * inside another library's callbacks.  This entry point has no counterpart in
+ * the reference.  Its intermediate blocks and work list live in fixed
+ * file-scope device arrays (SU2G_NOALLOC_* below, about 40 MiB), held by every
+ * GPU that loads libsu2g.so until the process exits; terms that need more are
+ * refused with SU2G_EINVAL.  The first call on a device looks up the arrays'
+ * device addresses (cudaGetSymbolAddress), so make it before any stream
+ * capture.  Calls share the arrays: calls that overlap on the GPU race and
+ * must be serialised by the caller.  Same arguments and result as
+ * su2g_hamiltonian_vector_multiplication, asynchronous on `stream`. */
+#define SU2G_NOALLOC_SCRATCH_DOUBLES 4194304 /* intermediate blocks: 32 MiB */
+#define SU2G_NOALLOC_MAX_TILES 65536
+#define SU2G_NOALLOC_MAX_SEGS 65536
+int su2g_hamiltonian_vector_multiplication_noalloc(const int* vec_desc, const int* vec_flag, const double* vec,
+                                                   su2g_tensor op1, su2g_tensor op2, double* y, void* stream);
+
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme
  * (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195, driven as in

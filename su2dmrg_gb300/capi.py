@@ -64,6 +64,7 @@ _PROTOS = {
     "su2g_heff_apply_profile": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_plan_destroy": (_i, [_vp]),
     "su2g_hamiltonian_vector_multiplication": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
+    "su2g_hamiltonian_vector_multiplication_noalloc": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_lanczos": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),

@@ -43,6 +43,8 @@ cudaError_t upload(const std::vector<T>& v, T** dptr) {
 }
 }  // namespace
 
+int su2g::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
 struct su2g_heff_plan {
   su2g::HeffWork work;
   int mode = SU2G_MODE_F64;

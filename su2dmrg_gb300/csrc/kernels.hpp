@@ -3,10 +3,14 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 #include "gemm_work.hpp"
 
 namespace su2g {
+
+// records the calling thread's su2g_last_error() text and returns code
+int set_last_error(int code, const std::string& msg);
 
 cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
                             cudaStream_t stream);
