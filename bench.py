@@ -329,7 +329,7 @@ def run_su2g(args):
                           "2 launches per step",
                 "achieved_definition": f"{pairs} x algorithmic FP64 FLOPs of the two GEMM launches / their time",
                 "launch_ms": {"pack_psi": prof[0], "gemm_phase1": prof[1], "pack_intermediates": prof[2],
-                              "gemm_phase2": prof[3]},
+                              "gemm_phase2": prof[3], "sum_split_tiles": prof[4]},
                 "peak_source": src}
         ref_plan = HeffPlan(w.psi, terms, hl, hr, mode=capi.MODE_F64)
         y64 = torch.empty_like(psi)

@@ -118,7 +118,7 @@ int su2g_heff_apply(su2g_heff_plan* plan, const double* psi, double* y, void* st
 /* su2g_heff_apply with a CUDA event between its launches; waits for the
  * result and writes the duration (ms) of each launch to ms[0..*nlaunch):
  * FP64 mode: phase 1, phase 2; split modes: pack psi, phase 1, pack the
- * intermediates, phase 2. */
+ * intermediates, phase 2, sum of the split phase-2 tiles. */
 int su2g_heff_apply_profile(su2g_heff_plan* plan, const double* psi, double* y, void* stream, double* ms,
                             int* nlaunch);
 int su2g_heff_plan_destroy(su2g_heff_plan* plan);

@@ -64,6 +64,7 @@ struct su2g_heff_plan {
   su2g::oz::OzSeg* d_oseg2 = nullptr;
   su2g::oz::OzTile* d_otile1 = nullptr;
   su2g::oz::OzTile* d_otile2 = nullptr;
+  su2g::oz::RedTile* d_red2 = nullptr;
   int* d_err = nullptr;
   // Lanczos workspace (allocated on first use)
   double* d_krylov = nullptr;
@@ -90,6 +91,7 @@ struct su2g_heff_plan {
     cudaFree(d_oseg2);
     cudaFree(d_otile1);
     cudaFree(d_otile2);
+    cudaFree(d_red2);
     cudaFree(d_err);
     d_seg1 = d_seg2 = nullptr;
     d_tile1 = d_tile2 = nullptr;
@@ -98,6 +100,7 @@ struct su2g_heff_plan {
     d_exps = d_err = nullptr;
     d_oseg1 = d_oseg2 = nullptr;
     d_otile1 = d_otile2 = nullptr;
+    d_red2 = nullptr;
   }
 };
 
@@ -138,6 +141,7 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   if (e == cudaSuccess) e = upload(w.seg2, &p->d_oseg2);
   if (e == cudaSuccess) e = upload(w.tile1, &p->d_otile1);
   if (e == cudaSuccess) e = upload(w.tile2, &p->d_otile2);
+  if (e == cudaSuccess) e = upload(w.red2, &p->d_red2);
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
   e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), b, p->d_packed, p->d_exps,
@@ -225,8 +229,6 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
   if (e == cudaSuccess) e = upload(p->work.seg2, &p->d_seg2);
   if (e == cudaSuccess) e = upload(p->work.tile1, &p->d_tile1);
   if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
-  if (e == cudaSuccess && p->work.scratch_len > 0)
-    e = cudaMalloc((void**)&p->d_scratch, p->work.scratch_len * sizeof(double));
   if (e == cudaSuccess && S > 0) {
     rc = su2g::oz::build_ozaki_work(p->work, S, &p->oz, &err);
     if (rc) {
@@ -234,8 +236,11 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
       delete p;
       return fail(rc, err);
     }
-    e = setup_split(p);
   }
+  const int64_t scratch_doubles = p->work.scratch_len + p->oz.partial_len;
+  if (e == cudaSuccess && scratch_doubles > 0)
+    e = cudaMalloc((void**)&p->d_scratch, scratch_doubles * sizeof(double));
+  if (e == cudaSuccess && S > 0) e = setup_split(p);
   if (e != cudaSuccess) {
     p->release();
     delete p;
@@ -259,7 +264,7 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
     su2g::oz::OzWork oz;
     rc = su2g::oz::build_ozaki_work(w, S, &oz, &err);
     if (rc) return fail(rc, err);
-    bytes += oz.packed_bytes + oz.exp_len * (int64_t)sizeof(int);
+    bytes += oz.packed_bytes + oz.exp_len * (int64_t)sizeof(int) + oz.partial_len * (int64_t)sizeof(double);
   }
   if (flops) *flops = w.flops;
   if (scratch_bytes) *scratch_bytes = bytes;
@@ -282,7 +287,7 @@ int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len
   if (flops) *flops = p->work.flops;
   if (psi_len) *psi_len = p->work.psi.total;
   if (scratch_bytes)
-    *scratch_bytes = p->work.scratch_len * (int64_t)sizeof(double) + p->oz.packed_bytes +
+    *scratch_bytes = (p->work.scratch_len + p->oz.partial_len) * (int64_t)sizeof(double) + p->oz.packed_bytes +
                      p->oz.exp_len * (int64_t)sizeof(int);
   if (ntiles)
     *ntiles = p->S > 0 ? (int)(p->oz.tile1.size() + p->oz.tile2.size())
@@ -310,6 +315,7 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
                                   p->d_exps, st));
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
+  SU2G_CUDA(su2g::oz::launch_reduce(p->d_red2, (int)w.red2.size(), b, st));
   return SU2G_OK;
 }
 
@@ -319,8 +325,8 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
   if (psi == y && psi) return fail(SU2G_EINVAL, "apply_profile: psi and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
   const su2g::Bases b = make_bases(p, psi, y);
-  cudaEvent_t ev[5];
-  for (int i = 0; i < 5; ++i) SU2G_CUDA(cudaEventCreate(&ev[i]));
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) SU2G_CUDA(cudaEventCreate(&ev[i]));
   cudaError_t e = cudaEventRecord(ev[0], st);
   int n = 0;
   if (p->S == 0) {
@@ -347,7 +353,9 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
       e = su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                       p->d_err, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
-    n = 4;
+    if (e == cudaSuccess) e = su2g::oz::launch_reduce(p->d_red2, (int)w.red2.size(), b, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[5], st);
+    n = 5;
   }
   if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
   for (int i = 0; i < n && e == cudaSuccess; ++i) {
@@ -355,7 +363,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
     e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
     ms[i] = t;
   }
-  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   if (e != cudaSuccess) return cuda_fail(e, "apply_profile");
   *nlaunch = n;
   return SU2G_OK;

@@ -50,6 +50,7 @@ constexpr int kChunkStages = 4;     // exact FP32 group sums over 4 stages = 128
 constexpr int kExpZero = -(1 << 20);  // exponent of an all-zero row
 constexpr int kFixedTop = 48;         // fixed point: group g weighs 2^(kFixedTop - 7g)
 constexpr int kMaxSegs = 1024;        // segments feeding one output tile
+constexpr int kTargetCtas = 4 * 152;  // phase-2 tiles are split until about this many CTAs run
 
 SU2G_HD constexpr int pairs(int S) { return S * (S + 1) / 2; }
 SU2G_HD constexpr int a_unit_bytes(int S) { return S * kTM * kKS * 2; }
@@ -76,6 +77,16 @@ struct OzSeg {
   int64_t b_exp;     // exponent index of the tile's first B row
   int nks;           // k tiles (stages) of this segment
   int pad;
+};
+
+// Sum of the partial tiles of one split output tile into its destination.
+struct RedTile {
+  int64_t c;         // element offset of the destination block origin
+  int c_buf;
+  int ldc;
+  int m0, n0, mlen, nlen;
+  int nparts;
+  int64_t part;      // scratch offset of the first partial (kTM x kTN doubles each, ldc = kTM)
 };
 
 struct OzTile {

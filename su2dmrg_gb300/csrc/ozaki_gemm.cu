@@ -90,12 +90,10 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -128,6 +126,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __shared__ uint32_t tmem_base_sh;
   __shared__ int fmax_sh[kTN];
   __shared__ int cshift_sh[kMaxSegs];
+  __shared__ int shb_sh[4][kTN];  // per epilogue warp: column shifts of the current segment
   __shared__ int abort_sh;
 
   const OzTile t = tiles[blockIdx.x];
@@ -279,33 +278,38 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       const int ea = exps[g.a_exp + row];
       const int cs = cshift_sh[s];
       const int sha = (ea == kExpZero) ? 1000 : emax - (ea - cs);
-      const int* __restrict__ fb = exps + g.b_exp;
+      // column shifts of this segment, staged per warp (no block barrier)
+      __syncwarp();
+#pragma unroll
+      for (int h = 0; h < kTN / 32; ++h) {
+        const int j = lane + 32 * h;
+        const int fj = exps[g.b_exp + j];
+        shb_sh[warp][j] = (fj == kExpZero) ? 1000 : fmax_sh[j] - (fj + cs);
+      }
+      __syncwarp();
       const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
       for (int c = 0; c < nchunks; ++c, ++chunk) {
         if (!mbar_wait(smem_u32(&bar_accf), chunk & 1)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
-        for (int cb = 0; cb < kTN / 16; ++cb) {
-          long long v[16];
+        for (int cb = 0; cb < kTN / 8; ++cb) {
+          // all S group sums of 8 columns in flight, one wait
+          uint32_t r[S][8];
 #pragma unroll
-          for (int x = 0; x < 16; ++x) v[x] = 0;
+          for (int gg = 0; gg < S; ++gg) tmem_ld8(tmem + lane_base + (uint32_t)(gg * kTN + cb * 8), r[gg]);
+          tmem_wait_ld();
 #pragma unroll
-          for (int gg = 2; gg <= S + 1; ++gg) {
-            uint32_t r[16];
-            tmem_ld16(tmem + lane_base + (uint32_t)((gg - 2) * kTN + cb * 16), r);
-            tmem_wait_ld();
+          for (int x = 0; x < 8; ++x) {
+            long long v = 0;
 #pragma unroll
-            for (int x = 0; x < 16; ++x) v[x] += shl_signed((long long)f32_to_int_exact(r[x]), kFixedTop - kBits * gg);
-          }
-#pragma unroll
-          for (int x = 0; x < 16; ++x) {
-            const int j = cb * 16 + x;
-            const int fj = fb[j];
-            const int sh = (fj == kExpZero) ? 1000 : sha + fmax_sh[j] - (fj + cs);
+            for (int gg = 0; gg < S; ++gg)
+              v += shl_signed((long long)f32_to_int_exact(r[gg][x]), kFixedTop - kBits * (gg + 2));
+            const int j = cb * 8 + x;
+            const int sh = sha + shb_sh[warp][j];
             if (sh == 0) {
-              acc[j] += v[x];
+              acc[j] += v;
             } else if (sh < 63) {
-              acc[j] += (v[x] + (1ll << (sh - 1))) >> sh;  // round to nearest
+              acc[j] += (v + (1ll << (sh - 1))) >> sh;  // round to nearest
             }
           }
         }

@@ -94,7 +94,27 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
   }
 }
 
+// partial tiles of a split output tile, summed in part order (deterministic)
+__global__ void __launch_bounds__(256) reduce_partials(const RedTile* __restrict__ reds, Bases bases) {
+  const RedTile r = reds[blockIdx.x];
+  const double* P = resolve(bases, kBufScratch, r.part);
+  double* C = resolve(bases, r.c_buf, r.c);
+  for (int idx = threadIdx.x; idx < kTM * kTN; idx += blockDim.x) {
+    const int i = idx % kTM, j = idx / kTM;
+    if (i >= r.mlen || j >= r.nlen) continue;
+    double s = 0.0;
+    for (int p = 0; p < r.nparts; ++p) s += P[(int64_t)p * kTM * kTN + idx];
+    C[(int64_t)(r.m0 + i) + (int64_t)(r.n0 + j) * r.ldc] = s;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  reduce_partials<<<n, 256, 0, stream>>>(reds, bases);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, const Bases& bases,
                         uint8_t* packed, int* exps, cudaStream_t stream) {

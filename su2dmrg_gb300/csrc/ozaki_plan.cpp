@@ -117,8 +117,58 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
         otile->push_back(t);
       }
   }
-  std::stable_sort(otile->begin(), otile->end(), [](const OzTile& x, const OzTile& y) { return x.work > y.work; });
   return SU2G_OK;
+}
+
+// Phase-2 tiles feed on many segments, but there may be fewer tiles than SMs:
+// split the segment run of each tile into parts of about equal work, each part
+// a CTA writing a partial tile into scratch, summed afterwards in part order.
+void split_phase2(OzWork& w) {
+  const int ntiles = (int)w.tile2.size();
+  if (ntiles == 0 || ntiles >= kTargetCtas) return;
+  const int want = (kTargetCtas + ntiles - 1) / ntiles;
+  std::vector<OzTile> out;
+  for (const OzTile& t : w.tile2) {
+    const int parts = std::min(want, t.nseg);
+    if (parts <= 1) {
+      out.push_back(t);
+      continue;
+    }
+    RedTile r;
+    r.c = t.c;
+    r.c_buf = t.c_buf;
+    r.ldc = t.ldc;
+    r.m0 = t.m0;
+    r.n0 = t.n0;
+    r.mlen = t.mlen;
+    r.nlen = t.nlen;
+    r.part = w.scratch_base + w.partial_len;
+    r.nparts = 0;
+    // cut the run where the cumulative work crosses multiples of work/parts
+    int64_t done = 0;
+    int s0 = t.seg0;
+    for (int s = t.seg0; s < t.seg0 + t.nseg; ++s) {
+      done += w.seg2[s].nks;
+      const bool cut = done * parts >= (int64_t)(r.nparts + 1) * t.work || s == t.seg0 + t.nseg - 1;
+      if (!cut) continue;
+      OzTile p = t;
+      p.c = w.scratch_base + w.partial_len;
+      p.c_buf = kBufScratch;
+      p.ldc = kTM;
+      p.m0 = 0;
+      p.n0 = 0;
+      p.seg0 = s0;
+      p.nseg = s + 1 - s0;
+      p.work = 0;
+      for (int q = s0; q <= s; ++q) p.work += w.seg2[q].nks;
+      out.push_back(p);
+      w.partial_len += (int64_t)kTM * kTN;
+      ++r.nparts;
+      s0 = s + 1;
+    }
+    w.red2.push_back(r);
+  }
+  w.tile2.swap(out);
 }
 
 }  // namespace
@@ -127,6 +177,7 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   OzWork& w = *out;
   w = OzWork();
   w.S = S;
+  w.scratch_base = hw.scratch_len;
   Builder B;
   B.S = S;
   B.w = &w;
@@ -137,6 +188,10 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   if (rc) return rc;
   rc = build_phase(B, hw.seg2, hw.blk2, &w.seg2, &w.tile2, err);
   if (rc) return rc;
+  split_phase2(w);
+  auto heavier = [](const OzTile& x, const OzTile& y) { return x.work > y.work; };
+  std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
+  std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
   for (int c = 0; c < 3; ++c) {
     w.units[c].clear();
     for (int j = 0; j < (int)w.jobs[c].size(); ++j)
@@ -175,6 +230,18 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
     *err = "split mode: tile segment out of bounds";
     return SU2G_EINVAL;
   }
+  const int64_t scratch_end = w.scratch_base + w.partial_len;
+  for (const OzTile& t : w.tile2)
+    if (t.c_buf == kBufScratch && (t.c < w.scratch_base || t.c + (int64_t)kTM * kTN > scratch_end)) {
+      *err = "split mode: partial tile out of bounds";
+      return SU2G_EINVAL;
+    }
+  for (const RedTile& r : w.red2)
+    if (r.nparts < 2 || r.part < w.scratch_base || r.part + (int64_t)r.nparts * kTM * kTN > scratch_end ||
+        r.mlen <= 0 || r.mlen > kTM || r.nlen <= 0 || r.nlen > kTN || r.ldc < r.m0 + r.mlen) {
+      *err = "split mode: partial sum out of bounds";
+      return SU2G_EINVAL;
+    }
   return SU2G_OK;
 }
 

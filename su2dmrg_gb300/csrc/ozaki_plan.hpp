@@ -22,8 +22,11 @@ struct OzWork {
   std::vector<Unit> units[3];
   std::vector<OzSeg> seg1, seg2;
   std::vector<OzTile> tile1, tile2;
-  int64_t packed_bytes = 0;  // bytes of all packed operands
-  int64_t exp_len = 0;       // int32 row exponents of all packed operands
+  std::vector<RedTile> red2;  // phase-2 tiles split across CTAs: fixed-order sums
+  int64_t packed_bytes = 0;   // bytes of all packed operands
+  int64_t exp_len = 0;        // int32 row exponents of all packed operands
+  int64_t scratch_base = 0;   // doubles of the plan scratch before the partial tiles
+  int64_t partial_len = 0;    // doubles of partial tiles after scratch_base
 };
 
 // The operand that is not an operator (psi or an intermediate) carries no
