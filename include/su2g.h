@@ -82,6 +82,9 @@ int su2g_bond_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, 
 int su2g_make_cgc(int j1, int j2, int j3, double* out);
 /* fac_hamilt_vec[i][j][k] of dmrg_su2.cpp:759-766 at out[(i*m+j)*m+k]. */
 int su2g_fac_hamilt_vec(int max_angm, double* out);
+/* fac_operator_transformation_left (side 0) / _rght (side 1)[j][m][l][i][k][p]
+ * of dmrg_su2.cpp:857-890 (0 where the reference leaves the entry unset). */
+int su2g_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p, double* out);
 
 /* -------------------------------------------------------------- H_eff -- */
 /* Builds the device work list of one effective Hamiltonian
@@ -149,6 +152,31 @@ int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_f
 #define SU2G_NOALLOC_MAX_SEGS 65536
 int su2g_hamiltonian_vector_multiplication_noalloc(const int* vec_desc, const int* vec_flag, const double* vec,
                                                    su2g_tensor op1, su2g_tensor op2, double* y, void* stream);
+
+/* -------------------------------------------------- environment updates -- */
+/* tensor_su2::operator_transformation(uu, vv, op, flag)
+ * (tensor_su2_dmrg_src.cpp:221-402): carries each operator op_t of the last
+ * environment (3 legs: bond, operator spin, bond) through the MPS tensors uu
+ * and vv (3 legs; leg `flag` attaches to the operator, the other of legs 0/1
+ * is the spin-1/2 physical leg, leg 2 the new bond) into a new operator on
+ * the new bond, with the fac_operator_transformation_{left,rght} factors.
+ * Called for a batch: op[t] -> out[t] (device), all sharing uu and vv, in one
+ * device pass.  Each out[t] must have the layout reported by
+ * su2g_operator_transformation_layout for op[t]: structure (uu leg 2, op
+ * leg 1, vv leg 2 inverted) with exactly the blocks some product reaches, as
+ * the reference creates them.  mode: SU2G_MODE_* as for H_eff.  Blocks until
+ * done. */
+int su2g_operator_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor op, int* out_desc,
+                                        int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len);
+int su2g_operator_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* ops,
+                                 double* const* outs, int mode, void* stream);
+/* tensor_su2::overlap_transformation(uu, vv, hh, flag)
+ * (tensor_su2_dmrg_src.cpp:531-688): the same for 2-leg scalar operators (the
+ * block Hamiltonian), output structure (uu leg 2, vv leg 2 inverted). */
+int su2g_overlap_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor hh, int* out_desc,
+                                       int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len);
+int su2g_overlap_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* hhs,
+                                double* const* outs, int mode, void* stream);
 
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme

@@ -382,3 +382,35 @@ def to_layout(src: Struct, x: np.ndarray, dst: Struct) -> np.ndarray:
             n = int(np.prod(dst.block_shape(i)))
             out[do[i]: do[i] + n] = x[so[i]: so[i] + n]
     return out
+
+
+# --------------------------------------------------------------------------
+# Environment updates (tensor_su2_dmrg_src.cpp:221-402, 531-688)
+# --------------------------------------------------------------------------
+def fac_operator_transformation(side, j, m, l, i, k, p):
+    f = lib().or_fac_operator_transformation
+    f.restype = ctypes.c_double
+    return f(side, j, m, l, i, k, p)
+
+
+def env_out_struct(kind: int, su: Struct, so: Struct, sv: Struct) -> Struct:
+    """Output structure of the transformations: (uu leg 2[, op leg 1], vv leg 2 inverted)."""
+    legs = [su.bonds[2]] + ([so.bonds[1]] if kind else []) + [sv.bonds[2].inverted()]
+    return Struct(legs, 0)
+
+
+def env_transform(kind: int, su: Struct, xu, sv: Struct, xv, so: Struct, xo, flag: int):
+    """Returns (out Struct with the reference's presence flags, packed data)."""
+    out = env_out_struct(kind, su, so, sv)
+    fout = np.zeros(out.nten, np.int32)
+    args = (kind, _p(su.desc()), _p(su.flag.astype(np.int32)), _p(np.ascontiguousarray(xu)),
+            _p(sv.desc()), _p(sv.flag.astype(np.int32)), _p(np.ascontiguousarray(xv)),
+            _p(so.desc()), _p(so.flag.astype(np.int32)), _p(np.ascontiguousarray(xo)), flag, _p(out.desc()), _p(fout))
+    if lib().or_env_transform(*args, None) != 0:
+        raise RuntimeError("or_env_transform failed (layout)")
+    out.flag = fout
+    _, total = out.offsets()
+    y = np.zeros(total)
+    if lib().or_env_transform(*args, _p(y)) != 0:
+        raise RuntimeError("or_env_transform failed")
+    return out, y

@@ -136,6 +136,34 @@ void ref_result_sizes(int* nten, int* nele1, int* nele2) {
 
 void ref_result_get(int* flag, double* tele1, double* tele2) { g_result.get_telement(tele1, tele2, flag); }
 
+// result = operator_transformation(uu, vv, op, flag)  (tensor_su2_dmrg_src.cpp:221-402)
+int ref_operator_transformation(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                                const double* xv, const int* dop, const int* fop, const double* xop, int flag) {
+  tensor_su2 uu, vv, op;
+  build_tensor(uu, du, fu, xu);
+  build_tensor(vv, dv, fv, xv);
+  build_tensor(op, dop, fop, xop);
+  g_result.operator_transformation(uu, vv, op, flag);
+  return g_result.get_nten();
+}
+
+// result = overlap_transformation(uu, vv, op, flag)  (tensor_su2_dmrg_src.cpp:531-688)
+int ref_overlap_transformation(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                               const double* xv, const int* dop, const int* fop, const double* xop, int flag) {
+  tensor_su2 uu, vv, op;
+  build_tensor(uu, du, fu, xu);
+  build_tensor(vv, dv, fv, xv);
+  build_tensor(op, dop, fop, xop);
+  g_result.overlap_transformation(uu, vv, op, flag);
+  return g_result.get_nten();
+}
+
+// fac_operator_transformation_{left,rght}[j][m][l][i][k][p] (dmrg_su2.cpp:857-890)
+double ref_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p) {
+  return side == 0 ? fac_operator_transformation_left[j][m][l][i][k][p]
+                   : fac_operator_transformation_rght[j][m][l][i][k][p];
+}
+
 // su2bond::fuse (su2bond.cpp:155-210); returns the sector count
 int ref_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, const int* d2, int* aout, int* dout) {
   std::vector<int> x1(a1, a1 + n1), y1(d1, d1 + n1), x2(a2, a2 + n2), y2(d2, d2 + n2);

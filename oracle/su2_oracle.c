@@ -423,3 +423,162 @@ int or_heff_spin0(int side, const int* hd, const int* hf, const double* hx, cons
   tensor_close(&out);
   return rc;
 }
+
+/* ----------------------------------------------------------------------- */
+/* Environment updates                                                     */
+/* ----------------------------------------------------------------------- */
+
+/* tensor::is_proportional_to (tensor.cpp:1231-1269) */
+static int or_proportional(const double* t, const double* ref, int n, double* ratio) {
+  const double tol = 1.e-12;
+  int zero = 1;
+  for (int e = 0; e < n; ++e)
+    if (fabs(t[e]) > tol) zero = 0;
+  if (zero) { *ratio = 0; return 1; }
+  int pos = 0;
+  double mx = 0;
+  for (int e = 0; e < n; ++e)
+    if (fabs(ref[e]) > mx) { pos = e; mx = fabs(ref[e]); }
+  if (mx <= tol) return 0;
+  double rat = t[pos] / ref[pos];
+  for (int e = 0; e < n; ++e) {
+    int a = fabs(t[e]) <= tol, b = fabs(ref[e]) <= tol;
+    if (a && b) continue;
+    if (a != b) return 0;
+    if (fabs(t[e] / ref[e] - rat) > tol) return 0;
+  }
+  *ratio = rat;
+  return 1;
+}
+
+/* fac_operator_transformation_{left,rght}[j][m][l][i][k][p] (dmrg_su2.cpp:857-890):
+ * contract_dmrg_operator_transformation (tensor_dmrg_src.cpp:104-166) of
+ * three CG tensors compared with make_cgc(j,m,l). */
+double or_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p) {
+  if (p < 0 || p > 2 || m < 0 || m > 6 || m % 2) return 0;
+  if (!(j >= abs(i - p) && j <= i + p && l >= abs(k - p) && l <= k + p)) return 0;
+  if (!(k >= abs(i - m) && k <= i + m && k % 2 == i % 2 && l >= abs(j - m) && l <= j + m && j % 2 == l % 2)) return 0;
+  int ni = i + 1, nj = j + 1, nk = k + 1, nl = l + 1, nm = m + 1, np = p + 1;
+  double* c1 = (double*)malloc(sizeof(double) * ni * np * nj);
+  double* c2 = (double*)malloc(sizeof(double) * nk * np * nl);
+  double* c3 = (double*)malloc(sizeof(double) * ni * nm * nk);
+  double* ref = (double*)malloc(sizeof(double) * nj * nm * nl);
+  double* t = (double*)calloc(nj * nm * nl, sizeof(double));
+  if (side == 0) { or_make_cgc(i, p, j, c1); or_make_cgc(k, p, l, c2); }
+  else { or_make_cgc(p, i, j, c1); or_make_cgc(p, k, l, c2); }
+  or_make_cgc(i, m, k, c3);
+  or_make_cgc(j, m, l, ref);
+  for (int a = 0; a < ni; ++a)
+    for (int b = 0; b < nk; ++b)
+      for (int mm = 0; mm < nm; ++mm) {
+        double x3 = c3[a + ni * (mm + nm * b)];
+        if (x3 == 0) continue;
+        for (int pp = 0; pp < np; ++pp)
+          for (int jj = 0; jj < nj; ++jj) {
+            double x1 = side == 0 ? c1[a + ni * (pp + np * jj)] : c1[pp + np * (a + ni * jj)];
+            if (x1 == 0) continue;
+            for (int ll = 0; ll < nl; ++ll) {
+              double x2 = side == 0 ? c2[b + nk * (pp + np * ll)] : c2[pp + np * (b + nk * ll)];
+              t[jj + nj * (mm + nm * ll)] += x1 * x3 * x2;
+            }
+          }
+      }
+  double rat = 0;
+  if (!or_proportional(t, ref, nj * nm * nl, &rat)) rat = 0;
+  free(c1); free(c2); free(c3); free(ref); free(t);
+  return rat;
+}
+
+/* tensor_su2::operator_transformation (kind 1, tensor_su2_dmrg_src.cpp:221-402)
+ * and tensor_su2::overlap_transformation (kind 0, :531-688):
+ *   out(c[, s], c') += fac * sum_p sum_{a,a'} uu(a,p,c) op(a[, s], a') vv(a',p,c')
+ * for uu/vv blocks that share the physical sector p and are attached to the
+ * op through leg `flag` (the other of legs 0/1 is physical), fac from the
+ * transformation table (kind 1, entries below 1e-8 skipped) or 1 (kind 0).
+ * The output structure is (uu leg 2[, op leg 1], vv leg 2 inverted); with
+ * yout == NULL only the presence flags fout are computed (a block exists where
+ * at least one product lands, as in the reference); otherwise yout receives
+ * the blocks in the layout of fout. */
+int or_env_transform(int kind, const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                     const double* xv, const int* dop, const int* fop, const double* xop, int flag, const int* dout,
+                     int* fout, double* yout) {
+  or_tensor u, v, o;
+  or_struct so;
+  if (tensor_open(&u, du, fu, xu) || tensor_open(&v, dv, fv, xv) || tensor_open(&o, dop, fop, xop)) return -1;
+  if (parse_desc(dout, &so)) return -1;
+  int64_t* yoff = (int64_t*)malloc(sizeof(int64_t) * so.nten);
+  if (yout) or_offsets(dout, fout, yoff);
+  else for (int i = 0; i < so.nten; ++i) fout[i] = 0;
+  const int pl = 1 - flag; /* physical leg of uu/vv */
+  int rc = 0;
+  for (int j = 0; j < o.s.nten && !rc; ++j) {
+    if (!o.flag[j]) continue;
+    int so_[OR_MAXLEG], ao[3];
+    block_sectors(&o.s, j, so_);
+    for (int q = 0; q < o.s.nbond; ++q) ao[q] = o.s.angm[q][so_[q]];
+    const int A = o.s.dim[0][so_[0]];
+    const int ms = kind ? o.s.dim[1][so_[1]] : 1;
+    const int Ap = o.s.dim[kind ? 2 : 1][so_[kind ? 2 : 1]];
+    const int a = ao[0], ap = ao[kind ? 2 : 1], s = kind ? ao[1] : 0;
+    for (int k = 0; k < u.s.nten && !rc; ++k) {
+      if (!u.flag[k]) continue;
+      int su[OR_MAXLEG];
+      block_sectors(&u.s, k, su);
+      if (u.s.angm[flag][su[flag]] != a) continue;
+      const int sig = u.s.angm[pl][su[pl]], c = u.s.angm[2][su[2]];
+      const int P = u.s.dim[pl][su[pl]], C = u.s.dim[2][su[2]];
+      for (int l = 0; l < v.s.nten && !rc; ++l) {
+        if (!v.flag[l]) continue;
+        int sv[OR_MAXLEG];
+        block_sectors(&v.s, l, sv);
+        if (v.s.angm[flag][sv[flag]] != ap || v.s.angm[pl][sv[pl]] != sig) continue;
+        const int cp = v.s.angm[2][sv[2]], Cp = v.s.dim[2][sv[2]];
+        int oang[3], osec[3];
+        if (kind) { oang[0] = c; oang[1] = s; oang[2] = cp; }
+        else { oang[0] = c; oang[1] = cp; }
+        if (!legal_angm(oang, kind ? 3 : 2, 0)) continue;
+        int missing = 0;
+        for (int q = 0; q < (kind ? 3 : 2); ++q) {
+          osec[q] = sector_of(&so, q, oang[q]);
+          if (osec[q] < 0) missing = 1;
+        }
+        if (missing) continue;
+        double fac = 1.0;
+        if (kind) {
+          fac = flag == 0 ? or_fac_operator_transformation(0, c, s, cp, a, ap, sig)
+                          : or_fac_operator_transformation(1, c, s, cp, a, ap, sig);
+          if (fabs(fac) < 1.e-8) continue;
+        }
+        const int m = block_index(&so, osec);
+        if (!yout) { fout[m] = 1; continue; }
+        if (!fout[m]) { rc = -4; break; }
+        const double* U = u.data + u.off[k];
+        const double* V = v.data + v.off[l];
+        const double* O = o.data + o.off[j];
+        double* Y = yout + yoff[m];
+        for (int p = 0; p < P; ++p)
+          for (int sg = 0; sg < ms; ++sg)
+            for (int cc = 0; cc < C; ++cc)
+              for (int ccp = 0; ccp < Cp; ++ccp) {
+                double acc = 0;
+                for (int aa = 0; aa < A; ++aa) {
+                  double uv = flag == 0 ? U[aa + A * (p + P * cc)] : U[p + P * (aa + A * cc)];
+                  if (uv == 0) continue;
+                  double inner = 0;
+                  for (int aap = 0; aap < Ap; ++aap) {
+                    double vv_ = flag == 0 ? V[aap + Ap * (p + P * ccp)] : V[p + P * (aap + Ap * ccp)];
+                    inner += O[aa + A * (sg + ms * aap)] * vv_;
+                  }
+                  acc += uv * inner;
+                }
+                Y[cc + C * (sg + ms * ccp)] += fac * acc;
+              }
+      }
+    }
+  }
+  free(yoff);
+  tensor_close(&u);
+  tensor_close(&v);
+  tensor_close(&o);
+  return rc;
+}

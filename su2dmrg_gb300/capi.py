@@ -56,6 +56,7 @@ _PROTOS = {
     "su2g_bond_fuse": (_i, [_i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
     "su2g_make_cgc": (_i, [_i, _i, _i, _vp]),
     "su2g_fac_hamilt_vec": (_i, [_i, _vp]),
+    "su2g_fac_operator_transformation": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "su2g_heff_plan_create": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp]),
     "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp, _vp]),
     "su2g_heff_plan_status": (_i, [_vp, _vp]),
@@ -66,6 +67,10 @@ _PROTOS = {
     "su2g_hamiltonian_vector_multiplication": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_hamiltonian_vector_multiplication_noalloc": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_lanczos": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "su2g_operator_transformation_layout": (_i, [Tensor, Tensor, _i, Tensor, _vp, _i, _vp, _i, _vp]),
+    "su2g_operator_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
+    "su2g_overlap_transformation_layout": (_i, [Tensor, Tensor, _i, Tensor, _vp, _i, _vp, _i, _vp]),
+    "su2g_overlap_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),
     "su2g_vec_scale": (_i, [_d, _vp, _i64, _vp]),

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "env_plan.hpp"
 #include "heff_plan.hpp"
 #include "kernels.hpp"
 #include "ozaki_plan.hpp"
@@ -209,34 +210,38 @@ int su2g_fac_hamilt_vec(int max_angm, double* out) {
   return SU2G_OK;
 }
 
-int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
-                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
-                          su2g_heff_plan** plan) {
-  if (!plan) return fail(SU2G_EINVAL, "plan_create: null output");
+int su2g_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p, double* out) {
+  if (!out || side < 0 || side > 1 || j < 0 || m < 0 || l < 0 || i < 0 || k < 0 || p < 0)
+    return fail(SU2G_EINVAL, "fac_operator_transformation: bad arguments");
+  *out = su2g::fac_operator_transformation(side, j, m, l, i, k, p);
+  return SU2G_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// device side of a plan whose host work lists are built: work lists, scratch
+// (intermediates + split partial tiles) and, in split mode, the packed operands
+int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
   *plan = nullptr;
   const int S = slices_of_mode(mode);
   if (S < 0) return fail(SU2G_EINVAL, "plan_create: unknown mode");
   su2g_heff_plan* p = new su2g_heff_plan();
   p->mode = mode;
   p->S = S;
+  p->work = std::move(work);
   std::string err;
-  int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &p->work, &err);
-  if (rc) {
-    delete p;
-    return fail(rc, err);
+  if (S > 0) {
+    const int rc = su2g::oz::build_ozaki_work(p->work, S, &p->oz, &err);
+    if (rc) {
+      delete p;
+      return fail(rc, err);
+    }
   }
   cudaError_t e = upload(p->work.seg1, &p->d_seg1);
   if (e == cudaSuccess) e = upload(p->work.seg2, &p->d_seg2);
   if (e == cudaSuccess) e = upload(p->work.tile1, &p->d_tile1);
   if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
-  if (e == cudaSuccess && S > 0) {
-    rc = su2g::oz::build_ozaki_work(p->work, S, &p->oz, &err);
-    if (rc) {
-      p->release();
-      delete p;
-      return fail(rc, err);
-    }
-  }
   const int64_t scratch_doubles = p->work.scratch_len + p->oz.partial_len;
   if (e == cudaSuccess && scratch_doubles > 0)
     e = cudaMalloc((void**)&p->d_scratch, scratch_doubles * sizeof(double));
@@ -248,6 +253,86 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
   }
   *plan = p;
   return SU2G_OK;
+}
+
+// one-shot environment update: build, run, wait, check, free
+int env_run(int kind, su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* ops, double* const* outs,
+            int mode, void* stream) {
+  if (!outs && nops > 0) return fail(SU2G_EINVAL, "env: missing output pointers");
+  su2g::HeffWork w;
+  std::vector<su2g::Struct> ys;
+  std::string err;
+  int rc = su2g::build_env_work(kind, uu, vv, flag, nops, ops, outs, &w, &ys, &err);
+  if (rc) return fail(rc, err);
+  su2g_heff_plan* p = nullptr;
+  rc = plan_from_work(std::move(w), mode, &p);
+  if (rc) return rc;
+  rc = su2g_heff_apply(p, nullptr, nullptr, stream);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  int code = 0;
+  if (!rc && e == cudaSuccess) rc = su2g_heff_plan_status(p, &code);
+  su2g_heff_plan_destroy(p);
+  if (e != cudaSuccess) return cuda_fail(e, "env transform");
+  return rc;
+}
+
+int env_layout(int kind, su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor op, int* out_desc, int out_desc_cap,
+               int* out_flag, int out_flag_cap, int64_t* out_len) {
+  su2g::HeffWork w;
+  std::vector<su2g::Struct> ys;
+  std::string err;
+  int rc = su2g::build_env_work(kind, uu, vv, flag, 1, &op, nullptr, &w, &ys, &err);
+  if (rc) return fail(rc, err);
+  const su2g::Struct& y = ys[0];
+  std::vector<int> d = {y.nbond, y.locspin};
+  for (int l = 0; l < y.nbond; ++l) {
+    d.push_back(y.legs[l].dir);
+    d.push_back(y.legs[l].n());
+    for (int a : y.legs[l].angm) d.push_back(a);
+    for (int x : y.legs[l].dim) d.push_back(x);
+  }
+  if (!out_desc || !out_flag || (int)d.size() > out_desc_cap || y.nten > out_flag_cap)
+    return fail(SU2G_EINVAL, "env layout: output arrays too small");
+  std::copy(d.begin(), d.end(), out_desc);
+  std::copy(y.flag.begin(), y.flag.end(), out_flag);
+  if (out_len) *out_len = y.total;
+  return SU2G_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                          su2g_heff_plan** plan) {
+  if (!plan) return fail(SU2G_EINVAL, "plan_create: null output");
+  *plan = nullptr;
+  if (slices_of_mode(mode) < 0) return fail(SU2G_EINVAL, "plan_create: unknown mode");
+  su2g::HeffWork w;
+  std::string err;
+  const int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err);
+  if (rc) return fail(rc, err);
+  return plan_from_work(std::move(w), mode, plan);
+}
+
+int su2g_operator_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor op, int* out_desc,
+                                        int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len) {
+  return env_layout(1, uu, vv, flag, op, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len);
+}
+
+int su2g_operator_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* ops,
+                                 double* const* outs, int mode, void* stream) {
+  return env_run(1, uu, vv, flag, nops, ops, outs, mode, stream);
+}
+
+int su2g_overlap_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor hh, int* out_desc,
+                                       int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len) {
+  return env_layout(0, uu, vv, flag, hh, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len);
+}
+
+int su2g_overlap_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* hhs,
+                                double* const* outs, int mode, void* stream) {
+  return env_run(0, uu, vv, flag, nops, hhs, outs, mode, stream);
 }
 
 int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,

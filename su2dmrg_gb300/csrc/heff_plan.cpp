@@ -338,7 +338,8 @@ int validate_heff_work(const HeffWork& w, std::string* err) {
   if (rc) return rc;
   // the output tiles cover y exactly (each element written once)
   int64_t written = 0;
-  for (const GemmTile& t : w.tile2) written += (int64_t)t.mlen * t.nlen;
+  for (const GemmTile& t : w.tile2)
+    if (t.c_buf == kBufY) written += (int64_t)t.mlen * t.nlen;
   if (written != w.psi.total) {
     *err = "phase 2 tiles do not cover y exactly";
     return SU2G_EINVAL;

@@ -6,7 +6,9 @@
 
 #include <cmath>
 #include <cstdlib>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 namespace su2g {
 
@@ -200,6 +202,100 @@ const std::vector<double>& fac_hamilt_vec_table() {
     fac_hamilt_vec(kMaxAngm, table.data());
   });
   return table;
+}
+
+namespace {
+
+// the conditions under which dmrg_su2.cpp:867-876 fills an entry
+bool optrans_defined(int j, int m, int l, int i, int k, int p) {
+  if (p < 0 || p > 2 || m < 0 || m > 6 || (m % 2) != 0) return false;
+  if (!(j >= std::abs(i - p) && j <= i + p)) return false;
+  if (!(l >= std::abs(k - p) && l <= k + p)) return false;
+  return k >= std::abs(i - m) && k <= i + m && (k % 2 == i % 2) && l >= std::abs(j - m) && l <= j + m &&
+         (j % 2 == l % 2);
+}
+
+// tensor::is_proportional_to (tensor.cpp:1231-1269): t = ratio * ref
+bool proportional(const std::vector<double>& t, const std::vector<double>& ref, double* ratio) {
+  const double tol = 1.e-12;
+  bool zero = true;
+  for (double v : t)
+    if (std::fabs(v) > tol) zero = false;
+  if (zero) {
+    *ratio = 0;
+    return true;
+  }
+  size_t pos = 0;
+  double mx = 0;
+  for (size_t e = 0; e < ref.size(); ++e)
+    if (std::fabs(ref[e]) > mx) {
+      pos = e;
+      mx = std::fabs(ref[e]);
+    }
+  if (mx <= tol) return false;
+  const double rat = t[pos] / ref[pos];
+  for (size_t e = 0; e < t.size(); ++e) {
+    const bool a = std::fabs(t[e]) <= tol, b = std::fabs(ref[e]) <= tol;
+    if (a && b) continue;
+    if (a != b) return false;
+    if (std::fabs(t[e] / ref[e] - rat) > tol) return false;
+  }
+  *ratio = rat;
+  return true;
+}
+
+double compute_optrans(int side, int j, int m, int l, int i, int k, int p) {
+  // side 0: T[jj,mm,ll] = sum C(i,p,j)[ii,pp,jj] C(i,m,k)[ii,mm,kk] C(k,p,l)[kk,pp,ll]
+  // side 1: T[jj,mm,ll] = sum C(p,i,j)[pp,ii,jj] C(i,m,k)[ii,mm,kk] C(p,k,l)[pp,kk,ll]
+  const int ni = i + 1, nj = j + 1, nk = k + 1, nl = l + 1, nm = m + 1, np = p + 1;
+  std::vector<double> c1(ni * np * nj), c2(nk * np * nl), c3(ni * nm * nk), ref(nj * nm * nl), t(nj * nm * nl, 0.0);
+  if (side == 0) {
+    make_cgc(i, p, j, c1.data());
+    make_cgc(k, p, l, c2.data());
+  } else {
+    make_cgc(p, i, j, c1.data());
+    make_cgc(p, k, l, c2.data());
+  }
+  make_cgc(i, m, k, c3.data());
+  make_cgc(j, m, l, ref.data());
+  for (int jj = 0; jj < nj; ++jj)
+    for (int mm = 0; mm < nm; ++mm)
+      for (int ll = 0; ll < nl; ++ll) {
+        double sum = 0;
+        for (int ii = 0; ii < ni; ++ii)
+          for (int kk = 0; kk < nk; ++kk) {
+            const double x3 = c3[ii + ni * (mm + nm * kk)];
+            if (x3 == 0) continue;
+            for (int pp = 0; pp < np; ++pp) {
+              const double x1 = side == 0 ? c1[ii + ni * (pp + np * jj)] : c1[pp + np * (ii + ni * jj)];
+              const double x2 = side == 0 ? c2[kk + nk * (pp + np * ll)] : c2[pp + np * (kk + nk * ll)];
+              sum += x1 * x3 * x2;
+            }
+          }
+        t[jj + nj * (mm + nm * ll)] = sum;
+      }
+  double ratio = 0;
+  if (!proportional(t, ref, &ratio)) return 0.0;
+  return ratio;
+}
+
+}  // namespace
+
+double fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p) {
+  if (!optrans_defined(j, m, l, i, k, p) || j >= kMaxAngm || l >= kMaxAngm || i >= kMaxAngm || k >= kMaxAngm)
+    return 0.0;
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int, int, int>, double> cache;
+  const auto key = std::make_tuple(side, j, m, l, i, k, p);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const double v = compute_optrans(side, j, m, l, i, k, p);
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = v;
+  return v;
 }
 
 }  // namespace su2g

@@ -78,4 +78,12 @@ void fac_hamilt_vec(int max_angm, double* out);
 // the table for kMaxAngm, computed once and cached
 const std::vector<double>& fac_hamilt_vec_table();
 
+// fac_operator_transformation_{left (side 0), rght (side 1)}[j][m][l][i][k][p]
+// of dmrg_su2.cpp:857-890: the ratio between the three-CG contraction of
+// tensor::contract_dmrg_operator_transformation and make_cgc(j, m, l), taken
+// at the largest entry of the latter (tensor::is_proportional_to,
+// tensor.cpp:1231-1269); 0 where the reference leaves the entry unset.
+// Entries are computed on first use and cached (thread safe).
+double fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p);
+
 }  // namespace su2g

@@ -247,3 +247,59 @@ def hamiltonian_vector_multiplication(vec: Su2Struct, vec_data, op1: Su2Struct, 
     vf = np.ascontiguousarray(vec.flag, np.int32)
     check(lib().su2g_hamiltonian_vector_multiplication(ptr(vd), ptr(vf), ptr(vec_data), t1, t2, ptr(y),
                                                        stream_handle(stream)))
+
+
+def _parse_desc(d):
+    d = [int(v) for v in d]
+    nb, loc, p = d[0], d[1], 2
+    bonds = []
+    for _ in range(nb):
+        dr, n = d[p], d[p + 1]
+        bonds.append(Su2Bond(dr, d[p + 2: p + 2 + n], d[p + 2 + n: p + 2 + 2 * n]))
+        p += 2 + 2 * n
+    return Su2Struct(bonds, loc)
+
+
+def _env_layout(kind: int, uu, xu, vv, xv, op, xo, flag: int) -> Su2Struct:
+    keep = []
+    fn = lib().su2g_operator_transformation_layout if kind else lib().su2g_overlap_transformation_layout
+    desc = np.zeros(4 + 3 * (2 + 2 * 64), np.int32)
+    flags = np.zeros(64 ** 3, np.int32)
+    n = ctypes.c_int64()
+    check(fn(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), _tensor(op, xo, keep), ptr(desc), len(desc),
+             ptr(flags), len(flags), ctypes.addressof(n)))
+    out = _parse_desc(desc)
+    out.flag = flags[: out.nten].copy()
+    return out
+
+
+def operator_transformation_layout(uu, xu, vv, xv, op, xo, flag: int) -> Su2Struct:
+    """Output structure of tensor_su2::operator_transformation (host only)."""
+    return _env_layout(1, uu, xu, vv, xv, op, xo, flag)
+
+
+def overlap_transformation_layout(uu, xu, vv, xv, hh, xh, flag: int) -> Su2Struct:
+    """Output structure of tensor_su2::overlap_transformation (host only)."""
+    return _env_layout(0, uu, xu, vv, xv, hh, xh, flag)
+
+
+def _env_run(kind, uu, xu, vv, xv, ops, outs, flag, mode, stream):
+    keep = []
+    arr = (capi.Tensor * max(1, len(ops)))()
+    for i, (s, x) in enumerate(ops):
+        arr[i] = _tensor(s, x, keep)
+    optr = (ctypes.c_void_p * max(1, len(outs)))(*[ptr(o) for o in outs])
+    fn = lib().su2g_operator_transformation if kind else lib().su2g_overlap_transformation
+    check(fn(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), len(ops), ctypes.addressof(arr),
+             ctypes.addressof(optr), int(mode), stream_handle(stream)))
+
+
+def operator_transformation(uu, xu, vv, xv, ops, outs, flag: int, mode: int = capi.MODE_F64, stream=None) -> None:
+    """Batch of tensor_su2::operator_transformation: ops = [(Su2Struct, device data)],
+    outs = device buffers laid out by operator_transformation_layout."""
+    _env_run(1, uu, xu, vv, xv, ops, outs, flag, mode, stream)
+
+
+def overlap_transformation(uu, xu, vv, xv, hhs, outs, flag: int, mode: int = capi.MODE_F64, stream=None) -> None:
+    """Batch of tensor_su2::overlap_transformation (2-leg scalar operators)."""
+    _env_run(0, uu, xu, vv, xv, hhs, outs, flag, mode, stream)

@@ -12,6 +12,9 @@ Fixtures:
   meta.npz             su2bond::fuse and su2struct block legality cases
   heff_term_*.npz      tensor_su2::hamiltonian_vector_multiplication cases
   spin0_*.npz          tensor_su2::contract cases of the spin-0 terms
+  env_op_*.npz         tensor_su2::operator_transformation cases (both flags)
+  env_ovl_*.npz        tensor_su2::overlap_transformation cases (both flags)
+  fac_optrans.npz      fac_operator_transformation_{left,rght} entries
   dmrg_energies.json   whole reference DMRG runs (E0 - 1000 per sweep)
 """
 from __future__ import annotations
@@ -143,6 +146,58 @@ def spin0_cases(L, rng):
     return cases
 
 
+def env_cases(L, rng):
+    """operator_transformation / overlap_transformation on random MPS tensors
+    with a spin-1/2 physical leg and random operators."""
+    cases = []
+    specs = [([0, 1, 2, 3, 4], [0, 1, 2, 3, 4, 5], 0.0), ([0, 2, 4], [1, 3, 5], 0.2), ([1, 3, 5, 7], [0, 2, 4, 6, 8], 0.1)]
+    for ci, (sa, sc, drop) in enumerate(specs):
+        da = [int(rng.integers(1, 7)) for _ in sa]
+        dc = [int(rng.integers(1, 7)) for _ in sc]
+        for flag in (0, 1):
+            phys = (-1, [1], [1])
+            bond_a = (-1, sa, da)
+            uub = [bond_a, phys, (1, sc, dc)] if flag == 0 else [phys, bond_a, (1, sc, dc)]
+            du = desc_of(uub)
+            fu = (legal_flags(L, du) * (rng.random(nten_of(uub)) >= drop)).astype(np.int32)
+            xu = random_data(uub, fu, rng)
+            xv = random_data(uub, fu, rng)
+            for kind, spin in (("op", (1, [2], [1])), ("op", (1, [0, 2], [1, 1])), ("ovl", None)):
+                if kind == "op":
+                    ob = [(1, sa, da), spin, (-1, sa, da)]
+                    fn = L.ref_operator_transformation
+                else:
+                    ob = [(1, sa, da), (-1, sa, da)]
+                    fn = L.ref_overlap_transformation
+                dop = desc_of(ob)
+                fop = (legal_flags(L, dop) * (rng.random(nten_of(ob)) >= drop)).astype(np.int32)
+                xop = random_data(ob, fop, rng)
+                fn(p(du), p(fu), p(xu), p(du), p(fu), p(xv), p(dop), p(fop), p(xop), flag)
+                rflag, rx, rcg = read_result(L)
+                nten = ctypes.c_int()
+                name = f"env_{kind}_{ci}_{flag}_{len(spin[1]) if spin else 0}"
+                cases.append(dict(name=name, flag=np.int32(flag), du=du, fu=fu, xu=xu, xv=xv, dop=dop, fop=fop, xop=xop,
+                                  rflag=rflag, rx=rx, rcg=rcg))
+    return cases
+
+
+def fac_optrans(L):
+    L.ref_fac_operator_transformation.restype = ctypes.c_double
+    idx, val = [], []
+    for side in (0, 1):
+        for j in range(11):
+            for m in (0, 2, 4, 6):
+                for l in range(11):
+                    for i in range(11):
+                        for k in range(11):
+                            for pp in (0, 1, 2):
+                                v = L.ref_fac_operator_transformation(side, j, m, l, i, k, pp)
+                                if v != 0.0:
+                                    idx.append((side, j, m, l, i, k, pp))
+                                    val.append(v)
+    return dict(idx=np.asarray(idx, np.int8), val=np.asarray(val))
+
+
 def meta_cases(L, rng):
     fa, fd, fo_a, fo_d, fn = [], [], [], [], []
     for _ in range(40):
@@ -220,7 +275,8 @@ def main():
     np.savez(os.path.join(HERE, "cgc.npz"), triples=np.asarray(trip, np.int32), values=np.concatenate(vals),
              idx=np.cumsum([0] + [len(v) for v in vals]))
     np.savez(os.path.join(HERE, "meta.npz"), **meta_cases(L, rng))
-    for c in heff_cases(L, rng) + spin0_cases(L, rng):
+    np.savez_compressed(os.path.join(HERE, "fac_optrans.npz"), **fac_optrans(L))
+    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:

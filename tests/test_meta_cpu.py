@@ -144,3 +144,19 @@ def test_split_work_lists_on_cpu(su2lib, mode):
     w = synthetic_heff(D=2000, nspin1=18, seed=1234)
     r = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr, mode=mode)
     assert r["scratch_bytes"] > 2e9  # packed operator slices + intermediates
+
+
+def test_env_layouts_match_reference(su2lib, oracle):
+    """Output structures of the transformations (which blocks exist), host only."""
+    import glob
+
+    from su2dmrg_gb300.su2 import operator_transformation_layout, overlap_transformation_layout
+
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "env_*.npz"))):
+        g = np.load(path)
+        su = oracle.struct_from_desc(g["du"], g["fu"])
+        so = oracle.struct_from_desc(g["dop"], g["fop"])
+        fn = overlap_transformation_layout if "env_ovl" in path else operator_transformation_layout
+        out = fn(su, g["xu"], su, g["xv"], so, g["xop"], int(g["flag"]))
+        assert out.flag.tolist() == g["rflag"].tolist(), path
+        assert out.size() == g["rx"].size

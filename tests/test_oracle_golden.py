@@ -134,3 +134,21 @@ def test_dmrg_energies_match_exact_diagonalisation():
             assert abs(r["energies_minus_1000"][-1] + 1000 - exact[key]) < 1e-8
             seen += 1
     assert seen == 3
+
+
+def test_fac_operator_transformation_matches_reference(oracle):
+    g = np.load(os.path.join(GOLDEN, "fac_optrans.npz"))
+    for r, v in zip(g["idx"], g["val"]):
+        got = oracle.fac_operator_transformation(*[int(x) for x in r])
+        assert abs(got - v) <= 1e-14 * abs(v), (r, got, v)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "env_*.npz"))))
+def test_env_transform_matches_reference(oracle, path):
+    g = np.load(path)
+    kind = 0 if "env_ovl" in path else 1
+    su = oracle.struct_from_desc(g["du"], g["fu"])
+    so = oracle.struct_from_desc(g["dop"], g["fop"])
+    out, y = oracle.env_transform(kind, su, g["xu"], su, g["xv"], so, g["xop"], int(g["flag"]))
+    assert out.flag.tolist() == g["rflag"].tolist()  # the same blocks exist
+    assert np.linalg.norm(y - g["rx"]) <= 1e-13 * np.linalg.norm(g["rx"])
