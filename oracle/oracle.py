@@ -414,3 +414,134 @@ def env_transform(kind: int, su: Struct, xu, sv: Struct, xv, so: Struct, xo, fla
     if lib().or_env_transform(*args, _p(y)) != 0:
         raise RuntimeError("or_env_transform failed")
     return out, y
+
+
+# --------------------------------------------------------------------------
+# Truncation (tensor_su2::svd, tensor_su2.cpp:1619-1758; tensor::svd,
+# tensor.cpp:1472-1700)
+# --------------------------------------------------------------------------
+def _eigh(a):
+    """dsyev, eigenvalues ascending (obtain_symmetric_matrix_eigenvector, tensor.cpp:731-759)."""
+    from scipy.linalg import eigh
+
+    w, v = eigh(a, driver="ev")
+    return w, v
+
+
+def _refine(G, w, v, n):
+    """Re-diagonalise the subspace of eigenvalues below 0.1 of the largest,
+    repeatedly (tensor.cpp:1491-1527)."""
+    tol1 = 1.0e-1
+    np_ = 0
+    for i in range(n - 1, -1, -1):
+        if w[i] / w[n - 1] < tol1:
+            np_ = i + 1
+            break
+    if np_ <= 1:
+        return w, v
+    ap = G.copy()
+    vp = v.copy()
+    npp = np_
+    np_ = n
+    w = w.copy()
+    v = v.copy()
+    while True:
+        vsub = vp[:np_, :npp]
+        vpp = vsub.T @ ap[:np_, :np_] @ vsub
+        ap = vpp.copy()
+        ww, vv = _eigh(vpp)
+        w[:npp] = ww
+        v[:, :npp] = v[:, :npp] @ vv
+        vp = vv
+        j = 0
+        for i in range(npp - 1, -1, -1):
+            if ww[i] / ww[npp - 1] < tol1:
+                j = i + 1
+                break
+        np_ = npp
+        npp = j
+        if npp <= 1:
+            break
+    return w, v
+
+
+def tensor_svd(blk, p1, p2, max_dcut):
+    """One sector: returns (u (m x dcut), v (n x dcut), s ascending (dcut))."""
+    m, n = blk.shape
+    tol = 1.0e-100
+    if m >= n:
+        G = blk.T @ blk
+        w, v = _eigh(G)
+        w, v = _refine(G, w, v, n)
+        u = blk @ v
+        k = n
+    else:
+        G = blk @ blk.T
+        w, u = _eigh(G)
+        w, u = _refine(G, w, u, m)
+        v = blk.T @ u
+        k = m
+    w = w.copy()
+    num = w[k - 1]
+    dcut = 0
+    if num > tol:
+        for i in range(k - 1, -1, -1):
+            if w[i] / num > tol:
+                w[i] = np.sqrt(w[i])
+                dcut += 1
+            else:
+                w[i] = 0
+    dcut = min(dcut, max_dcut, m if m >= n else n)
+    for i in range(k - 1, k - dcut - 1, -1):
+        if w[i] > 0:
+            if m >= n:
+                u[:, i] *= w[i] ** (p1 - 1.0)
+                v[:, i] *= w[i] ** p2
+            else:
+                v[:, i] *= w[i] ** (p2 - 1.0)
+                u[:, i] *= w[i] ** p1
+        else:
+            u[:, i] = 0
+            v[:, i] = 0
+    return u[:, k - dcut:], v[:, k - dcut:], w[k - dcut:k].copy()
+
+
+def svd_truncate(vs: Struct, x, p1, p2, max_dcut):
+    """Returns (kept per leg-0 sector, wout (kept, then discarded), [(u, v) per sector])."""
+    off, _ = vs.offsets()
+    n0, n1 = len(vs.bonds[0].angm), len(vs.bonds[1].angm)
+    res = {}
+    wsort, isort = [], []
+    for i in range(n0):
+        for j in range(n1):
+            if vs.bonds[0].angm[i] != vs.bonds[1].angm[j]:
+                continue
+            b = i + j * n0
+            if not vs.flag[b]:
+                continue
+            m, n = vs.bonds[0].dim[i], vs.bonds[1].dim[j]
+            blk = np.asarray(x[off[b]: off[b] + m * n]).reshape(m, n, order="F")
+            u, v, s = tensor_svd(blk, p1, p2, max_dcut)
+            res[i] = (u, v, s)
+            wsort += list(s)
+            isort += [i] * len(s)
+    n = len(wsort)
+    ws = np.asarray(wsort, np.float64)
+    iss = np.asarray(isort, np.int32)
+    lib().dsort2_(ctypes.byref(ctypes.c_int(n)), _p(ws), _p(iss))
+    dims = np.zeros(n0, np.int32)
+    for i in range(n - 1, max(0, n - max_dcut) - 1, -1):
+        dims[iss[i]] += 1
+    kept_w, disc_w, uv = [], [], {}
+    for i in range(n0):
+        if i not in res:
+            continue
+        u, v, s = res[i]
+        dc, d = len(s), dims[i]
+        if d > 0:
+            kept_w += list(s[dc - d:])
+            disc_w += list(s[:dc - d])
+            uv[i] = (u[:, dc - d:], v[:, dc - d:])
+        else:
+            disc_w += list(s)
+    return dims, np.asarray(kept_w + disc_w), uv

@@ -164,6 +164,24 @@ double ref_fac_operator_transformation(int side, int j, int m, int l, int i, int
                    : fac_operator_transformation_rght[j][m][l][i][k][p];
 }
 
+// vec.svd(tu, p1, tv, p2, wout) (tensor_su2.cpp:1619-1758) with the global
+// max_dcut; returns dout (entries of wout); kept[] receives the new bond's
+// multiplet counts per 2j in 0..63 (tu leg 2 after the call).
+int ref_svd(const int* dvec, const int* fvec, const double* xvec, const int* du, const int* fu, const double* xu,
+            const int* dv, const int* fv, const double* xv, double p1, double p2, int dcut, double* wout,
+            int* kept) {
+  tensor_su2 vec, tu, tv;
+  build_tensor(vec, dvec, fvec, xvec);
+  build_tensor(tu, du, fu, xu);
+  build_tensor(tv, dv, fv, xv);
+  max_dcut = dcut;
+  int dout = 0;
+  vec.svd(tu, p1, tv, p2, dout, wout);
+  for (int i = 0; i < 64; ++i) kept[i] = 0;
+  for (int i = 0; i < tu.get_nmoment(2); ++i) kept[tu.get_angularmoment(2, i)] = tu.get_bonddim(2, i);
+  return dout;
+}
+
 // su2bond::fuse (su2bond.cpp:155-210); returns the sector count
 int ref_fuse(int n1, const int* a1, const int* d1, int n2, const int* a2, const int* d2, int* aout, int* dout) {
   std::vector<int> x1(a1, a1 + n1), y1(d1, d1 + n1), x2(a2, a2 + n2), y2(d2, d2 + n2);

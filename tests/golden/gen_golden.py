@@ -15,6 +15,8 @@ Fixtures:
   env_op_*.npz         tensor_su2::operator_transformation cases (both flags)
   env_ovl_*.npz        tensor_su2::overlap_transformation cases (both flags)
   fac_optrans.npz      fac_operator_transformation_{left,rght} entries
+  svd_*.npz            tensor_su2::svd truncation cases (singular values, kept
+                       multiplets per sector)
   dmrg_energies.json   whole reference DMRG runs (E0 - 1000 per sweep)
 """
 from __future__ import annotations
@@ -181,6 +183,60 @@ def env_cases(L, rng):
     return cases
 
 
+def fuse_bond(a, b):
+    out = {}
+    for x, dx in zip(a[1], a[2]):
+        for y, dy in zip(b[1], b[2]):
+            for k in range(abs(x - y), min(x + y, 38) + 1, 2):
+                out[k] = out.get(k, 0) + dx * dy
+    ks = sorted(out)
+    return (-1, ks, [out[k] for k in ks])
+
+
+def svd_cases(L, rng):
+    L.ref_svd.restype = ctypes.c_int
+    cases = []
+    specs = [  # (left bond sectors, dims, right bond sectors, dims, p1, p2, max_dcut, scale decay)
+        ([0, 1, 2, 3], [3, 5, 4, 2], [0, 1, 2, 3], [3, 5, 4, 2], 1.0, 0.0, 10, 0.0),
+        ([0, 1, 2, 3], [3, 5, 4, 2], [0, 1, 2, 3], [2, 4, 6, 3], 0.0, 1.0, 12, 0.0),
+        ([0, 2, 4, 6], [4, 8, 6, 3], [0, 2, 4], [6, 7, 4], 1.0, 0.0, 20, 1.0),
+        ([1, 3, 5], [9, 7, 5], [1, 3, 5, 7], [5, 8, 8, 2], 0.0, 1.0, 1000, 0.3),
+        ([0, 1, 2, 3, 4], [6, 10, 9, 6, 3], [0, 1, 2, 3, 4], [6, 10, 9, 6, 3], 1.0, 0.0, 30, 3.0),
+    ]
+    ph = (-1, [1], [1])
+    for ci, (la, lda, ra, rda, p1, p2, dcut, decay) in enumerate(specs):
+        Lb, Rb = (-1, la, lda), (-1, ra, rda)
+        EL, ER = fuse_bond(Lb, ph), fuse_bond(Rb, ph)
+        vb = [EL, ER]
+        dvec = desc_of(vb)
+        fvec = legal_flags(L, dvec)
+        # blocks with decaying spectra: product of random orthogonal-ish factors
+        xs = []
+        for i in range(nten_of(vb)):
+            if not fvec[i]:
+                continue
+            m, n = block_shape(vb, i)
+            blk = rng.standard_normal((m, n))
+            if decay > 0:
+                u, sv, vt = np.linalg.svd(blk, full_matrices=False)
+                sv = np.exp(-decay * np.arange(len(sv))) * (1 + rng.random(len(sv)))
+                blk = (u * sv) @ vt
+            xs.append(blk.ravel(order="F"))
+        xvec = np.concatenate(xs)
+        tub = [Lb, ph, (1, [0], [1])]
+        tvb = [Rb, ph, (1, [0], [1])]
+        du, dv = desc_of(tub), desc_of(tvb)
+        fu, fv = legal_flags(L, du), legal_flags(L, dv)
+        xu, xv = random_data(tub, fu, rng), random_data(tvb, fv, rng)
+        w = np.zeros(4096)
+        kept = np.zeros(64, np.int32)
+        n = L.ref_svd(p(dvec), p(fvec), p(xvec), p(du), p(fu), p(xu), p(dv), p(fv), p(xv), ctypes.c_double(p1),
+                      ctypes.c_double(p2), dcut, p(w), p(kept))
+        cases.append(dict(name=f"svd_{ci}", dvec=dvec, fvec=fvec, xvec=xvec, p1=np.float64(p1), p2=np.float64(p2),
+                          dcut=np.int32(dcut), wout=w[:n].copy(), kept=kept))
+    return cases
+
+
 def fac_optrans(L):
     L.ref_fac_operator_transformation.restype = ctypes.c_double
     idx, val = [], []
@@ -276,7 +332,7 @@ def main():
              idx=np.cumsum([0] + [len(v) for v in vals]))
     np.savez(os.path.join(HERE, "meta.npz"), **meta_cases(L, rng))
     np.savez_compressed(os.path.join(HERE, "fac_optrans.npz"), **fac_optrans(L))
-    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng):
+    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:

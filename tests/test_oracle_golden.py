@@ -152,3 +152,39 @@ def test_env_transform_matches_reference(oracle, path):
     out, y = oracle.env_transform(kind, su, g["xu"], su, g["xv"], so, g["xop"], int(g["flag"]))
     assert out.flag.tolist() == g["rflag"].tolist()  # the same blocks exist
     assert np.linalg.norm(y - g["rx"]) <= 1e-13 * np.linalg.norm(g["rx"])
+
+
+def svd_value_tolerance(ref, smax):
+    """Singular values come from Gram eigenvalues (tensor.cpp:1488-1541), so a
+    value s is known to about eps*s_max^2/s: the bar is 1e-12*s_max plus that."""
+    return 1e-12 * smax + 1e-15 * smax**2 / np.maximum(np.abs(ref), 1e-300)
+
+
+def check_truncation_values(wout, ref, nkept):
+    """The kept values (the first nkept of wout, the reference's order) within
+    svd_value_tolerance; of the discarded tail only the values above 1e-6 of
+    the largest are compared (as a sorted set): below that the Gram
+    eigenvalues are rounding noise, and the reference keeps every positive one
+    above 1e-100 of the largest (tensor.cpp:1534-1541), so even their number
+    is noise."""
+    smax = np.abs(ref).max()
+    assert np.all(np.abs(wout[:nkept] - ref[:nkept]) <= svd_value_tolerance(ref[:nkept], smax))
+    floor = 1e-6 * smax
+    a = np.sort(wout[nkept:][wout[nkept:] > floor])
+    b = np.sort(ref[nkept:][ref[nkept:] > floor])
+    assert len(a) == len(b)
+    assert np.all(np.abs(a - b) <= svd_value_tolerance(b, smax))
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "svd_*.npz"))))
+def test_truncation_matches_reference(oracle, path):
+    """Kept multiplets per sector exactly; singular values as
+    check_truncation_values states."""
+    g = np.load(path)
+    vs = oracle.struct_from_desc(g["dvec"], g["fvec"])
+    dims, wout, uv = oracle.svd_truncate(vs, g["xvec"], float(g["p1"]), float(g["p2"]), int(g["dcut"]))
+    kept = np.zeros(64, np.int32)
+    for i, d in enumerate(dims):
+        kept[vs.bonds[0].angm[i]] = d
+    assert kept.tolist() == g["kept"].tolist()
+    check_truncation_values(wout, g["wout"], int(g["kept"].sum()))
