@@ -178,6 +178,30 @@ int su2g_overlap_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag,
 int su2g_overlap_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* hhs,
                                 double* const* outs, int mode, void* stream);
 
+/* ---------------------------------------------------------- truncation -- */
+/* vec.svd(tu, p1, tv, p2, dout, wout) (tensor_su2.cpp:1619-1758 with the
+ * per-sector tensor::svd of tensor.cpp:1472-1700): splits the two-leg wave
+ * function psi (device; legs = the fused legs 0, 1 of tu and of tv) back into
+ * two MPS tensors, keeping the max_dcut largest multiplets over all spin
+ * sectors (the reference's global max_dcut, passed here).  Per sector: Gram
+ * matrix of the smaller side, FP64 eigendecomposition with the reference's
+ * refinement of the small-eigenvalue subspace, values above 1e-100 of the
+ * largest kept, columns scaled by s^p1 (U) and s^p2 (V); the global choice
+ * uses the reference's Shell sort (sort2.f dsort2), so ties go the same way.
+ *   tu_desc, tv_desc  3-leg descs of the current tu / tv: legs 0, 1 are used
+ *   bond              out: the new bond [n, 2j[n], dim[n]] (direction -1),
+ *                     bond_cap >= 1 + 2 * (sectors of psi leg 0)
+ *   wout, dout        out: singular values, kept (per sector, ascending) then
+ *                     discarded, as the reference writes them; *dout = count
+ *   tu, tv            out (device, may be NULL): the new MPS tensors, layout
+ *                     of [3, 0, tu leg 0, tu leg 1, (-1, bond)] (resp. tv)
+ *                     with every legal block present (su2g_layout with a NULL
+ *                     flag array); at most tu_cap / tv_cap doubles
+ * Blocks until done. */
+int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const int* tu_desc, double p1,
+             const int* tv_desc, double p2, int max_dcut, int* bond, int bond_cap, double* wout, int wout_cap,
+             int* dout, double* tu, int64_t tu_cap, double* tv, int64_t tv_cap, void* stream);
+
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme
  * (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195, driven as in

@@ -545,3 +545,59 @@ def svd_truncate(vs: Struct, x, p1, p2, max_dcut):
         else:
             disc_w += list(s)
     return dims, np.asarray(kept_w + disc_w), uv
+
+
+def _fused_rows(b0: Bond, b1: Bond, c: int):
+    """Row ranges of the (a, sigma) sub-blocks inside fused sector 2j = c, in the
+    order tensor_su2::fuse places them (tensor_su2.cpp:878-900): sigma sectors
+    outer, bond sectors inner, d_a * d_sigma rows each (a fastest)."""
+    rows, pos = {}, 0
+    for j1, s in enumerate(b1.angm):
+        for j0, a in enumerate(b0.angm):
+            if abs(a - s) <= c <= a + s and (a + s - c) % 2 == 0:
+                rows[(j0, j1)] = (pos, b0.dim[j0] * b1.dim[j1])
+                pos += b0.dim[j0] * b1.dim[j1]
+    return rows
+
+
+def svd_mps(vs: Struct, dims, uv, tu_bonds, tv_bonds):
+    """The new MPS tensors of tensor_su2::svd (tensor_su2.cpp:1733-1745):
+    tu = fuse(tu legs 0, 1) contracted with the kept U columns, tv likewise
+    with V; new bond of direction -1 with the kept multiplets.  The fuse
+    tensor is a row placement with canonical CG, so each block of tu is a row
+    range of its sector's U.  Returns ((tu Struct, x), (tv Struct, x))."""
+    n0 = len(vs.bonds[0].angm)
+    kept = [i for i in range(n0) if dims[i] > 0]
+    newb = Bond(-1, [vs.bonds[0].angm[i] for i in kept], [int(dims[i]) for i in kept])
+    res = []
+    for side, (b0, b1) in ((0, tu_bonds), (1, tv_bonds)):
+        S = Struct([b0, b1, newb], 0).with_legal_flags()
+        off, tot = S.offsets()
+        x = np.zeros(tot)
+        for bi in range(S.nten):
+            if not S.flag[bi]:
+                continue
+            j0, j1, j2 = bi % len(b0.angm), (bi // len(b0.angm)) % len(b1.angm), bi // (len(b0.angm) * len(b1.angm))
+            c = newb.angm[j2]
+            r0, m = _fused_rows(b0, b1, c)[(j0, j1)]
+            mat = uv[vs.bonds[0].angm.index(c)][side]
+            x[off[bi]: off[bi] + m * newb.dim[j2]] = mat[r0: r0 + m, :].ravel(order="F")
+        res.append((S, x))
+    return tuple(res)
+
+
+def mps_sector_matrices(S: Struct, x):
+    """Inverse of the placement in svd_mps: {2j of leg 2: (fused rows x kept)}."""
+    b0, b1, b2 = S.bonds
+    off, _ = S.offsets()
+    out = {}
+    for j2, c in enumerate(b2.angm):
+        rows = _fused_rows(b0, b1, c)
+        nrow = sum(m for _, m in rows.values())
+        mat = np.zeros((nrow, b2.dim[j2]))
+        for (j0, j1), (r0, m) in rows.items():
+            bi = j0 + len(b0.angm) * (j1 + len(b1.angm) * j2)
+            if S.flag[bi]:
+                mat[r0: r0 + m, :] = np.asarray(x[off[bi]: off[bi] + m * b2.dim[j2]]).reshape(m, -1, order="F")
+        out[c] = mat
+    return out

@@ -44,6 +44,8 @@ int nkrylov = 0, disk = 0;
 namespace {
 dmrg_su2* g_tables = nullptr;  // owner of the recoupling tables
 tensor_su2 g_result;           // last result, read back by ref_result_*
+tensor_su2 g_result_b;         // second result (tv of ref_svd)
+tensor_su2* g_sel = &g_result;
 
 void desc_to_struct(const int* desc, su2struct& s) {
   int nb = desc[0], locspin = desc[1], p = 2;
@@ -130,11 +132,11 @@ int ref_contract(const int* da, const int* fa, const double* xa, int ia, const i
 }
 
 void ref_result_sizes(int* nten, int* nele1, int* nele2) {
-  *nten = g_result.get_nten();
-  g_result.get_nelement(*nele1, *nele2);
+  *nten = g_sel->get_nten();
+  g_sel->get_nelement(*nele1, *nele2);
 }
 
-void ref_result_get(int* flag, double* tele1, double* tele2) { g_result.get_telement(tele1, tele2, flag); }
+void ref_result_get(int* flag, double* tele1, double* tele2) { g_sel->get_telement(tele1, tele2, flag); }
 
 // result = operator_transformation(uu, vv, op, flag)  (tensor_su2_dmrg_src.cpp:221-402)
 int ref_operator_transformation(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
@@ -170,7 +172,10 @@ double ref_fac_operator_transformation(int side, int j, int m, int l, int i, int
 int ref_svd(const int* dvec, const int* fvec, const double* xvec, const int* du, const int* fu, const double* xu,
             const int* dv, const int* fv, const double* xv, double p1, double p2, int dcut, double* wout,
             int* kept) {
-  tensor_su2 vec, tu, tv;
+  // tu, tv end up in g_result, g_result_b (tensor_su2 has no copy assignment)
+  tensor_su2 vec;
+  tensor_su2& tu = g_result;
+  tensor_su2& tv = g_result_b;
   build_tensor(vec, dvec, fvec, xvec);
   build_tensor(tu, du, fu, xu);
   build_tensor(tv, dv, fv, xv);
@@ -180,6 +185,25 @@ int ref_svd(const int* dvec, const int* fvec, const double* xvec, const int* du,
   for (int i = 0; i < 64; ++i) kept[i] = 0;
   for (int i = 0; i < tu.get_nmoment(2); ++i) kept[tu.get_angularmoment(2, i)] = tu.get_bonddim(2, i);
   return dout;
+}
+
+// Selects which result ref_result_* read: 0 = the last result (tu after
+// ref_svd), 1 = tv after ref_svd.
+void ref_select_result(int which) { g_sel = which ? &g_result_b : &g_result; }
+
+// desc of the selected result; returns its length
+int ref_result_desc(int* out) {
+  su2struct& c = g_sel->get_cgc();
+  int p = 0;
+  out[p++] = c.get_nbond();
+  out[p++] = c.get_locspin();
+  for (int l = 0; l < c.get_nbond(); ++l) {
+    out[p++] = c.get_bonddir(l);
+    out[p++] = c.get_nmoment(l);
+    for (int i = 0; i < c.get_nmoment(l); ++i) out[p++] = c.get_angularmoment(l, i);
+    for (int i = 0; i < c.get_nmoment(l); ++i) out[p++] = c.get_bonddim(l, i);
+  }
+  return p;
 }
 
 // su2bond::fuse (su2bond.cpp:155-210); returns the sector count

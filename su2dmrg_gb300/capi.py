@@ -71,6 +71,7 @@ _PROTOS = {
     "su2g_operator_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
     "su2g_overlap_transformation_layout": (_i, [Tensor, Tensor, _i, Tensor, _vp, _i, _vp, _i, _vp]),
     "su2g_overlap_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
+    "su2g_svd": (_i, [_vp, _vp, _vp, _vp, _d, _vp, _d, _i, _vp, _i, _vp, _i, _vp, _vp, _i64, _vp, _i64, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),
     "su2g_vec_scale": (_i, [_d, _vp, _i64, _vp]),

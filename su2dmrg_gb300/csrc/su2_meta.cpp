@@ -9,6 +9,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <utility>
 
 namespace su2g {
 
@@ -296,6 +297,15 @@ double fac_operator_transformation(int side, int j, int m, int l, int i, int k, 
   std::lock_guard<std::mutex> lock(mu);
   cache[key] = v;
   return v;
+}
+
+void dsort2(int n, double* key, int* tag) {
+  for (int gap = n / 2; gap > 0; gap /= 2)
+    for (int i = gap; i < n; ++i)
+      for (int j = i - gap; j >= 0 && key[j] > key[j + gap]; j -= gap) {
+        std::swap(key[j], key[j + gap]);
+        std::swap(tag[j], tag[j + gap]);
+      }
 }
 
 }  // namespace su2g

@@ -86,4 +86,10 @@ const std::vector<double>& fac_hamilt_vec_table();
 // Entries are computed on first use and cached (thread safe).
 double fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p);
 
+// Ascending Shell sort of key[0..n) (gaps n/2, n/4, ..., 1, exchange inner
+// loop), carrying tag[] along: the dsort2 of sort2.f:76-108.  Equal keys end
+// up in the order this exchange sequence leaves them, which decides which of
+// two degenerate multiplets the truncation keeps.
+void dsort2(int n, double* key, int* tag);
+
 }  // namespace su2g

@@ -1,0 +1,355 @@
+// Truncation of a two-site vector (tensor_su2::svd, tensor_su2.cpp:1619-1758,
+// with the per-sector tensor::svd of tensor.cpp:1472-1700), on the GPU:
+//   * per sector, the Gram matrix of the smaller side (cuBLAS DGEMM) and its
+//     FP64 eigendecomposition (cuSOLVER syevd, eigenvalues ascending like
+//     dsyev), then the reference's refinement: while more than one eigenvalue
+//     lies below 0.1 of the largest of the current subspace, re-diagonalise
+//     the original Gram matrix projected on that subspace;
+//   * the other factor by one more product, singular values = sqrt of the
+//     eigenvalues above 1e-100 of the largest, columns scaled by s^(p1-1) and
+//     s^p2 (or the mirror for wide blocks);
+//   * on the host: all kept singular values sorted by the Shell sort of
+//     sort2.f (dsort2, whose handling of equal values decides ties), the
+//     largest max_dcut multiplets kept (no (2j+1) weighting), and the
+//     singular values reported kept-then-discarded as the reference writes
+//     them.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+#include "su2_meta.hpp"
+#include "su2g.h"
+
+namespace {
+
+int fail(int code, const std::string& msg) { return su2g::set_last_error(code, msg); }
+
+__global__ void scale_columns(double* a, int rows, int c0, int ncol, int ld, const double* f) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (int64_t)rows * ncol;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % rows), c = (int)(idx / rows);
+    a[(int64_t)(c0 + c) * ld + r] *= f[c];
+  }
+}
+
+struct Ctx {
+  cudaStream_t st;
+  cublasHandle_t blas = nullptr;
+  cusolverDnHandle_t sol = nullptr;
+  std::vector<void*> allocs;
+  std::string err;
+  int code = SU2G_OK;
+
+  ~Ctx() {
+    for (void* p : allocs) cudaFree(p);
+    if (blas) cublasDestroy(blas);
+    if (sol) cusolverDnDestroy(sol);
+  }
+  bool ok() const { return code == SU2G_OK; }
+  void set(int c, const std::string& m) {
+    if (code == SU2G_OK) {
+      code = c;
+      err = m;
+    }
+  }
+  double* dalloc(int64_t n) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(double));
+    if (e != cudaSuccess) {
+      set(e == cudaErrorMemoryAllocation ? SU2G_ENOMEM : SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+      return nullptr;
+    }
+    allocs.push_back(p);
+    return (double*)p;
+  }
+  void gemm(cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const double* a, int lda, const double* b,
+            int ldb, double* c, int ldc) {
+    if (!ok() || m == 0 || n == 0) return;
+    const double one = 1.0, zero = 0.0;
+    if (cublasDgemm(blas, ta, tb, m, n, k, &one, a, lda, b, ldb, &zero, c, ldc) != CUBLAS_STATUS_SUCCESS)
+      set(SU2G_ECUDA, "svd: cublasDgemm failed");
+  }
+  void copy(double* dst, const double* src, int64_t n) {
+    if (!ok()) return;
+    cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+  }
+  // symmetric eigendecomposition in place (a: n x n, ld n); w: host eigenvalues
+  void eigh(double* a, int n, std::vector<double>* w) {
+    if (!ok()) return;
+    int lwork = 0;
+    double* dw = dalloc(n);
+    if (!ok()) return;
+    if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS) {
+      set(SU2G_ECUDA, "svd: syevd buffer query failed");
+      return;
+    }
+    double* work = dalloc(lwork);
+    double* dinfo = dalloc(1);
+    if (!ok()) return;
+    if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, work, lwork,
+                         (int*)dinfo) != CUSOLVER_STATUS_SUCCESS) {
+      set(SU2G_ECUDA, "svd: syevd failed");
+      return;
+    }
+    w->assign(n, 0.0);
+    int info = 0;
+    cudaError_t e = cudaMemcpyAsync(w->data(), dw, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+    else if (info != 0) set(SU2G_ECUDA, "svd: syevd did not converge (info " + std::to_string(info) + ")");
+  }
+};
+
+// index after the last eigenvalue below tol1 of the largest (tensor.cpp:1492-1497)
+int small_count(const std::vector<double>& w, int n) {
+  for (int i = n - 1; i >= 0; --i)
+    if (w[i] / w[n - 1] < 1.e-1) return i + 1;
+  return 0;
+}
+
+struct Sector {
+  int i = -1;      // leg-0 sector index
+  int m = 0, n = 0;
+  int dc = 0;      // singular values kept by the sector's own rule
+  double* u = nullptr;  // m x dc (ld m), smallest first
+  double* v = nullptr;  // n x dc (ld n)
+  std::vector<double> s;  // dc values, ascending
+};
+
+// tensor::svd for one m x n block (n0 = 1)
+void sector_svd(Ctx& c, const double* blk, int m, int n, double p1, double p2, int max_dcut, Sector* out) {
+  const bool tall = m >= n;
+  const int k = tall ? n : m;
+  double* G = c.dalloc((int64_t)k * k);
+  double* A0 = c.dalloc((int64_t)k * k);
+  if (!c.ok()) return;
+  if (tall) c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, blk, m, blk, m, G, n);
+  else c.gemm(CUBLAS_OP_N, CUBLAS_OP_T, m, m, n, blk, m, blk, m, G, m);
+  c.copy(A0, G, (int64_t)k * k);
+  std::vector<double> w;
+  c.eigh(G, k, &w);  // G now holds the eigenvectors (k x k)
+  if (!c.ok()) return;
+  int np = small_count(w, k);
+  if (np > 1) {  // refinement of the small-eigenvalue subspace (tensor.cpp:1498-1529)
+    double* ap = c.dalloc((int64_t)k * k);
+    double* vp = c.dalloc((int64_t)k * k);
+    double* app = c.dalloc((int64_t)k * k);
+    double* vpp = c.dalloc((int64_t)k * k);
+    double* tmp = c.dalloc((int64_t)k * k);
+    c.copy(ap, A0, (int64_t)k * k);
+    c.copy(vp, G, (int64_t)k * k);
+    int npp = np;
+    np = k;
+    std::vector<double> ws;
+    do {
+      c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, npp, np, np, vp, np, ap, np, app, npp);
+      c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, npp, npp, np, app, npp, vp, np, vpp, npp);
+      c.copy(ap, vpp, (int64_t)npp * npp);
+      c.eigh(vpp, npp, &ws);
+      if (!c.ok()) return;
+      for (int q = 0; q < npp; ++q) w[q] = ws[q];
+      c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, k, npp, npp, G, k, vpp, npp, tmp, k);
+      c.copy(G, tmp, (int64_t)k * npp);
+      c.copy(vp, vpp, (int64_t)npp * npp);
+      const int j = small_count(ws, npp);
+      np = npp;
+      npp = j;
+    } while (npp > 1 && c.ok());
+  }
+  if (!c.ok()) return;
+  double *U, *V;
+  if (tall) {  // V = eigenvectors (n x n), U = blk V (m x n)
+    V = G;
+    U = c.dalloc((int64_t)m * n);
+    c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, m, n, n, blk, m, V, n, U, m);
+  } else {  // U = eigenvectors (m x m), V = blk^T U (n x m)
+    U = G;
+    V = c.dalloc((int64_t)n * m);
+    c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, m, m, blk, m, U, m, V, n);
+  }
+  if (!c.ok()) return;
+  // singular values above 1e-100 of the largest, scaling (tensor.cpp:1532-1567)
+  const double num = w[k - 1];
+  int dcut = 0;
+  if (num > 1.e-100)
+    for (int i = k - 1; i >= 0; --i) {
+      if (w[i] / num > 1.e-100) {
+        w[i] = std::sqrt(w[i]);
+        ++dcut;
+      } else {
+        w[i] = 0;
+      }
+    }
+  if (dcut > max_dcut) dcut = max_dcut;
+  if (dcut > (tall ? m : n)) dcut = tall ? m : n;
+  std::vector<double> fu(dcut), fv(dcut);
+  for (int q = 0; q < dcut; ++q) {
+    const double s = w[k - dcut + q];
+    if (s > 0) {
+      fu[q] = tall ? std::pow(s, p1 - 1.) : std::pow(s, p1);
+      fv[q] = tall ? std::pow(s, p2) : std::pow(s, p2 - 1.);
+    } else {
+      fu[q] = fv[q] = 0.0;
+    }
+  }
+  if (dcut > 0) {
+    double* dfu = c.dalloc(dcut);
+    double* dfv = c.dalloc(dcut);
+    if (!c.ok()) return;
+    cudaMemcpyAsync(dfu, fu.data(), dcut * sizeof(double), cudaMemcpyHostToDevice, c.st);
+    cudaMemcpyAsync(dfv, fv.data(), dcut * sizeof(double), cudaMemcpyHostToDevice, c.st);
+    scale_columns<<<256, 256, 0, c.st>>>(U, m, k - dcut, dcut, m, dfu);
+    scale_columns<<<256, 256, 0, c.st>>>(V, n, k - dcut, dcut, n, dfv);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+  }
+  out->m = m;
+  out->n = n;
+  out->dc = dcut;
+  out->u = U + (int64_t)m * (k - dcut);
+  out->v = V + (int64_t)n * (k - dcut);
+  out->s.assign(w.begin() + (k - dcut), w.begin() + k);
+}
+
+}  // namespace
+
+// first row of the (a, sigma) sub-block inside fused sector 2j = c, in the
+// order tensor_su2::fuse places them (tensor_su2.cpp:878-900): sigma sectors
+// outer, bond sectors inner, d_a * d_sigma rows each
+int fused_row(const su2g::Bond& b0, const su2g::Bond& b1, int c, int j0, int j1) {
+  int pos = 0;
+  for (int q1 = 0; q1 < b1.n(); ++q1)
+    for (int q0 = 0; q0 < b0.n(); ++q0) {
+      const int a = b0.angm[q0], s = b1.angm[q1];
+      if (c < std::abs(a - s) || c > a + s || (a + s - c) % 2) continue;
+      if (q0 == j0 && q1 == j1) return pos;
+      pos += b0.dim[q0] * b1.dim[q1];
+    }
+  return -1;
+}
+
+bool same_sectors(const su2g::Bond& a, const su2g::Bond& b) { return a.angm == b.angm && a.dim == b.dim; }
+
+extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const int* tu_desc, double p1,
+                        const int* tv_desc, double p2, int max_dcut, int* bond, int bond_cap, double* wout,
+                        int wout_cap, int* dout, double* tu, int64_t tu_cap, double* tv, int64_t tv_cap,
+                        void* stream) {
+  su2g::Struct P, TU, TV;
+  std::string e;
+  if (!psi_desc || !P.parse(psi_desc, &e)) return fail(SU2G_EINVAL, "svd: psi: " + e);
+  if (P.nbond != 2) return fail(SU2G_EINVAL, "svd: psi must have 2 legs");
+  if (!tu_desc || !TU.parse(tu_desc, &e) || TU.nbond != 3) return fail(SU2G_EINVAL, "svd: tu: 3-leg desc expected " + e);
+  if (!tv_desc || !TV.parse(tv_desc, &e) || TV.nbond != 3) return fail(SU2G_EINVAL, "svd: tv: 3-leg desc expected " + e);
+  if (!bond || !wout || !dout || max_dcut < 0) return fail(SU2G_EINVAL, "svd: bad arguments");
+  // psi legs are the fused (tu leg 0, tu leg 1) and (tv leg 0, tv leg 1) (tensor_su2.cpp:1628-1634)
+  if (!same_sectors(su2g::fuse(TU.legs[0], TU.legs[1]), P.legs[0]) ||
+      !same_sectors(su2g::fuse(TV.legs[0], TV.legs[1]), P.legs[1]))
+    return fail(SU2G_EINVAL, "svd: psi legs are not the fused legs 0, 1 of tu / tv");
+  P.set_layout(psi_flag);
+  if (P.total > 0 && !psi) return fail(SU2G_EINVAL, "svd: null psi");
+  Ctx c;
+  c.st = (cudaStream_t)stream;
+  if (cublasCreate(&c.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&c.sol) != CUSOLVER_STATUS_SUCCESS)
+    return fail(SU2G_ECUDA, "svd: cannot create cuBLAS/cuSOLVER handles");
+  cublasSetStream(c.blas, c.st);
+  cusolverDnSetStream(c.sol, c.st);
+  const int n0 = P.legs[0].n(), n1 = P.legs[1].n();
+  std::vector<Sector> secs;
+  // sectors in the reference's loop order: leg-0 sector, then the leg-1 sector of equal spin
+  for (int i = 0; i < n0 && c.ok(); ++i)
+    for (int j = 0; j < n1 && c.ok(); ++j) {
+      if (P.legs[0].angm[i] != P.legs[1].angm[j]) continue;
+      const int b = i + j * n0;
+      if (!P.flag[b]) continue;
+      Sector s;
+      s.i = i;
+      sector_svd(c, psi + P.offset[b], P.legs[0].dim[i], P.legs[1].dim[j], p1, p2, max_dcut, &s);
+      secs.push_back(s);
+    }
+  if (!c.ok()) return fail(c.code, c.err);
+  // global selection of the max_dcut largest multiplets (tensor_su2.cpp:1686-1695)
+  std::vector<double> ws;
+  std::vector<int> is;
+  for (const Sector& s : secs)
+    for (int q = 0; q < s.dc; ++q) {
+      ws.push_back(s.s[q]);
+      is.push_back(s.i);
+    }
+  const int n = (int)ws.size();
+  su2g::dsort2(n, ws.data(), is.data());
+  std::vector<int> dim(n0, 0);
+  for (int q = n - 1; q >= std::max(0, n - max_dcut); --q) ++dim[is[q]];
+  // the new bond: kept sectors of psi leg 0, direction -1 (tensor_su2.cpp:1733)
+  su2g::Bond nb;
+  nb.dir = -1;
+  for (int i = 0; i < n0; ++i)
+    if (dim[i] > 0) {
+      nb.angm.push_back(P.legs[0].angm[i]);
+      nb.dim.push_back(dim[i]);
+    }
+  if (bond_cap < 1 + 2 * nb.n()) return fail(SU2G_EINVAL, "svd: bond output too small");
+  bond[0] = nb.n();
+  for (int q = 0; q < nb.n(); ++q) {
+    bond[1 + q] = nb.angm[q];
+    bond[1 + nb.n() + q] = nb.dim[q];
+  }
+  // kept values (per sector, ascending), then the discarded ones (tensor_su2.cpp:1706-1731)
+  if (n > wout_cap) return fail(SU2G_EINVAL, "svd: wout too small (" + std::to_string(n) + " values)");
+  int total_kept = 0;
+  for (int d : dim) total_kept += d;
+  int mk = 0, md = total_kept;
+  for (const Sector& s : secs) {
+    const int d = dim[s.i];
+    for (int q = 0; q < d; ++q) wout[mk + q] = s.s[s.dc - d + q];
+    for (int q = 0; q < s.dc - d; ++q) wout[md + q] = s.s[q];
+    mk += d;
+    md += s.dc - d;
+  }
+  *dout = md;
+  // tu = fuse(tu legs 0, 1) x kept U, tv likewise with V: row ranges of the
+  // kept columns, every legal block present (tensor_su2.cpp:1733-1745)
+  for (int side = 0; side < 2; ++side) {
+    double* out = side ? tv : tu;
+    if (!out) continue;
+    const su2g::Struct& T = side ? TV : TU;
+    su2g::Struct O;
+    O.nbond = 3;
+    O.locspin = 0;
+    O.legs[0] = T.legs[0];
+    O.legs[1] = T.legs[1];
+    O.legs[2] = nb;
+    O.nten = O.legs[0].n() * O.legs[1].n() * nb.n();
+    O.set_layout(nullptr);
+    if (O.total > (side ? tv_cap : tu_cap))
+      return fail(SU2G_EINVAL, std::string("svd: ") + (side ? "tv" : "tu") + " output too small (" +
+                                   std::to_string(O.total) + " doubles)");
+    for (int b = 0; b < O.nten; ++b) {
+      if (!O.flag[b]) continue;
+      int sec[3];
+      O.sectors(b, sec);
+      const int ang = nb.angm[sec[2]], d = nb.dim[sec[2]];
+      const Sector* src = nullptr;
+      for (const Sector& s : secs)
+        if (P.legs[0].angm[s.i] == ang) src = &s;
+      const int r0 = fused_row(O.legs[0], O.legs[1], ang, sec[0], sec[1]);
+      const int rows = O.legs[0].dim[sec[0]] * O.legs[1].dim[sec[1]];
+      if (!src || r0 < 0) return fail(SU2G_EINVAL, "svd: internal placement error");
+      const int ld = side ? src->n : src->m;
+      const double* col0 = (side ? src->v : src->u) + (int64_t)ld * (src->dc - d) + r0;
+      cudaError_t ce = cudaMemcpy2DAsync(out + O.offset[b], rows * sizeof(double), col0, ld * sizeof(double),
+                                         rows * sizeof(double), d, cudaMemcpyDeviceToDevice, c.st);
+      if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+    }
+  }
+  cudaError_t ce = cudaStreamSynchronize(c.st);
+  if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+  return SU2G_OK;
+}

@@ -66,7 +66,8 @@ class Su2Struct:
 
     def legal(self) -> np.ndarray:
         out = np.zeros(self.nten, np.int32)
-        n = lib().su2g_struct_legal(ptr(self.desc()), ptr(out))
+        desc = self.desc()  # held: ptr() of a temporary could dangle during the call
+        n = lib().su2g_struct_legal(ptr(desc), ptr(out))
         if n < 0:
             raise capi.Su2gError(capi.SU2G_EINVAL, "malformed structure")
         return out
@@ -77,7 +78,8 @@ class Su2Struct:
 
     def offsets(self):
         off = np.zeros(self.nten, np.int64)
-        total = lib().su2g_layout(ptr(self.desc()), ptr(np.ascontiguousarray(self.flag, np.int32)), ptr(off))
+        desc, flag = self.desc(), np.ascontiguousarray(self.flag, np.int32)
+        total = lib().su2g_layout(ptr(desc), ptr(flag), ptr(off))
         if total < 0:
             raise capi.Su2gError(capi.SU2G_EINVAL, "malformed structure")
         return off, int(total)
@@ -303,3 +305,45 @@ def operator_transformation(uu, xu, vv, xv, ops, outs, flag: int, mode: int = ca
 def overlap_transformation(uu, xu, vv, xv, hhs, outs, flag: int, mode: int = capi.MODE_F64, stream=None) -> None:
     """Batch of tensor_su2::overlap_transformation (2-leg scalar operators)."""
     _env_run(0, uu, xu, vv, xv, hhs, outs, flag, mode, stream)
+
+
+def svd(vec: Su2Struct, vec_data, tu: Su2Struct, p1: float, tv: Su2Struct, p2: float, max_dcut: int, stream=None):
+    """vec.svd(tu, p1, tv, p2, dout, wout) (tensor_su2.cpp:1619-1758) on the GPU.
+
+    vec: the two-leg wave function (device data); tu, tv: the current MPS
+    tensors' structures (legs 0, 1 are used).  Returns (tu_struct, tu_data,
+    tv_struct, tv_data, wout): the new MPS tensors as device arrays (every
+    legal block present) and the singular values, kept then discarded, as the
+    reference writes them."""
+    import torch
+
+    vd = np.ascontiguousarray(vec.desc(), np.int32)
+    vf = np.ascontiguousarray(vec.flag, np.int32)
+    ud = np.ascontiguousarray(tu.desc(), np.int32)
+    wd = np.ascontiguousarray(tv.desc(), np.int32)
+    # capacity: every common sector keeps at most min(its two sizes, max_dcut) multiplets
+    b0, b1 = vec.bonds
+    ucap = vcap = nval = 0
+    for a, m in zip(b0.angm, b0.dim):
+        if a in b1.angm:
+            n = b1.dim[b1.angm.index(a)]
+            k = min(m, n, max_dcut)
+            ucap += m * k
+            vcap += n * k
+            nval += min(m, n)
+    bond = np.zeros(1 + 2 * len(b0.angm), np.int32)
+    wout = np.zeros(max(1, nval))
+    dout = ctypes.c_int(0)
+    dev = vec_data.device if hasattr(vec_data, "device") else torch.device("cuda")
+    xu = torch.empty(max(1, ucap), dtype=torch.float64, device=dev)
+    xv = torch.empty(max(1, vcap), dtype=torch.float64, device=dev)
+    check(lib().su2g_svd(ptr(vd), ptr(vf), ptr(vec_data), ptr(ud), float(p1), ptr(wd), float(p2), int(max_dcut),
+                         ptr(bond), len(bond), ptr(wout), len(wout), ctypes.addressof(dout), ptr(xu), ucap, ptr(xv),
+                         vcap, stream_handle(stream)))
+    nb = int(bond[0])
+    newb = Su2Bond(-1, bond[1: 1 + nb].tolist(), bond[1 + nb: 1 + 2 * nb].tolist())
+    out = []
+    for s, x in ((tu, xu), (tv, xv)):
+        st = Su2Struct([s.bonds[0], s.bonds[1], newb], 0).with_legal_flags()
+        out += [st, x[: st.size()]]
+    return out[0], out[1], out[2], out[3], wout[: dout.value].copy()

@@ -232,8 +232,16 @@ def svd_cases(L, rng):
         kept = np.zeros(64, np.int32)
         n = L.ref_svd(p(dvec), p(fvec), p(xvec), p(du), p(fu), p(xu), p(dv), p(fv), p(xv), ctypes.c_double(p1),
                       ctypes.c_double(p2), dcut, p(w), p(kept))
+        out = {}
+        for sel, nm in ((0, "tu"), (1, "tv")):  # the new MPS tensors tu, tv
+            L.ref_select_result(sel)
+            d = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(d))
+            f, x, _ = read_result(L)
+            out.update({f"{nm}_desc": d[:nd].copy(), f"{nm}_flag": f, f"{nm}_x": x})
+        L.ref_select_result(0)
         cases.append(dict(name=f"svd_{ci}", dvec=dvec, fvec=fvec, xvec=xvec, p1=np.float64(p1), p2=np.float64(p2),
-                          dcut=np.int32(dcut), wout=w[:n].copy(), kept=kept))
+                          dcut=np.int32(dcut), wout=w[:n].copy(), kept=kept, du=du, dv=dv, **out))
     return cases
 
 

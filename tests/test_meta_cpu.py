@@ -160,3 +160,30 @@ def test_env_layouts_match_reference(su2lib, oracle):
         out = fn(su, g["xu"], su, g["xv"], so, g["xop"], int(g["flag"]))
         assert out.flag.tolist() == g["rflag"].tolist(), path
         assert out.size() == g["rx"].size
+
+
+def test_svd_argument_checks_without_gpu(su2lib):
+    """su2g_svd rejects a psi whose legs are not the fused legs of tu / tv, and
+    bad arguments, with SU2G_EINVAL before any device work."""
+    import ctypes
+
+    from su2dmrg_gb300 import capi
+
+    g = np.load(os.path.join(GOLDEN, "svd_0.npz"))
+    dvec, fvec, du, dv = (np.ascontiguousarray(g[k], np.int32) for k in ("dvec", "fvec", "du", "dv"))
+    bond = np.zeros(256, np.int32)
+    wout = np.zeros(4096)
+    dout = ctypes.c_int()
+
+    def call(d_u, d_v, dcut=10, wcap=4096):
+        return su2lib.su2g_svd(dvec.ctypes.data, fvec.ctypes.data, 8, d_u.ctypes.data, 1.0, d_v.ctypes.data, 0.0,
+                               dcut, bond.ctypes.data, len(bond), wout.ctypes.data, wcap, ctypes.addressof(dout),
+                               None, 0, None, 0, None)
+
+    bad = du.copy()
+    bad[4 + bad[3]] += 1  # first multiplet dim of tu leg 0
+    assert call(bad, dv) == capi.SU2G_EINVAL
+    assert b"fused" in su2lib.su2g_last_error()
+    assert call(du, dv, dcut=-1) == capi.SU2G_EINVAL
+    two_leg = dvec.copy()
+    assert call(two_leg, dv) == capi.SU2G_EINVAL

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
+from svd_checks import check_mps, check_truncation_values
 
 
 def test_fac_hamilt_vec_bit_exact(oracle):
@@ -154,28 +155,6 @@ def test_env_transform_matches_reference(oracle, path):
     assert np.linalg.norm(y - g["rx"]) <= 1e-13 * np.linalg.norm(g["rx"])
 
 
-def svd_value_tolerance(ref, smax):
-    """Singular values come from Gram eigenvalues (tensor.cpp:1488-1541), so a
-    value s is known to about eps*s_max^2/s: the bar is 1e-12*s_max plus that."""
-    return 1e-12 * smax + 1e-15 * smax**2 / np.maximum(np.abs(ref), 1e-300)
-
-
-def check_truncation_values(wout, ref, nkept):
-    """The kept values (the first nkept of wout, the reference's order) within
-    svd_value_tolerance; of the discarded tail only the values above 1e-6 of
-    the largest are compared (as a sorted set): below that the Gram
-    eigenvalues are rounding noise, and the reference keeps every positive one
-    above 1e-100 of the largest (tensor.cpp:1534-1541), so even their number
-    is noise."""
-    smax = np.abs(ref).max()
-    assert np.all(np.abs(wout[:nkept] - ref[:nkept]) <= svd_value_tolerance(ref[:nkept], smax))
-    floor = 1e-6 * smax
-    a = np.sort(wout[nkept:][wout[nkept:] > floor])
-    b = np.sort(ref[nkept:][ref[nkept:] > floor])
-    assert len(a) == len(b)
-    assert np.all(np.abs(a - b) <= svd_value_tolerance(b, smax))
-
-
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "svd_*.npz"))))
 def test_truncation_matches_reference(oracle, path):
     """Kept multiplets per sector exactly; singular values as
@@ -188,3 +167,17 @@ def test_truncation_matches_reference(oracle, path):
         kept[vs.bonds[0].angm[i]] = d
     assert kept.tolist() == g["kept"].tolist()
     check_truncation_values(wout, g["wout"], int(g["kept"].sum()))
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "svd_*.npz"))))
+def test_truncation_mps_matches_reference(oracle, path):
+    """The new MPS tensors tu, tv: the oracle's row placement of the kept
+    U, V columns against the reference's fuse + contract, gauge-free."""
+    g = np.load(path)
+    vs = oracle.struct_from_desc(g["dvec"], g["fvec"])
+    dims, _, uv = oracle.svd_truncate(vs, g["xvec"], float(g["p1"]), float(g["p2"]), int(g["dcut"]))
+    su, sv = oracle.struct_from_desc(g["du"]), oracle.struct_from_desc(g["dv"])
+    tu, tv = oracle.svd_mps(vs, dims, uv, su.bonds[:2], sv.bonds[:2])
+    rtu = (oracle.struct_from_desc(g["tu_desc"], g["tu_flag"]), g["tu_x"])
+    rtv = (oracle.struct_from_desc(g["tv_desc"], g["tv_flag"]), g["tv_x"])
+    check_mps(oracle, tu, tv, rtu, rtv)
