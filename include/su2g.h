@@ -178,6 +178,54 @@ int su2g_overlap_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag,
 int su2g_overlap_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* hhs,
                                 double* const* outs, int mode, void* stream);
 
+/* The rest of a site update (dmrg_su2::prepare_site_operator_from_{left,right},
+ * dmrg_su2_omp.cpp:319-825) as one batch over the MPS tensors uu, vv:
+ *   SU2G_ENV_OVERLAP     overlap_transformation(uu, vv, x, flag)      x: 2-leg scalar operator
+ *   SU2G_ENV_TRANSFORM   operator_transformation(uu, vv, x, flag)     x: 3-leg operator
+ *   SU2G_ENV_INITIAL     operator_initial(uu, vv, site1, flag), or with x (2-leg) as endt
+ *                        operator_initial(uu, vv, site1, x, flag)      (tensor_su2_dmrg_src.cpp:27-218)
+ *   SU2G_ENV_PAIRUP      operator_pairup(uu, vv, x, site1, flag)      (tensor_su2_dmrg_src.cpp:691-890)
+ *   SU2G_ENV_PERMUTATION permutation(uu, vv, x, site1, site2, flag)   (tensor_su2_hamiltonian.cpp:871-1108)
+ * x lives on the device; site1/site2 are the engine's site operators (sigma,
+ * qterm, ...) with their data on the HOST.  Each job adds coef times its
+ * result to outs[slot]; jobs naming one slot must produce the same structure
+ * and are summed (the reference's hh[i] = overlap + sum of pairups).  The
+ * layout of outs[slot] is what su2g_env_layout reports: the union of the
+ * blocks the slot's jobs reach, as the reference creates them.  Physical legs
+ * of uu, vv must have multiplicity 1; operator_initial needs single-element
+ * site blocks; permutation needs an operator spin of multiplicity 1.  Blocks
+ * until done. */
+#define SU2G_ENV_OVERLAP 0
+#define SU2G_ENV_TRANSFORM 1
+#define SU2G_ENV_INITIAL 2
+#define SU2G_ENV_PAIRUP 3
+#define SU2G_ENV_PERMUTATION 4
+typedef struct {
+  int kind;          /* SU2G_ENV_* */
+  int slot;          /* output index */
+  double coef;       /* scale of this job's contribution */
+  su2g_tensor x;     /* environment operator (device); desc NULL: none */
+  su2g_tensor site1; /* site operator (host data) */
+  su2g_tensor site2; /* second site operator of a permutation (host data) */
+} su2g_env_job;
+int su2g_env_layout(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int slot,
+                    int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len);
+int su2g_env_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                 double* const* outs, int mode, void* stream);
+/* Host-only dry run of su2g_env_run: builds and bounds-checks the work list
+ * for `mode` (no device work, no allocation) and reports the algorithmic
+ * flops and the device scratch it needs. */
+int su2g_env_validate(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                      int mode, double* flops, int64_t* scratch_bytes);
+
+/* Recoupling factors of the site updates, computed on first use from the
+ * Clebsch-Gordan contractions the reference tabulates (dmrg_su2.cpp:776-1019):
+ *   table 0  fac_operator_onsite_{left,rght}[a][b][c][d][e]   (e = p0 + 3 p1)
+ *   table 1  fac_operator_pairup_{left,rght}[a][b][c][d][e]   (e = p0 + 3 p1)
+ *   table 2  fac_permutation_{left,rght}[a][b][c][d][e]       (e < 18, spin-1/2 sites)
+ * side 0 = left, 1 = right; 0 where the reference leaves the entry unset. */
+int su2g_fac_table(int table, int side, int a, int b, int c, int d, int e, double* out);
+
 /* ---------------------------------------------------------- truncation -- */
 /* vec.svd(tu, p1, tv, p2, dout, wout) (tensor_su2.cpp:1619-1758 with the
  * per-sector tensor::svd of tensor.cpp:1472-1700): splits the two-leg wave

@@ -601,3 +601,232 @@ def mps_sector_matrices(S: Struct, x):
                 mat[r0: r0 + m, :] = np.asarray(x[off[bi]: off[bi] + m * b2.dim[j2]]).reshape(m, -1, order="F")
         out[c] = mat
     return out
+
+
+# --------------------------------------------------------------------------
+# Site updates: operator_initial (tensor_su2_dmrg_src.cpp:27-218),
+# operator_pairup (:691-890), permutation (tensor_su2_hamiltonian.cpp:871-1108)
+# and their recoupling tables (dmrg_su2.cpp:776-1019)
+# --------------------------------------------------------------------------
+def _cg(a, b, c):
+    return make_cgc(a, b, c).reshape((a + 1, b + 1, c + 1), order="F")
+
+
+def make_singlet(j):
+    """tensor::make_singlet (tensor.cpp:1331-1350): S[r, j - r] = (-1)^((j - m_r)/2) / sqrt(j + 1)."""
+    s = np.zeros((j + 1, j + 1))
+    for r in range(j + 1):
+        m = 2 * r - j
+        s[r, j - r] = (1 if ((j - m) // 2) % 2 == 0 else -1) / np.sqrt(j + 1.0)
+    return s
+
+
+def _ratio(t, ref):
+    """tensor::is_proportional_to (tensor.cpp:1231-1269); None if not proportional."""
+    tol = 1e-12
+    tt, rr = t.ravel(order="F"), ref.ravel(order="F")
+    if np.all(np.abs(tt) <= tol):
+        return 0.0
+    pos = int(np.argmax(np.abs(rr)))
+    rat = tt[pos] / rr[pos]
+    for a, b in zip(tt, rr):
+        if abs(a) <= tol and abs(b) <= tol:
+            continue
+        if (abs(a) <= tol) != (abs(b) <= tol) or abs(a / b - rat) > tol:
+            return None
+    return rat
+
+
+def _tri(a, b, c):
+    return abs(a - b) <= c <= a + b
+
+
+_SITE_CACHE = {}
+
+
+def fac_operator_onsite(side, j, m, l, i, q):
+    """fac_operator_onsite_{left,rght}[j][m][l][i][p0 + 3 p1] (dmrg_su2.cpp:804-833)."""
+    p0, p1 = q % 3, q // 3
+    if not (0 <= q < 9 and m in (0, 2, 4, 6) and _tri(i, p0, j) and _tri(i, p1, l) and _tri(j, m, l)
+            and j % 2 == l % 2 and _tri(p0, m, p1)):
+        return 0.0
+    key = (0, side, j, m, l, i, q)
+    if key not in _SITE_CACHE:
+        if side == 0:
+            t = np.einsum("iaj,amb,ibl->jml", _cg(i, p0, j), _cg(p0, m, p1), _cg(i, p1, l))
+        else:
+            t = np.einsum("aij,amb,bil->jml", _cg(p0, i, j), _cg(p0, m, p1), _cg(p1, i, l))
+        r = _ratio(t, _cg(j, m, l))
+        _SITE_CACHE[key] = 0.0 if r is None else float(r)
+    return _SITE_CACHE[key]
+
+
+def fac_operator_pairup(side, j, i, k, m, q):
+    """fac_operator_pairup_{left,rght}[j][i][k][m][p0 + 3 p1] (dmrg_su2.cpp:920-943)."""
+    p0, p1 = q % 3, q // 3
+    if not (0 <= q < 9 and m in (0, 2, 4, 6) and _tri(i, p0, j) and _tri(k, p1, j) and _tri(i, m, k)
+            and _tri(p0, m, p1)):
+        return 0.0
+    key = (1, side, j, i, k, m, q)
+    if key not in _SITE_CACHE:
+        w = np.sqrt(m + 1.0) * np.einsum("amb,nm->anb", _cg(p0, m, p1), make_singlet(m))
+        if side == 0:
+            t = np.einsum("iaj,imk,amb,kbl->jl", _cg(i, p0, j), _cg(i, m, k), w, _cg(k, p1, j))
+        else:
+            t = np.einsum("aij,imk,amb,bkl->jl", _cg(p0, i, j), _cg(i, m, k), w, _cg(p1, k, j))
+        r = _ratio(t, np.eye(j + 1))
+        _SITE_CACHE[key] = 0.0 if r is None else float(r)
+    return _SITE_CACHE[key]
+
+
+def fac_permutation(side, i, j, k, l, t):
+    """fac_permutation_{left,rght}[i][j][k][l][t] for spin-1/2 sites (dmrg_su2.cpp:974-1017)."""
+    P = 1
+    if not (0 <= t < 18 and _tri(i, P, j) and _tri(k, P, l)):
+        return 0.0
+    a1, a2, a3 = (t % 3) * 2, ((t // 3) % 2) * 2 + 1, ((t // 6) % 3) * 2
+    if not (_tri(a1, P, a2) and _tri(a2, P, a3)) or i % 2 != k % 2 or j % 2 != l % 2:
+        return 0.0
+    key = (2, side, i, j, k, l, t)
+    if key not in _SITE_CACHE:
+        r = None
+        if side == 0 and _tri(a1, i, k) and _tri(a3, j, l):
+            tt = np.einsum("iqj,qxy,iak,pay,kpl->jxl", _cg(i, P, j), _cg(P, a3, a2), _cg(i, a1, k), _cg(P, a1, a2),
+                           _cg(k, P, l))
+            r = _ratio(tt, _cg(j, a3, l))
+        if side == 1 and _tri(a3, i, k) and _tri(a1, j, l):
+            tt = np.einsum("qij,yqx,ixk,ypa,pkl->jal", _cg(P, i, j), _cg(a2, P, a3), _cg(i, a3, k), _cg(a2, P, a1),
+                           _cg(P, k, l))
+            r = _ratio(tt, _cg(j, a1, l))
+        _SITE_CACHE[key] = 0.0 if r is None else float(r)
+    return _SITE_CACHE[key]
+
+
+def _blocks(S: Struct, x):
+    """{block index: F-ordered array} of the present blocks."""
+    off, _ = S.offsets()
+    out = {}
+    for b in range(S.nten):
+        if S.flag[b]:
+            shp = S.block_shape(b)
+            out[b] = np.asarray(x[off[b]: off[b] + int(np.prod(shp))]).reshape(shp, order="F")
+    return out
+
+
+def site_update(kind: str, flag: int, su: Struct, xu, sv: Struct, xv, x=None, sites=()):
+    """kind 'init' (x = endt or None), 'pair' (x = op1), 'perm' (x = vec); sites
+    = [(Struct, host data), ...].  Returns (out Struct with the reference's
+    presence flags, packed data).  Physical legs of multiplicity 1."""
+    pl = 1 - flag
+    U, V = _blocks(su, xu), _blocks(sv, xv)
+    X = _blocks(*x) if x is not None else None
+    XS = x[0] if x is not None else None
+    site = [(_blocks(s, d), s) for s, d in sites]
+    if kind == "pair":
+        ybonds = [su.bonds[2], sv.bonds[2].inverted()]
+    elif kind == "init":
+        ybonds = [su.bonds[2], sites[0][0].bonds[1], sv.bonds[2].inverted()]
+    else:
+        mid = sites[1][0].bonds[1] if flag == 0 else sites[0][0].bonds[2]
+        ybonds = [su.bonds[2], mid, sv.bonds[2].inverted()]
+    Y = Struct(ybonds, 0)
+    legal = Y.legal()
+    acc = {}
+
+    def umat(blk):  # (bond multiplets, c): the physical leg has multiplicity 1
+        return blk.reshape(-1, blk.shape[2], order="F")
+
+    def add(ang, mat):
+        sec = [Y.bonds[q].angm.index(a) if a in Y.bonds[q].angm else -1 for q, a in enumerate(ang)]
+        if min(sec) < 0:
+            return False
+        b = 0
+        for q in range(len(sec) - 1, -1, -1):
+            b = b * len(Y.bonds[q].angm) + sec[q]
+        if not legal[b]:
+            return False
+        acc[b] = acc.get(b, 0) + mat
+        return True
+
+    ua = lambda k: su.block_angm(k)
+    va = lambda l: sv.block_angm(l)
+    if kind == "init":
+        (sb, ss), = site
+        for j, op in sb.items():
+            sig, s, sigp = ss.block_angm(j)
+            for k, ub in U.items():
+                if ua(k)[pl] != sig:
+                    continue
+                a, c = ua(k)[flag], ua(k)[2]
+                ends = [(None, a)] if X is None else [(e, XS.block_angm(e)[1]) for e in X if XS.block_angm(e)[0] == a]
+                for e, ap in ends:
+                    left = umat(ub) if e is None else X[e].T @ umat(ub)
+                    for l, vb in V.items():
+                        if va(l)[pl] != sigp or va(l)[flag] != ap:
+                            continue
+                        cp = va(l)[2]
+                        fac = fac_operator_onsite(flag, c, s, cp, ap, sig + sigp * 3)
+                        if abs(fac) < 1e-8:
+                            continue
+                        add((c, s, cp), (fac * op.ravel()[0] * (left.T @ umat(vb)))[:, None, :])
+    elif kind == "pair":
+        (sb, ss), = site
+        for j, xb in X.items():
+            a, s, ap = XS.block_angm(j)
+            for k, ub in U.items():
+                if ua(k)[flag] != a:
+                    continue
+                sig, c = ua(k)[pl], ua(k)[2]
+                for l, vb in V.items():
+                    if va(l)[flag] != ap:
+                        continue
+                    sigp, cp = va(l)[pl], va(l)[2]
+                    for n, ob in sb.items():
+                        if ss.block_angm(n) != (sig, s, sigp):
+                            continue
+                        fac = fac_operator_pairup(flag, c, a, ap, s, sig + sigp * 3)
+                        if abs(fac) < 1e-8:
+                            continue
+                        tot = sum(ob.ravel()[g] * (umat(ub).T @ xb[:, g, :] @ umat(vb)) for g in range(xb.shape[1]))
+                        add((c, cp), fac * tot)
+    else:
+        (b1, s1), (b2, s2) = site
+        for j, ub in U.items():
+            a, sig, c = ua(j)[flag], ua(j)[pl], ua(j)[2]
+            for k, xb in X.items():
+                if XS.block_angm(k)[0] != a:
+                    continue
+                s, ap = XS.block_angm(k)[1], XS.block_angm(k)[2]
+                for l, vb in V.items():
+                    if va(l)[flag] != ap:
+                        continue
+                    sigp, cp = va(l)[pl], va(l)[2]
+                    core = umat(ub).T @ xb[:, 0, :] @ umat(vb)
+                    for m, o1 in b1.items():
+                        a4 = s1.block_angm(m)
+                        for n, o2 in b2.items():
+                            a5 = s2.block_angm(n)
+                            if (flag == 0 and a4[2] != a5[2]) or (flag == 1 and a4[0] != a5[0]):
+                                continue
+                            if (flag == 0 and a4[1] != s) or (flag == 1 and a5[2] != s):
+                                continue
+                            if sig != a5[flag] or sigp != a4[flag]:
+                                continue
+                            so = a5[1] if flag == 0 else a4[2]
+                            # C integer division, as the reference computes the index
+                            cdiv = lambda x: int(x / 2)
+                            t = (a4[1] // 2 + cdiv(a4[2] - 1) * 3 + (a5[1] // 2) * 6 if flag == 0
+                                 else a4[2] // 2 + cdiv(a4[0] - 1) * 3 + (a5[2] // 2) * 6)
+                            fac = fac_permutation(flag, a, c, ap, cp, t)
+                            if abs(fac) < 1e-8:
+                                continue
+                            fac1 = float(np.dot(o1.ravel(order="F"), o2.ravel(order="F")))
+                            add((c, so, cp), (fac * fac1 * core)[:, None, :])
+    Y.flag = np.zeros(Y.nten, np.int32)
+    for b in acc:
+        Y.flag[b] = 1
+    off, tot = Y.offsets()
+    y = np.zeros(tot)
+    for b, mat in acc.items():
+        y[off[b]: off[b] + mat.size] = np.asarray(mat).ravel(order="F")
+    return Y, y

@@ -110,6 +110,12 @@ void ref_make_cgc(int j1, int j2, int j3, double* out) {
   for (int e = 0; e < c.get_nelement(); ++e) out[e] = c.get_telement(e);
 }
 
+void ref_make_singlet(int j, double* out) {
+  tensor c;
+  c.make_singlet(j);
+  for (int e = 0; e < c.get_nelement(); ++e) out[e] = c.get_telement(e);
+}
+
 // result = hamiltonian_vector_multiplication(vec, op1, op2)
 int ref_heff_term(const int* vd, const int* vf, const double* vx, const int* d1, const int* f1,
                   const double* x1, const int* d2, const int* f2, const double* x2) {
@@ -158,6 +164,73 @@ int ref_overlap_transformation(const int* du, const int* fu, const double* xu, c
   build_tensor(op, dop, fop, xop);
   g_result.overlap_transformation(uu, vv, op, flag);
   return g_result.get_nten();
+}
+
+// The engine's own site operators (dmrg_su2::initialize_local_operators,
+// dmrg_su2.cpp:427-525): kind 0 = sigma[idx], 1 = qterm[idx], 2 = ring[idx].
+static tensor_su2* site_operator(int kind, int idx) {
+  static bool ready = false;
+  if (!ready) {
+    g_tables->initialize_local_operators();
+    ready = true;
+  }
+  return kind == 0 ? &g_tables->sigma[idx] : kind == 1 ? &g_tables->qterm[idx] : &g_tables->ring[idx];
+}
+
+// Selects a site operator as the tensor ref_result_* read.
+void ref_select_site(int kind, int idx) { g_sel = site_operator(kind, idx); }
+
+// result = operator_initial(uu, vv, site op, flag)  (tensor_su2_dmrg_src.cpp:27-204)
+// or, with an endt desc, operator_initial(uu, vv, site op, endt, flag) (:207-218)
+int ref_operator_initial(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                         const double* xv, int skind, int sidx, const int* de, const int* fe, const double* xe,
+                         int flag) {
+  tensor_su2 uu, vv, endt;
+  build_tensor(uu, du, fu, xu);
+  build_tensor(vv, dv, fv, xv);
+  if (de) {
+    build_tensor(endt, de, fe, xe);
+    g_result.operator_initial(uu, vv, *site_operator(skind, sidx), endt, flag);
+  } else {
+    g_result.operator_initial(uu, vv, *site_operator(skind, sidx), flag);
+  }
+  g_sel = &g_result;
+  return g_result.get_nten();
+}
+
+// result = operator_pairup(uu, vv, op1, site op, flag)  (tensor_su2_dmrg_src.cpp:691-890)
+int ref_operator_pairup(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                        const double* xv, const int* d1, const int* f1, const double* x1, int skind, int sidx,
+                        int flag) {
+  tensor_su2 uu, vv, op1;
+  build_tensor(uu, du, fu, xu);
+  build_tensor(vv, dv, fv, xv);
+  build_tensor(op1, d1, f1, x1);
+  g_result.operator_pairup(uu, vv, op1, *site_operator(skind, sidx), flag);
+  g_sel = &g_result;
+  return g_result.get_nten();
+}
+
+// result = permutation(uu, vv, vec, site op 1, site op 2, flag)
+// (tensor_su2_hamiltonian.cpp:871-1108)
+int ref_permutation(const int* du, const int* fu, const double* xu, const int* dv, const int* fv,
+                    const double* xv, const int* dvec, const int* fvec, const double* xvec, int k1, int i1, int k2,
+                    int i2, int flag) {
+  tensor_su2 uu, vv, vec;
+  build_tensor(uu, du, fu, xu);
+  build_tensor(vv, dv, fv, xv);
+  build_tensor(vec, dvec, fvec, xvec);
+  g_result.permutation(uu, vv, vec, *site_operator(k1, i1), *site_operator(k2, i2), flag);
+  g_sel = &g_result;
+  return g_result.get_nten();
+}
+
+// fac_operator_onsite_{left,rght}[j][m][l][i][q], fac_operator_pairup_{left,rght}[j][i][k][m][q]
+// (q = p0 + p1 * physpn2) and fac_permutation_{left,rght}[i][j][k][l][t] (dmrg_su2.cpp:776-1019)
+double ref_fac_table(int table, int side, int a, int b, int c, int d, int e) {
+  if (table == 0) return side == 0 ? fac_operator_onsite_left[a][b][c][d][e] : fac_operator_onsite_rght[a][b][c][d][e];
+  if (table == 1) return side == 0 ? fac_operator_pairup_left[a][b][c][d][e] : fac_operator_pairup_rght[a][b][c][d][e];
+  return side == 0 ? fac_permutation_left[a][b][c][d][e] : fac_permutation_rght[a][b][c][d][e];
 }
 
 // fac_operator_transformation_{left,rght}[j][m][l][i][k][p] (dmrg_su2.cpp:857-890)

@@ -40,6 +40,17 @@ class Term(ctypes.Structure):
     _fields_ = [("op1", Tensor), ("op2", Tensor), ("coef", ctypes.c_double)]
 
 
+class EnvJob(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("slot", ctypes.c_int), ("coef", ctypes.c_double), ("x", Tensor),
+                ("site1", Tensor), ("site2", Tensor)]
+
+
+ENV_OVERLAP = 0
+ENV_TRANSFORM = 1
+ENV_INITIAL = 2
+ENV_PAIRUP = 3
+ENV_PERMUTATION = 4
+
 _lib = None
 
 _vp = ctypes.c_void_p
@@ -71,6 +82,10 @@ _PROTOS = {
     "su2g_operator_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
     "su2g_overlap_transformation_layout": (_i, [Tensor, Tensor, _i, Tensor, _vp, _i, _vp, _i, _vp]),
     "su2g_overlap_transformation": (_i, [Tensor, Tensor, _i, _i, _vp, _vp, _i, _vp]),
+    "su2g_env_layout": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
+    "su2g_env_run": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _vp, _i, _vp]),
+    "su2g_env_validate": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _i, _vp, _vp]),
+    "su2g_fac_table": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "su2g_svd": (_i, [_vp, _vp, _vp, _vp, _d, _vp, _d, _i, _vp, _i, _vp, _i, _vp, _vp, _i64, _vp, _i64, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),

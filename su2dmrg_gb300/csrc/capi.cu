@@ -210,6 +210,15 @@ int su2g_fac_hamilt_vec(int max_angm, double* out) {
   return SU2G_OK;
 }
 
+int su2g_fac_table(int table, int side, int a, int b, int c, int d, int e, double* out) {
+  if (!out || table < 0 || table > 2 || (side != 0 && side != 1))
+    return fail(SU2G_EINVAL, "fac_table: bad arguments");
+  *out = table == 0   ? su2g::fac_operator_onsite(side, a, b, c, d, e)
+         : table == 1 ? su2g::fac_operator_pairup(side, a, b, c, d, e)
+                      : su2g::fac_permutation(side, a, b, c, d, e);
+  return SU2G_OK;
+}
+
 int su2g_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p, double* out) {
   if (!out || side < 0 || side > 1 || j < 0 || m < 0 || l < 0 || i < 0 || k < 0 || p < 0)
     return fail(SU2G_EINVAL, "fac_operator_transformation: bad arguments");
@@ -256,13 +265,14 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
 }
 
 // one-shot environment update: build, run, wait, check, free
-int env_run(int kind, su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* ops, double* const* outs,
-            int mode, void* stream) {
-  if (!outs && nops > 0) return fail(SU2G_EINVAL, "env: missing output pointers");
+int env_batch_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                  double* const* outs, int mode, void* stream) {
+  if (!outs && nslots > 0) return fail(SU2G_EINVAL, "env: missing output pointers");
+  if (slices_of_mode(mode) < 0) return fail(SU2G_EINVAL, "env: unknown mode");
   su2g::HeffWork w;
   std::vector<su2g::Struct> ys;
   std::string err;
-  int rc = su2g::build_env_work(kind, uu, vv, flag, nops, ops, outs, &w, &ys, &err);
+  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs, &w, &ys, &err);
   if (rc) return fail(rc, err);
   su2g_heff_plan* p = nullptr;
   rc = plan_from_work(std::move(w), mode, &p);
@@ -272,16 +282,24 @@ int env_run(int kind, su2g_tensor uu, su2g_tensor vv, int flag, int nops, const 
   int code = 0;
   if (!rc && e == cudaSuccess) rc = su2g_heff_plan_status(p, &code);
   su2g_heff_plan_destroy(p);
-  if (e != cudaSuccess) return cuda_fail(e, "env transform");
+  if (e != cudaSuccess) return cuda_fail(e, "env update");
   return rc;
 }
 
-int env_layout(int kind, su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor op, int* out_desc, int out_desc_cap,
-               int* out_flag, int out_flag_cap, int64_t* out_len) {
+int env_batch_layout(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int slot,
+                     int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len) {
   su2g::HeffWork w;
   std::vector<su2g::Struct> ys;
   std::string err;
-  int rc = su2g::build_env_work(kind, uu, vv, flag, 1, &op, nullptr, &w, &ys, &err);
+  // the jobs of the slot asked for, as a batch of one slot
+  std::vector<su2g_env_job> mine;
+  for (int t = 0; t < njobs && jobs; ++t)
+    if (jobs[t].slot == slot) {
+      mine.push_back(jobs[t]);
+      mine.back().slot = 0;
+    }
+  if (mine.empty()) return fail(SU2G_EINVAL, "env layout: no job writes slot " + std::to_string(slot));
+  int rc = su2g::build_env_batch(uu, vv, flag, (int)mine.size(), mine.data(), 1, nullptr, &w, &ys, &err);
   if (rc) return fail(rc, err);
   const su2g::Struct& y = ys[0];
   std::vector<int> d = {y.nbond, y.locspin};
@@ -297,6 +315,32 @@ int env_layout(int kind, su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor o
   std::copy(y.flag.begin(), y.flag.end(), out_flag);
   if (out_len) *out_len = y.total;
   return SU2G_OK;
+}
+
+// overlap_transformation / operator_transformation batches: one job per operator
+std::vector<su2g_env_job> transform_jobs(int kind, int nops, const su2g_tensor* ops) {
+  std::vector<su2g_env_job> js(std::max(nops, 0));
+  for (int t = 0; t < nops; ++t) {
+    js[t] = su2g_env_job{};
+    js[t].kind = kind;
+    js[t].slot = t;
+    js[t].coef = 1.0;
+    js[t].x = ops[t];
+  }
+  return js;
+}
+
+int env_run(int kind, su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* ops, double* const* outs,
+            int mode, void* stream) {
+  if (nops < 0 || (nops > 0 && !ops)) return fail(SU2G_EINVAL, "env: bad operator list");
+  const std::vector<su2g_env_job> js = transform_jobs(kind, nops, ops);
+  return env_batch_run(uu, vv, flag, nops, js.data(), nops, outs, mode, stream);
+}
+
+int env_layout(int kind, su2g_tensor uu, su2g_tensor vv, int flag, su2g_tensor op, int* out_desc, int out_desc_cap,
+               int* out_flag, int out_flag_cap, int64_t* out_len) {
+  const std::vector<su2g_env_job> js = transform_jobs(kind, 1, &op);
+  return env_batch_layout(uu, vv, flag, 1, js.data(), 0, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len);
 }
 }  // namespace
 
@@ -333,6 +377,42 @@ int su2g_overlap_transformation_layout(su2g_tensor uu, su2g_tensor vv, int flag,
 int su2g_overlap_transformation(su2g_tensor uu, su2g_tensor vv, int flag, int nops, const su2g_tensor* hhs,
                                 double* const* outs, int mode, void* stream) {
   return env_run(0, uu, vv, flag, nops, hhs, outs, mode, stream);
+}
+
+int su2g_env_layout(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int slot,
+                    int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap, int64_t* out_len) {
+  return env_batch_layout(uu, vv, flag, njobs, jobs, slot, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len);
+}
+
+int su2g_env_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                 double* const* outs, int mode, void* stream) {
+  return env_batch_run(uu, vv, flag, njobs, jobs, nslots, outs, mode, stream);
+}
+
+int su2g_env_validate(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                      int mode, double* flops, int64_t* scratch_bytes) {
+  const int S = slices_of_mode(mode);
+  if (S < 0) return fail(SU2G_EINVAL, "env_validate: unknown mode");
+  if (nslots < 0) return fail(SU2G_EINVAL, "env_validate: bad slot count");
+  // stand-in output addresses: the work list is only built and checked
+  std::vector<double*> outs(std::max(nslots, 1));
+  for (int s = 0; s < nslots; ++s) outs[s] = reinterpret_cast<double*>((uintptr_t)(s + 1) << 40);
+  su2g::HeffWork w;
+  std::vector<su2g::Struct> ys;
+  std::string err;
+  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs.data(), &w, &ys, &err);
+  if (rc) return fail(rc, err);
+  int64_t bytes = w.scratch_len * (int64_t)sizeof(double);
+  if (S > 0) {
+    su2g::oz::OzWork oz;
+    rc = su2g::oz::build_ozaki_work(w, S, &oz, &err);
+    if (rc) return fail(rc, err);
+    bytes = (w.scratch_len + oz.partial_len) * (int64_t)sizeof(double) + oz.packed_bytes +
+            oz.exp_len * (int64_t)sizeof(int32_t);
+  }
+  if (flops) *flops = w.flops;
+  if (scratch_bytes) *scratch_bytes = bytes;
+  return SU2G_OK;
 }
 
 int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,

@@ -166,6 +166,12 @@ void split_phase2(OzWork& w) {
       ++r.nparts;
       s0 = s + 1;
     }
+    if (r.nparts < 2) {  // one segment carries nearly all the work: keep the tile whole
+      out.pop_back();
+      w.partial_len -= (int64_t)kTM * kTN;
+      out.push_back(t);
+      continue;
+    }
     w.red2.push_back(r);
   }
   w.tile2.swap(out);

@@ -299,6 +299,223 @@ double fac_operator_transformation(int side, int j, int m, int l, int i, int k, 
   return v;
 }
 
+void make_singlet(int j, double* out) {
+  const int n = j + 1;
+  for (int e = 0; e < n * n; ++e) out[e] = 0;
+  for (int r = 0; r < n; ++r) out[r + n * (n - 1 - r)] = singlet_entry(j, r);
+}
+
+namespace {
+
+// dense CG block C(j1, j2, j3) as a column-major array
+struct Cg {
+  int n0, n1, n2;
+  std::vector<double> v;
+  Cg(int a, int b, int c) : n0(a + 1), n1(b + 1), n2(c + 1), v((size_t)(a + 1) * (b + 1) * (c + 1)) {
+    make_cgc(a, b, c, v.data());
+  }
+  double operator()(int x, int y, int z) const { return v[x + n0 * (y + n1 * z)]; }
+};
+
+bool tri(int a, int b, int c) { return c >= std::abs(a - b) && c <= a + b; }
+
+template <class F>
+double cached(int table, int side, int a, int b, int c, int d, int e, F compute) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int, int, int>, double> cache;
+  const auto key = std::make_tuple(table, side, a, b, c, d, e);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const double v = compute();
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = v;
+  return v;
+}
+
+// tensor::contract_dmrg_operator_initial (tensor_dmrg_src.cpp:69-101) of the
+// table loop at dmrg_su2.cpp:804-833:
+//   side 0  T[j,m,l] = sum C(i,p0,j)[i,q0,j] C(p0,m,p1)[q0,m,q1] C(i,p1,l)[i,q1,l]
+//   side 1  T[j,m,l] = sum C(p0,i,j)[q0,i,j] C(p0,m,p1)[q0,m,q1] C(p1,i,l)[q1,i,l]
+double compute_onsite(int side, int j, int m, int l, int i, int p0, int p1) {
+  const Cg u = side ? Cg(p0, i, j) : Cg(i, p0, j);
+  const Cg v = side ? Cg(p1, i, l) : Cg(i, p1, l);
+  const Cg o(p0, m, p1), ref(j, m, l);
+  std::vector<double> t(ref.v.size(), 0.0);
+  for (int jj = 0; jj <= j; ++jj)
+    for (int mm = 0; mm <= m; ++mm)
+      for (int ll = 0; ll <= l; ++ll) {
+        double sum = 0;
+        for (int ii = 0; ii <= i; ++ii)
+          for (int q0 = 0; q0 <= p0; ++q0) {
+            const double x = side ? u(q0, ii, jj) : u(ii, q0, jj);
+            if (x == 0) continue;
+            for (int q1 = 0; q1 <= p1; ++q1) sum += x * o(q0, mm, q1) * (side ? v(q1, ii, ll) : v(ii, q1, ll));
+          }
+        t[jj + (j + 1) * (mm + (m + 1) * ll)] = sum;
+      }
+  double r = 0;
+  return proportional(t, ref.v, &r) ? r : 0.0;
+}
+
+// tensor::contract_dmrg_operator_pairup (tensor_dmrg_src.cpp:169-211) of the
+// table loop at dmrg_su2.cpp:920-943, with the site factor
+// w[q0,n,q1] = sqrt(m+1) sum_mm C(p0,m,p1)[q0,mm,q1] S_m[n,mm]:
+//   side 0  T[j,l] = sum C(i,p0,j)[i,q0,j] C(i,m,k)[i,n,k] w[q0,n,q1] C(k,p1,l)[k,q1,l]
+//   side 1  T[j,l] = sum C(p0,i,j)[q0,i,j] C(i,m,k)[i,n,k] w[q0,n,q1] C(p1,k,l)[q1,k,l]
+// compared with the identity (l = j).
+double compute_pairup(int side, int j, int i, int k, int m, int p0, int p1) {
+  const int l = j;
+  const Cg u = side ? Cg(p0, i, j) : Cg(i, p0, j);
+  const Cg v = side ? Cg(p1, k, l) : Cg(k, p1, l);
+  const Cg o(p0, m, p1), op(i, m, k);
+  std::vector<double> sg((size_t)(m + 1) * (m + 1));
+  make_singlet(m, sg.data());
+  const int n0 = p0 + 1, nm = m + 1, n1 = p1 + 1;
+  std::vector<double> w((size_t)n0 * nm * n1, 0.0);
+  for (int q0 = 0; q0 < n0; ++q0)
+    for (int n = 0; n < nm; ++n)
+      for (int q1 = 0; q1 < n1; ++q1) {
+        double s = 0;
+        for (int mm = 0; mm < nm; ++mm) s += o(q0, mm, q1) * sg[n + nm * mm];
+        w[q0 + n0 * (n + nm * q1)] = s * std::sqrt((double)(m + 1));
+      }
+  // e[jj, n, kk, q1] = sum_ii,q0 u[ii,q0,jj] C(i,m,k)[ii,n,kk] w[q0,n,q1]
+  std::vector<double> t((size_t)(j + 1) * (l + 1), 0.0), ident((size_t)(j + 1) * (j + 1), 0.0);
+  for (int e = 0; e <= j; ++e) ident[e + (j + 1) * e] = 1.0;
+  for (int jj = 0; jj <= j; ++jj)
+    for (int ll = 0; ll <= l; ++ll) {
+      double sum = 0;
+      for (int ii = 0; ii <= i; ++ii)
+        for (int q0 = 0; q0 < n0; ++q0) {
+          const double x = side ? u(q0, ii, jj) : u(ii, q0, jj);
+          if (x == 0) continue;
+          for (int n = 0; n < nm; ++n)
+            for (int kk = 0; kk <= k; ++kk) {
+              const double y = op(ii, n, kk);
+              if (y == 0) continue;
+              for (int q1 = 0; q1 < n1; ++q1)
+                sum += x * y * w[q0 + n0 * (n + nm * q1)] * (side ? v(q1, kk, ll) : v(kk, q1, ll));
+            }
+        }
+      t[jj + (j + 1) * ll] = sum;
+    }
+  double r = 0;
+  return proportional(t, ident, &r) ? r : 0.0;
+}
+
+// tensor::contract_dmrg_permutation (tensor_dmrg_src.cpp:476-533) of the
+// table loop at dmrg_su2.cpp:974-1017 (spin-1/2 sites, P = 1), with
+// (a1, a2, a3) decoded from t as a1 = 2 (t % 3), a2 = 2 ((t / 3) % 2) + 1,
+// a3 = 2 ((t / 6) % 3):
+//   side 0  T[j,x,l] = sum C(i,P,j)[i,q,j] C(P,a3,a2)[q,x,y] C(i,a1,k)[i,a,k] C(P,a1,a2)[p,a,y] C(k,P,l)[k,p,l]
+//           compared with C(j,a3,l)
+//   side 1  T[j,a,l] = sum C(P,i,j)[q,i,j] C(a2,P,a3)[y,q,x] C(i,a3,k)[i,x,k] C(a2,P,a1)[y,p,a] C(P,k,l)[p,k,l]
+//           compared with C(j,a1,l)
+double compute_permutation(int side, int i, int j, int k, int l, int t) {
+  const int P = 1;
+  const int a1 = (t % 3) * 2, a2 = ((t / 3) % 2) * 2 + 1, a3 = ((t / 6) % 3) * 2;
+  if (!(tri(a1, P, a2) && tri(a2, P, a3))) return 0.0;
+  if (i % 2 != k % 2 || j % 2 != l % 2) return 0.0;
+  const int s_in = side ? a3 : a1;   // spin carried by the operator between i and k
+  const int s_out = side ? a1 : a3;  // spin of the result between j and l
+  if (!tri(s_in, i, k) || !tri(s_out, j, l)) return 0.0;
+  const Cg u = side ? Cg(P, i, j) : Cg(i, P, j);
+  const Cg v = side ? Cg(P, k, l) : Cg(k, P, l);
+  const Cg vec(i, s_in, k), ref(j, s_out, l);
+  // site factors: side 0 fu = C(P,a3,a2)[q,x,y], fv = C(P,a1,a2)[p,a,y];
+  //               side 1 fu = C(a2,P,a3)[y,q,x], fv = C(a2,P,a1)[y,p,a]
+  const Cg fu = side ? Cg(a2, P, a3) : Cg(P, a3, a2);
+  const Cg fv = side ? Cg(a2, P, a1) : Cg(P, a1, a2);
+  const int ny = a2 + 1, nq = P + 1, nx = s_out + 1, na = s_in + 1;
+  std::vector<double> tt(ref.v.size(), 0.0);
+  if (side == 0) {
+    // vec couples to the v-side factor: b[ii,y,ll] = sum_a,kk,p vec[ii,a,kk] fv[p,a,y] v[kk,p,ll]
+    std::vector<double> b((size_t)(i + 1) * ny * (l + 1), 0.0);
+    for (int ii = 0; ii <= i; ++ii)
+      for (int y = 0; y < ny; ++y)
+        for (int ll = 0; ll <= l; ++ll) {
+          double s = 0;
+          for (int a = 0; a < na; ++a)
+            for (int kk = 0; kk <= k; ++kk) {
+              const double z = vec(ii, a, kk);
+              if (z == 0) continue;
+              for (int p = 0; p < nq; ++p) s += z * fv(p, a, y) * v(kk, p, ll);
+            }
+          b[ii + (i + 1) * (y + ny * ll)] = s;
+        }
+    // T[jj,x,ll] = sum_ii,q,y u[ii,q,jj] fu[q,x,y] b[ii,y,ll]
+    for (int jj = 0; jj <= j; ++jj)
+      for (int x = 0; x < nx; ++x)
+        for (int ll = 0; ll <= l; ++ll) {
+          double s = 0;
+          for (int ii = 0; ii <= i; ++ii)
+            for (int q = 0; q < nq; ++q) {
+              const double z = u(ii, q, jj);
+              if (z == 0) continue;
+              for (int y = 0; y < ny; ++y) s += z * fu(q, x, y) * b[ii + (i + 1) * (y + ny * ll)];
+            }
+          tt[jj + (j + 1) * (x + nx * ll)] = s;
+        }
+  } else {
+    // vec couples to the u-side factor: h[y,kk,jj] = sum_ii,q,x u[q,ii,jj] fu[y,q,x] vec[ii,x,kk]
+    std::vector<double> h((size_t)ny * (k + 1) * (j + 1), 0.0);
+    for (int y = 0; y < ny; ++y)
+      for (int kk = 0; kk <= k; ++kk)
+        for (int jj = 0; jj <= j; ++jj) {
+          double s = 0;
+          for (int ii = 0; ii <= i; ++ii)
+            for (int q = 0; q < nq; ++q) {
+              const double z = u(q, ii, jj);
+              if (z == 0) continue;
+              for (int x = 0; x < na; ++x) s += z * fu(y, q, x) * vec(ii, x, kk);
+            }
+          h[y + ny * (kk + (k + 1) * jj)] = s;
+        }
+    // T[jj,a,ll] = sum_y,kk,p h[y,kk,jj] fv[y,p,a] v[p,kk,ll]
+    for (int jj = 0; jj <= j; ++jj)
+      for (int a = 0; a < nx; ++a)
+        for (int ll = 0; ll <= l; ++ll) {
+          double s = 0;
+          for (int y = 0; y < ny; ++y)
+            for (int kk = 0; kk <= k; ++kk) {
+              const double z = h[y + ny * (kk + (k + 1) * jj)];
+              if (z == 0) continue;
+              for (int p = 0; p < nq; ++p) s += z * fv(y, p, a) * v(p, kk, ll);
+            }
+          tt[jj + (j + 1) * (a + nx * ll)] = s;
+        }
+  }
+  double r = 0;
+  return proportional(tt, ref.v, &r) ? r : 0.0;
+}
+
+bool in_table(int x) { return x >= 0 && x < kMaxAngm; }
+
+}  // namespace
+
+double fac_operator_onsite(int side, int j, int m, int l, int i, int q) {
+  const int p0 = q % 3, p1 = q / 3;
+  if (q < 0 || q >= 9 || m < 0 || m > 6 || m % 2 || !in_table(j) || !in_table(l) || !in_table(i)) return 0.0;
+  if (!tri(i, p0, j) || !tri(i, p1, l) || !tri(j, m, l) || j % 2 != l % 2 || !tri(p0, m, p1)) return 0.0;
+  return cached(0, side, j, m, l, i, q, [&] { return compute_onsite(side, j, m, l, i, p0, p1); });
+}
+
+double fac_operator_pairup(int side, int j, int i, int k, int m, int q) {
+  const int p0 = q % 3, p1 = q / 3;
+  if (q < 0 || q >= 9 || m < 0 || m > 6 || m % 2 || !in_table(j) || !in_table(i) || !in_table(k)) return 0.0;
+  if (!tri(i, p0, j) || !tri(k, p1, j) || !tri(i, m, k) || !tri(p0, m, p1)) return 0.0;
+  return cached(1, side, j, i, k, m, q, [&] { return compute_pairup(side, j, i, k, m, p0, p1); });
+}
+
+double fac_permutation(int side, int i, int j, int k, int l, int t) {
+  if (t < 0 || t >= 18 || !in_table(i) || !in_table(j) || !in_table(k) || !in_table(l)) return 0.0;
+  if (!tri(i, 1, j) || !tri(k, 1, l)) return 0.0;
+  return cached(2, side, i, j, k, l, t, [&] { return compute_permutation(side, i, j, k, l, t); });
+}
+
 void dsort2(int n, double* key, int* tag) {
   for (int gap = n / 2; gap > 0; gap /= 2)
     for (int i = gap; i < n; ++i)

@@ -86,6 +86,18 @@ const std::vector<double>& fac_hamilt_vec_table();
 // Entries are computed on first use and cached (thread safe).
 double fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p);
 
+// The site-update tables of dmrg_su2.cpp:776-1019, same conventions (first
+// use computes, later uses read a thread-safe cache; 0 where the reference
+// leaves an entry unset):
+//   fac_operator_onsite_{left,rght}[j][m][l][i][p0 + 3 p1]
+//   fac_operator_pairup_{left,rght}[j][i][k][m][p0 + 3 p1]
+//   fac_permutation_{left,rght}[i][j][k][l][t]  (spin-1/2 sites, t < 18)
+double fac_operator_onsite(int side, int j, int m, int l, int i, int q);
+double fac_operator_pairup(int side, int j, int i, int k, int m, int q);
+double fac_permutation(int side, int i, int j, int k, int l, int t);
+// tensor::make_singlet (tensor.cpp:1331-1350), (j+1) x (j+1) column-major
+void make_singlet(int j, double* out);
+
 // Ascending Shell sort of key[0..n) (gaps n/2, n/4, ..., 1, exchange inner
 // loop), carrying tag[] along: the dsort2 of sort2.f:76-108.  Equal keys end
 // up in the order this exchange sequence leaves them, which decides which of

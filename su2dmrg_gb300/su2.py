@@ -347,3 +347,105 @@ def svd(vec: Su2Struct, vec_data, tu: Su2Struct, p1: float, tv: Su2Struct, p2: f
         st = Su2Struct([s.bonds[0], s.bonds[1], newb], 0).with_legal_flags()
         out += [st, x[: st.size()]]
     return out[0], out[1], out[2], out[3], wout[: dout.value].copy()
+
+
+_ENV_KINDS = {"overlap": capi.ENV_OVERLAP, "transform": capi.ENV_TRANSFORM, "init": capi.ENV_INITIAL,
+              "pair": capi.ENV_PAIRUP, "perm": capi.ENV_PERMUTATION}
+
+
+class _EnvJobs:
+    """ctypes job array; keeps every desc/flag/data array alive for the call."""
+
+    def __init__(self, jobs):
+        self.keep = []
+        self.arr = (capi.EnvJob * max(1, len(jobs)))()
+        for i, jb in enumerate(jobs):
+            kind, slot, coef = jb["kind"], jb.get("slot", 0), jb.get("coef", 1.0)
+            e = self.arr[i]
+            e.kind = _ENV_KINDS[kind] if isinstance(kind, str) else int(kind)
+            e.slot = int(slot)
+            e.coef = float(coef)
+            if jb.get("x") is not None:
+                e.x = _tensor(jb["x"][0], jb["x"][1], self.keep)
+            for name in ("site1", "site2"):
+                if jb.get(name) is not None:
+                    s, d = jb[name]
+                    d = np.ascontiguousarray(d, np.float64)  # site operators travel as host data
+                    self.keep.append(d)
+                    setattr(e, name, _tensor(s, d, self.keep))
+        self.n = len(jobs)
+
+    @property
+    def ptr(self):
+        return ctypes.addressof(self.arr)
+
+
+def env_layout(uu, xu, vv, xv, flag: int, jobs, slot: int = 0) -> Su2Struct:
+    """Structure of output slot `slot` of an env batch (host only)."""
+    keep = []
+    J = _EnvJobs(jobs)
+    desc = np.zeros(4 + 3 * (2 + 2 * 64), np.int32)
+    flags = np.zeros(64 ** 3, np.int32)
+    n = ctypes.c_int64()
+    check(lib().su2g_env_layout(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, int(slot),
+                                ptr(desc), len(desc), ptr(flags), len(flags), ctypes.addressof(n)))
+    out = _parse_desc(desc)
+    out.flag = flags[: out.nten].copy()
+    return out
+
+
+def env_run(uu, xu, vv, xv, flag: int, jobs, outs, mode: int = capi.MODE_F64, stream=None) -> None:
+    """Runs an env batch: jobs = [{"kind": "overlap"|"transform"|"init"|"pair"|"perm",
+    "slot": s, "coef": c, "x": (Su2Struct, device data) or None,
+    "site1"/"site2": (Su2Struct, host data)}], outs[s] = device buffers laid out
+    by env_layout(..., slot=s)."""
+    keep = []
+    J = _EnvJobs(jobs)
+    optr = (ctypes.c_void_p * max(1, len(outs)))(*[ptr(o) for o in outs])
+    check(lib().su2g_env_run(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, len(outs),
+                             ctypes.addressof(optr), int(mode), stream_handle(stream)))
+
+
+def env_validate(uu, xu, vv, xv, flag: int, jobs, mode: int = capi.MODE_F64) -> dict:
+    """Host-only dry run of env_run: {"flops": ..., "scratch_bytes": ...}."""
+    keep = []
+    J = _EnvJobs(jobs)
+    nslots = 1 + max(int(j.get("slot", 0)) for j in jobs)
+    flops = ctypes.c_double()
+    scratch = ctypes.c_int64()
+    check(lib().su2g_env_validate(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, nslots,
+                                  int(mode), ctypes.addressof(flops), ctypes.addressof(scratch)))
+    return {"flops": flops.value, "scratch_bytes": scratch.value}
+
+
+def env_batch(uu, xu, vv, xv, flag: int, jobs, mode: int = capi.MODE_F64, stream=None):
+    """env_layout + allocation + env_run: returns [(Su2Struct, device tensor)] per slot."""
+    import torch
+
+    nslots = 1 + max(int(j.get("slot", 0)) for j in jobs)
+    dev = xu.device if hasattr(xu, "device") else torch.device("cuda")
+    res = []
+    for s in range(nslots):
+        st = env_layout(uu, xu, vv, xv, flag, jobs, s)
+        res.append((st, torch.empty(max(1, st.size()), dtype=torch.float64, device=dev)))
+    env_run(uu, xu, vv, xv, flag, jobs, [r[1] for r in res], mode, stream)
+    return res
+
+
+def operator_initial(uu, xu, vv, xv, op, op_host, flag: int, endt=None, mode: int = capi.MODE_F64, stream=None):
+    """tensor_su2::operator_initial(uu, vv, op[, endt], flag); op data on the host,
+    endt = (Su2Struct, device data) or None.  Returns (Su2Struct, device tensor)."""
+    return env_batch(uu, xu, vv, xv, flag, [{"kind": "init", "x": endt, "site1": (op, op_host)}], mode, stream)[0]
+
+
+def operator_pairup(uu, xu, vv, xv, op1, x1, op2, op2_host, flag: int, mode: int = capi.MODE_F64, stream=None):
+    """tensor_su2::operator_pairup(uu, vv, op1, op2, flag); op2 data on the host."""
+    return env_batch(uu, xu, vv, xv, flag, [{"kind": "pair", "x": (op1, x1), "site1": (op2, op2_host)}], mode,
+                     stream)[0]
+
+
+def permutation(uu, xu, vv, xv, vec, xvec, op1, op1_host, op2, op2_host, flag: int, mode: int = capi.MODE_F64,
+                stream=None):
+    """tensor_su2::permutation(uu, vv, vec, op1, op2, flag); op1, op2 data on the host."""
+    return env_batch(uu, xu, vv, xv, flag, [{"kind": "perm", "x": (vec, xvec), "site1": (op1, op1_host),
+                                             "site2": (op2, op2_host)}], mode, stream)[0]

@@ -183,6 +183,78 @@ def env_cases(L, rng):
     return cases
 
 
+def site_operator(L, kind, idx):
+    """The engine's own site operator (sigma / qterm) as desc, flag, data."""
+    L.ref_select_site(kind, idx)
+    d = np.zeros(256, np.int32)
+    n = L.ref_result_desc(p(d))
+    f, x, _ = read_result(L)
+    L.ref_select_result(0)
+    return d[:n].copy(), f, x
+
+
+def site_cases(L, rng):
+    """operator_initial (with and without endt), operator_pairup and
+    permutation on random MPS tensors and environment operators, with the
+    engine's site operators, in the directions the engine uses them
+    (dmrg_su2_omp.cpp:319-825)."""
+    cases = []
+    specs = [([0, 1, 2, 3, 4], [0, 1, 2, 3, 4, 5], 0.0), ([0, 2, 4, 6], [1, 3, 5, 7], 0.15),
+             ([1, 3, 5], [0, 2, 4, 6], 0.1)]
+    S, Q = 0, 1  # site operator kinds: sigma, qterm
+    for ci, (sa, sc, drop) in enumerate(specs):
+        da = [int(rng.integers(1, 7)) for _ in sa]
+        dc = [int(rng.integers(1, 7)) for _ in sc]
+        for flag in (0, 1):
+            phys = (1, [1], [1])
+            bond_a = (-1, sa, da)
+            uub = [bond_a, phys, (1, sc, dc)] if flag == 0 else [phys, bond_a, (1, sc, dc)]
+            du = desc_of(uub)
+            fu = (legal_flags(L, du) * (rng.random(nten_of(uub)) >= drop)).astype(np.int32)
+            xu = random_data(uub, fu, rng)
+            xv = random_data(uub, fu, rng)
+
+            def rand_op(bonds):
+                d = desc_of(bonds)
+                f = (legal_flags(L, d) * (rng.random(nten_of(bonds)) >= drop)).astype(np.int32)
+                return d, f, random_data(bonds, f, rng)
+
+            jobs = []
+            sig = site_operator(L, S, 0 if flag == 0 else 1)
+            jobs.append(("init", None, [sig], lambda x, s: L.ref_operator_initial(
+                p(du), p(fu), p(xu), p(du), p(fu), p(xv), S, 0 if flag == 0 else 1, None, None, None, flag)))
+            endt = rand_op([(1, sa, da), (-1, sa, da)])
+            jobs.append(("initendt", endt, [sig], lambda x, s: L.ref_operator_initial(
+                p(du), p(fu), p(xu), p(du), p(fu), p(xv), S, 0 if flag == 0 else 1, p(x[0]), p(x[1]), p(x[2]),
+                flag)))
+            op1 = rand_op([(1, sa, da), (-1, [2], [1]), (-1, sa, da)])
+            sig2 = site_operator(L, S, 1 if flag == 0 else 0)
+            jobs.append(("pair", op1, [sig2], lambda x, s: L.ref_operator_pairup(
+                p(du), p(fu), p(xu), p(du), p(fu), p(xv), p(x[0]), p(x[1]), p(x[2]), S, 1 if flag == 0 else 0,
+                flag)))
+            # the two permutations of the plaquette chains (dmrg_su2_omp.cpp:430-434, 728-732)
+            q1, q2 = (0, 1) if flag == 0 else (6, 7)
+            q3, q4 = (2, 3) if flag == 0 else (4, 5)
+            for tag, (a1, a2), spin in (("perm1", (q1, q2), (-1, [2], [1])), ("perm2", (q3, q4), (-1, [0, 2, 4], [1, 1, 1]))):
+                vec = rand_op([(1, sa, da), spin, (-1, sa, da)])
+                sites = [site_operator(L, Q, a1), site_operator(L, Q, a2)]
+                jobs.append((tag, vec, sites, lambda x, s, a1=a1, a2=a2: L.ref_permutation(
+                    p(du), p(fu), p(xu), p(du), p(fu), p(xv), p(x[0]), p(x[1]), p(x[2]), Q, a1, Q, a2, flag)))
+            for tag, x, sites, fn in jobs:
+                fn(x, sites)
+                d = np.zeros(1024, np.int32)
+                nd = L.ref_result_desc(p(d))
+                rflag, rx, _ = read_result(L)
+                c = dict(name=f"site_{tag}_{ci}_{flag}", kind=np.str_(tag), flag=np.int32(flag), du=du, fu=fu, xu=xu,
+                         xv=xv, rdesc=d[:nd].copy(), rflag=rflag, rx=rx)
+                if x is not None:
+                    c.update(dx=x[0], fx=x[1], xx=x[2])
+                for si, (sd, sf, sx) in enumerate(sites):
+                    c.update({f"ds{si}": sd, f"fs{si}": sf, f"xs{si}": sx})
+                cases.append(c)
+    return cases
+
+
 def fuse_bond(a, b):
     out = {}
     for x, dx in zip(a[1], a[2]):
@@ -243,6 +315,26 @@ def svd_cases(L, rng):
         cases.append(dict(name=f"svd_{ci}", dvec=dvec, fvec=fvec, xvec=xvec, p1=np.float64(p1), p2=np.float64(p2),
                           dcut=np.int32(dcut), wout=w[:n].copy(), kept=kept, du=du, dv=dv, **out))
     return cases
+
+
+def fac_site_tables(L):
+    """Nonzero entries of fac_operator_onsite / fac_operator_pairup /
+    fac_permutation (left and right) over the index ranges a spin-1/2 chain
+    with 2j <= 12 bonds reaches."""
+    L.ref_fac_table.restype = ctypes.c_double
+    idx, val = [], []
+    for table in range(3):
+        for side in (0, 1):
+            for a in range(13):
+                for b in (range(7) if table == 0 else range(13)):
+                    for c in range(13):
+                        for d in (range(7) if table == 1 else range(13)):
+                            for e in range(18 if table == 2 else 9):
+                                v = L.ref_fac_table(table, side, a, b, c, d, e)
+                                if v != 0.0:
+                                    idx.append((table, side, a, b, c, d, e))
+                                    val.append(v)
+    return dict(idx=np.asarray(idx, np.int8), val=np.asarray(val))
 
 
 def fac_optrans(L):
@@ -340,7 +432,8 @@ def main():
              idx=np.cumsum([0] + [len(v) for v in vals]))
     np.savez(os.path.join(HERE, "meta.npz"), **meta_cases(L, rng))
     np.savez_compressed(os.path.join(HERE, "fac_optrans.npz"), **fac_optrans(L))
-    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng):
+    np.savez_compressed(os.path.join(HERE, "fac_site.npz"), **fac_site_tables(L))
+    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng) + site_cases(L, rng):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:

@@ -187,3 +187,55 @@ def test_svd_argument_checks_without_gpu(su2lib):
     assert call(du, dv, dcut=-1) == capi.SU2G_EINVAL
     two_leg = dvec.copy()
     assert call(two_leg, dv) == capi.SU2G_EINVAL
+
+
+def test_fac_site_tables_match_reference(su2lib):
+    """The library's onsite / pairup / permutation recoupling factors against
+    the reference's own tables (1e-14 relative: the reference forms them with
+    BLAS contractions, summation order unpinned)."""
+    import ctypes
+
+    g = np.load(os.path.join(GOLDEN, "fac_site.npz"))
+    out = ctypes.c_double()
+    for r, v in zip(g["idx"], g["val"]):
+        assert su2lib.su2g_fac_table(*[int(x) for x in r], ctypes.addressof(out)) == 0
+        assert abs(out.value - v) <= 1e-14 * abs(v), (r, out.value, v)
+    assert su2lib.su2g_fac_table(3, 0, 0, 0, 0, 0, 0, ctypes.addressof(out)) != 0
+
+
+def test_site_update_layouts_match_reference(su2lib, oracle):
+    """Which blocks operator_initial / operator_pairup / permutation create
+    (host only: the layout pass reads no device data)."""
+    import glob
+
+    from su2dmrg_gb300.su2 import env_layout
+
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "site_*.npz"))):
+        g = np.load(path)
+        su = oracle.struct_from_desc(g["du"], g["fu"])
+        kind = str(g["kind"])
+        kind = "init" if kind.startswith("init") else ("pair" if kind == "pair" else "perm")
+        job = {"kind": kind}
+        if "dx" in g.files:
+            job["x"] = (oracle.struct_from_desc(g["dx"], g["fx"]), g["xx"])
+        for i in range(2):
+            if f"ds{i}" in g.files:
+                job[f"site{i + 1}"] = (oracle.struct_from_desc(g[f"ds{i}"], g[f"fs{i}"]), g[f"xs{i}"])
+        out = env_layout(su, g["xu"], su, g["xv"], int(g["flag"]), [job])
+        assert out.desc().tolist() == g["rdesc"].tolist(), path
+        assert out.flag.tolist() == g["rflag"].tolist(), path
+        assert out.size() == g["rx"].size, path
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("flag", [0, 1])
+def test_site_step_work_lists_on_cpu(su2lib, oracle, flag, mode):
+    """The batched site step of the GPU tests, built and bounds-checked on
+    the host in every mode (the split planner's tile cuts included)."""
+    from test_site_gpu import job_dicts, site_step_case
+
+    from su2dmrg_gb300.su2 import env_validate
+
+    su, xu, xv, jobs, _ = site_step_case(oracle, flag)
+    r = env_validate(su, xu, su, xv, flag, job_dicts(jobs), mode=mode)
+    assert r["flops"] > 1e7 and r["scratch_bytes"] > 0

@@ -181,3 +181,33 @@ def test_truncation_mps_matches_reference(oracle, path):
     rtu = (oracle.struct_from_desc(g["tu_desc"], g["tu_flag"]), g["tu_x"])
     rtv = (oracle.struct_from_desc(g["tv_desc"], g["tv_flag"]), g["tv_x"])
     check_mps(oracle, tu, tv, rtu, rtv)
+
+
+def test_fac_site_tables_match_reference(oracle):
+    g = np.load(os.path.join(GOLDEN, "fac_site.npz"))
+    fns = (oracle.fac_operator_onsite, oracle.fac_operator_pairup, oracle.fac_permutation)
+    for r, v in zip(g["idx"], g["val"]):
+        got = fns[int(r[0])](*[int(x) for x in r[1:]])
+        assert abs(got - v) <= 1e-14 * abs(v), (r, got, v)
+
+
+def site_case(oracle, g):
+    """(kind, flag, su, xu, xv, x, sites) of a site-update fixture."""
+    su = oracle.struct_from_desc(g["du"], g["fu"])
+    x = (oracle.struct_from_desc(g["dx"], g["fx"]), g["xx"]) if "dx" in g.files else None
+    sites = [(oracle.struct_from_desc(g[f"ds{i}"], g[f"fs{i}"]), g[f"xs{i}"]) for i in range(2) if f"ds{i}" in g.files]
+    kind = str(g["kind"])
+    kind = "init" if kind.startswith("init") else ("pair" if kind == "pair" else "perm")
+    return kind, int(g["flag"]), su, g["xu"], g["xv"], x, sites
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "site_*.npz"))))
+def test_site_update_matches_reference(oracle, path):
+    """operator_initial / operator_pairup / permutation: the same blocks, the
+    same values to 1e-13 relative (Frobenius)."""
+    g = np.load(path)
+    kind, flag, su, xu, xv, x, sites = site_case(oracle, g)
+    out, y = oracle.site_update(kind, flag, su, xu, su, xv, x, sites)
+    assert out.desc().tolist() == g["rdesc"].tolist()
+    assert out.flag.tolist() == g["rflag"].tolist()
+    assert np.linalg.norm(y - g["rx"]) <= 1e-13 * np.linalg.norm(g["rx"])
