@@ -125,6 +125,23 @@ int su2g_heff_apply(su2g_heff_plan* plan, const double* psi, double* y, void* st
 int su2g_heff_apply_profile(su2g_heff_plan* plan, const double* psi, double* y, void* stream, double* ms,
                             int* nlaunch);
 int su2g_heff_plan_destroy(su2g_heff_plan* plan);
+/* Adds the excited-state penalty of hamiltonian_vector_multiplication_idmrg
+ * (dmrg_su2.cpp:611-622): every later application also does
+ *   y -= weight * (o . psi) * o
+ * with o a device vector in psi's layout (the reference's overlapvec[j]) that
+ * must stay valid, and weight its gs_enr[j].  The dot product stays on the
+ * device (deterministic reduction). */
+int su2g_heff_plan_add_projector(su2g_heff_plan* plan, const double* o, double weight);
+
+/* Linear combination out = sum_i coef[i] * ops[i] of operators of one
+ * structure (the summed partner sum_k coup * opr[ir][k] that
+ * hamiltonian_vector_multiplication_idmrg rebuilds on every call,
+ * dmrg_su2.cpp:588-600, formed once per step instead; or hh[i] += ...).  The
+ * output holds the union of the operands' blocks (layout from
+ * su2g_operator_combine_layout: flags of that union, packed length); each
+ * element is summed in operand order.  Blocks until done. */
+int su2g_operator_combine_layout(int n, const su2g_tensor* ops, int* out_flag, int out_flag_cap, int64_t* out_len);
+int su2g_operator_combine(int n, const su2g_tensor* ops, const double* coef, double* out, void* stream);
 
 /* One-shot form of tensor_su2::hamiltonian_vector_multiplication(vec, op1, op2)
  * (tensor_su2_dmrg_src.cpp:893-1041): y = (op1, op2) vec with the recoupling

@@ -228,8 +228,38 @@ def heff_apply(prob: HeffProblem, psi: np.ndarray) -> np.ndarray:
             coef = h[2] if len(h) > 2 else 1.0
             heff_spin0(side, h[0], h[1], prob.psi, psi, prob.psi, y, coef)
     for (s1, x1, s2, x2, c) in prob.terms:
-        heff_term(prob.psi, psi, s1, x1, s2, x2, prob.psi, y, c)
+        if len(s1.bonds) == 2 and len(s2.bonds) == 2:
+            heff_scalar_pair(prob.psi, psi, s1, x1, s2, x2, prob.psi, y, c)
+        else:
+            heff_term(prob.psi, psi, s1, x1, s2, x2, prob.psi, y, c)
     return y
+
+
+def heff_scalar_pair(vs: Struct, vx, s1: Struct, x1, s2: Struct, x2, ys: Struct, y, coef=1.0) -> None:
+    """y += coef * hamiltonian_vector_multiplication(vec, op1, op2) for two
+    2-leg scalar operators: contract(contract(op1, 0, vec, 0), 1, op2, 0)
+    (tensor_su2_dmrg_src.cpp:902-906), i.e. (L^T psi) R per spin sector."""
+    V, L, R = _blocks(vs, vx), _blocks(s1, x1), _blocks(s2, x2)
+    yoff, _ = ys.offsets()
+    for k, vb in V.items():
+        ja, jb = vs.block_angm(k)
+        for j, lb in L.items():
+            if s1.block_angm(j)[0] != ja:
+                continue
+            jc = s1.block_angm(j)[1]
+            t = lb.T @ vb
+            for l, rb in R.items():
+                if s2.block_angm(l)[0] != jb:
+                    continue
+                jd = s2.block_angm(l)[1]
+                if jc != jd:
+                    continue
+                sec = (ys.bonds[0].angm.index(jc), ys.bonds[1].angm.index(jd))
+                m = sec[0] + len(ys.bonds[0].angm) * sec[1]
+                if not ys.flag[m]:
+                    raise RuntimeError("scalar pair reaches a block the output layout does not store")
+                blk = coef * (t @ rb)
+                y[yoff[m]: yoff[m] + blk.size] += blk.ravel(order="F")
 
 
 def heff_flops(prob: HeffProblem) -> float:

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 #define private public
 #include "dmrg_su2_omp.hpp"
@@ -46,6 +47,10 @@ dmrg_su2* g_tables = nullptr;  // owner of the recoupling tables
 tensor_su2 g_result;           // last result, read back by ref_result_*
 tensor_su2 g_result_b;         // second result (tv of ref_svd)
 tensor_su2* g_sel = &g_result;
+tensor_su2 g_vec1, g_vec2;             // ref_idmrg_capture: psi and H_eff psi
+std::vector<tensor_su2*> g_export;     // tensors exported by ref_idmrg_capture
+std::vector<int> g_term_i;             // its term list (see ref_idmrg_capture)
+std::vector<double> g_term_d;
 
 void desc_to_struct(const int* desc, su2struct& s) {
   int nb = desc[0], locspin = desc[1], p = 2;
@@ -231,6 +236,104 @@ double ref_fac_table(int table, int side, int a, int b, int c, int d, int e) {
   if (table == 0) return side == 0 ? fac_operator_onsite_left[a][b][c][d][e] : fac_operator_onsite_rght[a][b][c][d][e];
   if (table == 1) return side == 0 ? fac_operator_pairup_left[a][b][c][d][e] : fac_operator_pairup_rght[a][b][c][d][e];
   return side == 0 ? fac_permutation_left[a][b][c][d][e] : fac_permutation_rght[a][b][c][d][e];
+}
+
+
+// Runs do_idmrg + niter sweeps (as ref_run_dmrg), then at the last two-site
+// step (il, ir) = (ns/2 - 1, ns/2) forms the engine's own input vector
+// (prepare_input_vector, dmrg_su2_omp.cpp:229-254) and applies the engine's
+// own hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664) to it.
+// Exported tensors (ref_idmrg_select): 0 = psi, 1 = H_eff psi, 2 = hh[il],
+// 3 = hh[ir], then the operators the terms name.  The term list mirrors the
+// loops of hamiltonian_vector_multiplication_idmrg:
+//   ints  = [nterms, per term: nl, l_idx..., nr, r_idx...]
+//   dbls  = [per term: coef, l_coef..., r_coef...]
+// each term being coef * hvm(psi, sum_l l_coef L_l, sum_r r_coef R_r).
+// Returns the number of exported tensors.
+int ref_idmrg_capture(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
+                      int nthreads, double* energies) {
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  omp_set_nested(1);
+  omp_set_max_active_levels(2);
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  c->do_idmrg();
+  energies[0] = c->get_enr();
+  for (int i = 0; i < niter; ++i) {
+    c->sweep();
+    energies[i + 1] = c->get_enr();
+  }
+  const int ns = c->ns, il = ns / 2 - 1, ir = ns / 2;
+  c->prepare_input_vector(il, ir, g_vec1);
+  c->hamiltonian_vector_multiplication_idmrg(il, ir, g_vec1, g_vec2);
+  g_export = {&g_vec1, &g_vec2, &c->hh[il], &c->hh[ir]};
+  g_term_i.assign(1, 0);
+  g_term_d.clear();
+  auto idx = [&](tensor_su2* t) {
+    for (size_t q = 0; q < g_export.size(); ++q)
+      if (g_export[q] == t) return (int)q;
+    g_export.push_back(t);
+    return (int)g_export.size() - 1;
+  };
+  auto term = [&](const std::vector<std::pair<tensor_su2*, double>>& l,
+                  const std::vector<std::pair<tensor_su2*, double>>& r, double coef) {
+    g_term_i[0]++;
+    g_term_d.push_back(coef);
+    g_term_i.push_back((int)l.size());
+    for (auto& e : l) {
+      g_term_i.push_back(idx(e.first));
+      g_term_d.push_back(e.second);
+    }
+    g_term_i.push_back((int)r.size());
+    for (auto& e : r) {
+      g_term_i.push_back(idx(e.first));
+      g_term_d.push_back(e.second);
+    }
+  };
+  if (il < ns / 2) {
+    for (int j = 0; j <= il; ++j) {
+      std::vector<std::pair<tensor_su2*, double>> r;
+      for (int k = ir; k < ns; ++k)
+        if (c->hmap[j][k] > 0) r.push_back({&c->opr[ir][k], c->coup[c->hmap[j][k]]});
+      if (!r.empty()) term({{&c->opr[il][j], 1.0}}, r, 1.0);
+    }
+  } else {
+    for (int k = ir; k < ns; ++k) {
+      std::vector<std::pair<tensor_su2*, double>> l;
+      for (int j = 0; j <= il; ++j)
+        if (c->hmap[j][k] > 0) l.push_back({&c->opr[il][j], c->coup[c->hmap[j][k]]});
+      if (!l.empty()) term(l, {{&c->opr[ir][k], 1.0}}, 1.0);
+    }
+  }
+  for (int m = 0; m < 2 * ns; ++m) {
+    const int j = m % ns;
+    if (il != ir - 1 || c->plqflg[il][j] != 1 || c->plqflg[ir][j] != 1) continue;
+    const int* q = c->plqpos[j];
+    if (il >= q[0] && ir <= q[1]) term({{&c->opr[il][q[0]], 1.0}}, {{&c->plqopr[ir][m], 1.0}}, -qdelta);
+    else if (il >= q[1] && ir <= q[2]) term({{&c->plqopr[il][m], 1.0}}, {{&c->plqopr[ir][m], 1.0}}, -qdelta);
+    else if (il >= q[2] && ir <= q[3]) term({{&c->plqopr[il][m], 1.0}}, {{&c->opr[ir][q[3]], 1.0}}, -qdelta);
+  }
+  return (int)g_export.size();
+}
+
+void ref_idmrg_select(int i) { g_sel = g_export[i]; }
+int ref_idmrg_terms(int* ints, int ncap_i, double* dbls, int ncap_d) {
+  if ((int)g_term_i.size() > ncap_i || (int)g_term_d.size() > ncap_d) return -1;
+  std::copy(g_term_i.begin(), g_term_i.end(), ints);
+  std::copy(g_term_d.begin(), g_term_d.end(), dbls);
+  return (int)g_term_i.size();
 }
 
 // fac_operator_transformation_{left,rght}[j][m][l][i][k][p] (dmrg_su2.cpp:857-890)

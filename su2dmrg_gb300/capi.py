@@ -75,6 +75,9 @@ _PROTOS = {
     "su2g_heff_apply": (_i, [_vp, _vp, _vp, _vp]),
     "su2g_heff_apply_profile": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_plan_destroy": (_i, [_vp]),
+    "su2g_heff_plan_add_projector": (_i, [_vp, _vp, _d]),
+    "su2g_operator_combine_layout": (_i, [_i, _vp, _vp, _i, _vp]),
+    "su2g_operator_combine": (_i, [_i, _vp, _vp, _vp, _vp]),
     "su2g_hamiltonian_vector_multiplication": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_hamiltonian_vector_multiplication_noalloc": (_i, [_vp, _vp, _vp, Tensor, Tensor, _vp, _vp]),
     "su2g_lanczos": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),

@@ -71,6 +71,10 @@ struct su2g_heff_plan {
   double* d_krylov = nullptr;
   int krylov_vectors = 0;
   double* d_red = nullptr;
+  // excited-state projectors y -= w (o . psi) o
+  std::vector<const double*> proj_vec;
+  std::vector<double> proj_w;
+  double* d_proj = nullptr;  // dot scratch, reduction_scratch_doubles() per projector
 
   void release() {
     cudaFree(d_seg1);
@@ -94,6 +98,8 @@ struct su2g_heff_plan {
     cudaFree(d_otile2);
     cudaFree(d_red2);
     cudaFree(d_err);
+    cudaFree(d_proj);
+    d_proj = nullptr;
     d_seg1 = d_seg2 = nullptr;
     d_tile1 = d_tile2 = nullptr;
     d_scratch = d_krylov = d_red = nullptr;
@@ -460,6 +466,31 @@ int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len
   return SU2G_OK;
 }
 
+// y -= w_j (o_j . psi) o_j for every projector, the dot product kept on the device
+static cudaError_t apply_projectors(su2g_heff_plan* p, const double* psi, double* y, cudaStream_t st) {
+  const int64_t n = p->work.psi.total;
+  const int ns = su2g::reduction_scratch_doubles();
+  for (size_t j = 0; j < p->proj_vec.size(); ++j) {
+    double* scr = p->d_proj + (int64_t)j * ns;
+    cudaError_t e = su2g::launch_dot(p->proj_vec[j], psi, n, scr, st);
+    if (e == cudaSuccess) e = su2g::launch_axpy_dev(-p->proj_w[j], scr + ns - 1, p->proj_vec[j], y, n, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+int su2g_heff_plan_add_projector(su2g_heff_plan* p, const double* o, double weight) {
+  if (!p || (!o && p->work.psi.total > 0)) return fail(SU2G_EINVAL, "add_projector: bad arguments");
+  const int ns = su2g::reduction_scratch_doubles();
+  double* d = nullptr;
+  SU2G_CUDA(cudaMalloc((void**)&d, (p->proj_vec.size() + 1) * ns * sizeof(double)));
+  cudaFree(p->d_proj);
+  p->d_proj = d;
+  p->proj_vec.push_back(o);
+  p->proj_w.push_back(weight);
+  return SU2G_OK;
+}
+
 int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* stream) {
   if (!p) return fail(SU2G_EINVAL, "heff_apply: null plan");
   if (p->work.psi.total > 0 && (!psi || !y)) return fail(SU2G_EINVAL, "heff_apply: null vector");
@@ -469,6 +500,7 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
   if (p->S == 0) {
     SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st));
     SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st));
+    SU2G_CUDA(apply_projectors(p, psi, y, st));
     return SU2G_OK;
   }
   const su2g::oz::OzWork& w = p->oz;
@@ -481,6 +513,7 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
   SU2G_CUDA(su2g::oz::launch_reduce(p->d_red2, (int)w.red2.size(), b, st));
+  SU2G_CUDA(apply_projectors(p, psi, y, st));
   return SU2G_OK;
 }
 
@@ -527,6 +560,10 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
     float t = 0;
     e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
     ms[i] = t;
+  }
+  if (e == cudaSuccess && !p->proj_vec.empty()) {  // untimed: the projectors complete y
+    e = apply_projectors(p, psi, y, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   if (e != cudaSuccess) return cuda_fail(e, "apply_profile");

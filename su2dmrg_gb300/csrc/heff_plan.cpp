@@ -25,7 +25,7 @@ int parse_tensor(const su2g_tensor& t, int want_legs, Op* op, const char* what, 
     *err = std::string(what) + ": " + e;
     return SU2G_EINVAL;
   }
-  if (op->s.nbond != want_legs) {
+  if (want_legs > 0 && op->s.nbond != want_legs) {
     *err = std::string(what) + ": wrong number of legs";
     return SU2G_EINVAL;
   }
@@ -88,11 +88,31 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
   }
 
   std::vector<Op> op1(nterms), op2(nterms);
+  std::vector<char> scalar_pair(nterms, 0);
   for (int t = 0; t < nterms; ++t) {
-    int rc = parse_tensor(terms[t].op1, 3, &op1[t], "op1", err);
+    int rc = parse_tensor(terms[t].op1, 0, &op1[t], "op1", err);
     if (rc) return rc;
-    rc = parse_tensor(terms[t].op2, 3, &op2[t], "op2", err);
+    rc = parse_tensor(terms[t].op2, 0, &op2[t], "op2", err);
     if (rc) return rc;
+    if (op1[t].s.nbond == 2 && op2[t].s.nbond == 2) {
+      // two scalar operators: contract(contract(op1, 0, vec, 0), 1, op2, 0),
+      // tensor_su2_dmrg_src.cpp:902-906, i.e. L^T psi R per sector with no
+      // recoupling factor; carried as 3-leg operators whose middle leg is one
+      // spin-0 multiplet (the same packed layout)
+      scalar_pair[t] = 1;
+      for (Op* o : {&op1[t], &op2[t]}) {
+        Struct& x = o->s;
+        x.legs[2] = x.legs[1];
+        x.legs[1] = Bond();
+        x.legs[1].dir = 1;
+        x.legs[1].angm = {0};
+        x.legs[1].dim = {1};
+        x.nbond = 3;
+      }
+    } else if (op1[t].s.nbond != 3 || op2[t].s.nbond != 3) {
+      *err = "term " + std::to_string(t) + ": operators need 3 legs each (or 2 legs each)";
+      return SU2G_EINVAL;
+    }
     const Struct &s1 = op1[t].s, &s2 = op2[t].s;
     // bond checks of tensor_su2_dmrg_src.cpp:908-921 plus the output legs
     // matching psi (the result is accumulated into psi-shaped vectors)
@@ -156,7 +176,9 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
           const int jd = s2.block_angm(l, 2);
           const int oa[2] = {jc, jd};
           if (!legal_angm(oa, 2, 0)) continue;
-          if (!fac_of(ja, s, jc, &f)) {
+          if (scalar_pair[t]) {
+            f = 1.0;
+          } else if (!fac_of(ja, s, jc, &f)) {
             *err = "angular momentum beyond the recoupling table (2j >= 25)";
             return SU2G_EINVAL;
           }

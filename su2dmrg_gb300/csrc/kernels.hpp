@@ -21,6 +21,9 @@ int reduction_scratch_doubles();
 cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* scratch, cudaStream_t stream);
 cudaError_t launch_axpy(double alpha, const double* x, double* y, int64_t n, cudaStream_t stream);
 cudaError_t launch_scale(double alpha, double* x, int64_t n, cudaStream_t stream);
+// y += alpha * (*scale) * x with the scale read on the device (combine.cu)
+cudaError_t launch_axpy_dev(double alpha, const double* scale, const double* x, double* y, int64_t n,
+                            cudaStream_t stream);
 
 namespace oz {
 struct PackJob;

@@ -221,6 +221,12 @@ class HeffPlan:
                                             ctypes.addressof(n)))
         return [ms[i] for i in range(n.value)]
 
+    def add_projector(self, o, weight: float) -> None:
+        """Excited-state penalty y -= weight (o . psi) o on every later
+        application (o: device vector in psi's layout, kept alive here)."""
+        self._data_refs.append(o)
+        check(lib().su2g_heff_plan_add_projector(self._h, ptr(o), float(weight)))
+
     def lanczos(self, psi, mlanc: int = 5, stream=None):
         e = ctypes.c_double()
         nmv = ctypes.c_int()
@@ -449,3 +455,26 @@ def permutation(uu, xu, vv, xv, vec, xvec, op1, op1_host, op2, op2_host, flag: i
     """tensor_su2::permutation(uu, vv, vec, op1, op2, flag); op1, op2 data on the host."""
     return env_batch(uu, xu, vv, xv, flag, [{"kind": "perm", "x": (vec, xvec), "site1": (op1, op1_host),
                                              "site2": (op2, op2_host)}], mode, stream)[0]
+
+
+def operator_combine(ops, coefs, stream=None):
+    """sum_i coefs[i] * ops[i] for ops = [(Su2Struct, device data)] of one
+    structure: returns (Su2Struct with the union of blocks, device tensor)."""
+    import torch
+
+    keep = []
+    arr = (capi.Tensor * len(ops))()
+    for i, (s, x) in enumerate(ops):
+        arr[i] = _tensor(s, x, keep)
+    first = ops[0][0]
+    flags = np.zeros(first.nten, np.int32)
+    n = ctypes.c_int64()
+    check(lib().su2g_operator_combine_layout(len(ops), ctypes.addressof(arr), ptr(flags), len(flags),
+                                             ctypes.addressof(n)))
+    out = Su2Struct(list(first.bonds), first.locspin)
+    out.flag = flags
+    c = np.ascontiguousarray(coefs, np.float64)
+    dev = ops[0][1].device if hasattr(ops[0][1], "device") else torch.device("cuda")
+    y = torch.empty(max(1, n.value), dtype=torch.float64, device=dev)
+    check(lib().su2g_operator_combine(len(ops), ctypes.addressof(arr), ptr(c), ptr(y), stream_handle(stream)))
+    return out, y

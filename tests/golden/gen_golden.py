@@ -414,6 +414,49 @@ def dmrg_runs(L):
     return out
 
 
+def idmrg_cases(L):
+    """The engine's own H_eff (hamiltonian_vector_multiplication_idmrg) at the
+    last two-site step of short runs: real environments, the input vector the
+    engine builds, its output, and the term decomposition it sums."""
+    runs = [
+        # (lx, ly, sec, D, niter, jcoup, qcoup, boundary)
+        (6, 4, 0, 40, 1, 2.0, 0.0, 2),  # J1-J2
+        (6, 4, 0, 30, 1, 1.0, 1.0, 2),  # J-Q: plaquette terms
+    ]
+    L.ref_idmrg_capture.restype = ctypes.c_int
+    cases = []
+    cwd = os.getcwd()
+    for ci, (lx, ly, sec, d, niter, jc, qc, bd) in enumerate(runs):
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            e = np.zeros(64)
+            nt = L.ref_idmrg_capture(lx, ly, sec, d, niter, ctypes.c_double(jc), ctypes.c_double(qc), bd, 1, p(e))
+            os.chdir(cwd)
+        c = dict(name=f"idmrg_{ci}", lx=lx, ly=ly, d=d, jcoup=jc, qcoup=qc, ntensors=np.int32(nt))
+        for i in range(nt):
+            L.ref_idmrg_select(i)
+            dd = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(dd))
+            if dd[0] == 0:
+                f, x = np.zeros(0, np.int32), np.zeros(0)
+            else:
+                f, x, _ = read_result(L)
+            c.update({f"t{i}_desc": dd[:nd].copy(), f"t{i}_flag": f, f"t{i}_x": x})
+        ti, td = np.zeros(100000, np.int32), np.zeros(100000)
+        n = L.ref_idmrg_terms(p(ti), len(ti), p(td), len(td))
+        ti = ti[:n].copy()
+        nd, q = 0, 1
+        for _ in range(ti[0]):  # per term: coef, then one coefficient per named operator
+            nl = ti[q]
+            nr = ti[q + 1 + nl]
+            nd += 1 + nl + nr
+            q += 2 + nl + nr
+        c.update(term_i=ti, term_d=td[:nd].copy())
+        L.ref_select_result(0)
+        cases.append(c)
+    return cases
+
+
 def main():
     L = ctypes.CDLL(REFLIB)
     L.ref_setup(1, 25)
@@ -436,6 +479,10 @@ def main():
     for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng) + site_cases(L, rng):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
+    if "--no-idmrg" not in sys.argv:
+        for c in idmrg_cases(L):
+            name = c.pop("name")
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)

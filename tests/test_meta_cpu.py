@@ -239,3 +239,24 @@ def test_site_step_work_lists_on_cpu(su2lib, oracle, flag, mode):
     su, xu, xv, jobs, _ = site_step_case(oracle, flag)
     r = env_validate(su, xu, su, xv, flag, job_dicts(jobs), mode=mode)
     assert r["flops"] > 1e7 and r["scratch_bytes"] > 0
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_idmrg_work_lists_on_cpu(su2lib, oracle, mode):
+    """The engine's own two-site H_eff terms (plaquette and scalar pairs
+    included) build and bounds-check as one plan in every mode (host only)."""
+    import glob
+
+    import idmrg_case
+
+    from su2dmrg_gb300.su2 import HeffPlan
+
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "idmrg_*.npz"))):
+        g = np.load(path)
+        vs, vx, yref, _, T, terms, hl, hr = idmrg_case.load(oracle, g)
+        tl = []
+        for coef, left, right in terms:
+            L, R = idmrg_case.combine_host(oracle, T, left), idmrg_case.combine_host(oracle, T, right)
+            tl.append((L[0], L[1], R[0], R[1], coef))
+        r = HeffPlan.validate(vs, tl, (hl[0], hl[1], 1.0), (hr[0], hr[1], 1.0), mode=mode)
+        assert r["flops"] > 0

@@ -211,3 +211,24 @@ def test_site_update_matches_reference(oracle, path):
     assert out.desc().tolist() == g["rdesc"].tolist()
     assert out.flag.tolist() == g["rflag"].tolist()
     assert np.linalg.norm(y - g["rx"]) <= 1e-13 * np.linalg.norm(g["rx"])
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "idmrg_*.npz"))))
+def test_idmrg_heff_matches_reference(oracle, path):
+    """The engine's own H_eff psi at a real two-site step (J1-J2 and J-Q
+    runs) rebuilt from its term decomposition: the combined partner
+    operators, the spin-0 block Hamiltonians and the plaquette terms; 1e-12
+    relative."""
+    import idmrg_case
+
+    g = np.load(path)
+    vs, vx, yref, outside, T, terms, hl, hr = idmrg_case.load(oracle, g)
+    assert outside <= 1e-24 * np.dot(yref, yref)
+    tl = []
+    for coef, left, right in terms:
+        L = idmrg_case.combine_host(oracle, T, left)
+        R = idmrg_case.combine_host(oracle, T, right)
+        tl.append((L[0], L[1], R[0], R[1], coef))
+    prob = oracle.HeffProblem(vs, tl, hl, hr)
+    y = oracle.heff_apply(prob, vx)
+    assert np.linalg.norm(y - yref) <= 1e-12 * np.linalg.norm(yref)
