@@ -14,20 +14,21 @@
 //     C_ij = 2^(e_i + f_j - 7(S+1)) sum_{g=2}^{S+1} 2^(7(S+1-g)) G_g(i,j),
 //     G_g  = sum_{p+q=g} sum_k dA_p(i,k) dB_q(j,k)
 // (pairs with p+q > S+1 are dropped: they weigh below 2^-7(S+2)).  With
-// |d| <= 65 and at most S pairs per group, a group summed over 128 values of
-// k stays below 2^22 in magnitude, so the FP32 tensor-core accumulation of
-// one group over one K chunk of 128 is exact, and the chunk sums are combined
-// in 64-bit integers, C = 2^(e_i + f_j - 48) sum_g 2^(48 - 7g) G_g.  The only
+// |d| <= 65 and at most S <= 7 pairs per group, a group summed over 512
+// values of k stays below 7 * 512 * 65^2 = 15,142,400 < 2^24 in magnitude
+// (every partial sum too), so the FP32 tensor-core accumulation of one group
+// over one K chunk of 512 is exact, and the chunk sums are combined in 64-bit
+// integers, C = 2^(e_i + f_j - 48) sum_g 2^(48 - 7g) G_g.  The only
 // rounding is in forming N (2^-48 relative to the row maximum for S = 7), in
 // the dropped pairs, and in aligning products of different exponents to the
 // tile's common fixed point (2^-46 of the tile's largest product).
 //
 // Packed operand layout (bytes), built by the pack kernel:
-//   [row tile rt][k tile kt][slice p][rows RT x 32 k, tcgen05 canonical
+//   [row tile rt][k tile kt][slice p][rows RT x 16 k, tcgen05 canonical
 //   no-swizzle K-major layout: 8x8 core matrices, core (r/8, k/8) at
-//   (r/8)*512 + (k/8)*128, element (r%8, k%8) at (r%8)*16 + (k%8)*2]
+//   (r/8)*256 + (k/8)*128, element (r%8, k%8) at (r%8)*16 + (k%8)*2]
 // with RT = 128 for the A (M) role and 64 for the B (N) role, rows padded to
-// RT and K padded to 32 with zeros; one int32 exponent per (padded) row.
+// RT and K padded to 16 with zeros; one int32 exponent per (padded) row.
 #pragma once
 #include <cstdint>
 
@@ -45,8 +46,10 @@ namespace oz {
 constexpr int kBits = 7;            // bits per digit
 constexpr int kTM = 128;            // tile rows (MMA M)
 constexpr int kTN = 64;             // tile columns (MMA N)
-constexpr int kKS = 32;             // K per shared-memory stage
-constexpr int kChunkStages = 4;     // exact FP32 group sums over 4 stages = 128 k
+constexpr int kKS = 16;             // K per packed unit and shared-memory stage (one MMA deep)
+constexpr int kSBO = 8 * kKS * 2;   // bytes between 8-row core groups of a unit
+constexpr int kChunkStages = 32;    // exact FP32 group sums over 32 stages = 512 k
+constexpr int kStages = 4;          // shared-memory ring depth of the tile GEMM
 constexpr int kExpZero = -(1 << 20);  // exponent of an all-zero row
 constexpr int kFixedTop = 48;         // fixed point: group g weighs 2^(kFixedTop - 7g)
 constexpr int kMaxSegs = 1024;        // segments feeding one output tile

@@ -1,14 +1,15 @@
 // Split-precision tile GEMM on the tcgen05 tensor cores (representation in
-// ozaki.hpp).  One CTA computes one 128 x 64 output tile:
+// ozaki.hpp).  One CTA computes one 128 x 64 output tile with three roles:
 //
-//   warp 4, lane 0  producer + MMA issuer: bulk-copies the packed A (S slices
-//                   x 128 x 32) and B (S slices x 64 x 32) units of each K
-//                   stage into a two-stage shared-memory ring
-//                   (cp.async.bulk + mbarrier transaction counts) and issues
-//                   the BF16 MMAs: for every digit pair (p, q) with
-//                   p + q <= S + 1, D[g = p+q] += A_p B_q^T, one FP32 TMEM
-//                   accumulator of 128 lanes x 64 columns per group g;
-//   warps 0-3       epilogue: after every K chunk of 128 (or segment end) they
+//   warp 4, lane 0  producer: bulk-copies the packed A (S slices x 128 x 16)
+//                   and B (S slices x 64 x 16) units of each K stage into a
+//                   kStages-deep shared-memory ring (cp.async.bulk + mbarrier
+//                   transaction counts), running ahead of the MMAs;
+//   warp 5, lane 0  MMA issuer: for every digit pair (p, q) with
+//                   p + q <= S + 1, D[g = p+q] += A_p B_q^T (one BF16 MMA of
+//                   K = 16), one FP32 TMEM accumulator of 128 lanes x 64
+//                   columns per group g; frees each stage with a commit;
+//   warps 0-3       epilogue: after every K chunk of 512 (or segment end) they
 //                   read the S group sums from TMEM (tcgen05.ld, lane = tile
 //                   row), convert them exactly to integers, weight them by
 //                   2^(48 - 7g) and add them, aligned to the tile's largest
@@ -16,7 +17,8 @@
 //                   at the end each thread scales its row to FP64 and stores it.
 //
 // Every mbarrier wait is bounded; on time-out the CTA records an error code
-// in *err, drains its outstanding tensor-core work (bounded) and returns.
+// in *err, drains its outstanding tensor-core work and bulk copies (bounded)
+// and returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -28,7 +30,7 @@ namespace su2g {
 namespace oz {
 namespace {
 
-constexpr int kThreads = 160;  // 4 epilogue warps + 1 producer/MMA warp
+constexpr int kThreads = 192;  // 4 epilogue warps + producer warp + MMA warp
 constexpr long long kWaitIters = 1ll << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -65,12 +67,12 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
 }
 
 // K-major, no swizzle: core matrices 8 rows x 16 B; LBO = 128 B between
-// K-adjacent cores, SBO = 512 B between 8-row groups (32 k per stage).
+// K-adjacent cores, SBO = kSBO = 256 B between 8-row groups (16 k per stage).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFF);
   d |= (uint64_t)(128 >> 4) << 16;
-  d |= (uint64_t)(512 >> 4) << 32;
+  d |= (uint64_t)(kSBO >> 4) << 32;
   d |= (uint64_t)1 << 46;
   return d;
 }
@@ -100,11 +102,8 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// exact FP32 integer (|v| < 2^22) to int32: 1.5*2^23 + v keeps v in the low mantissa bits
-__device__ __forceinline__ int f32_to_int_exact(uint32_t bits) {
-  const float v = __uint_as_float(bits) + 12582912.0f;
-  return (int)(__float_as_uint(v) - 0x4B400000u);
-}
+// an FP32 group sum is an integer below 2^24 in magnitude: the conversion is exact
+__device__ __forceinline__ int f32_to_int_exact(uint32_t bits) { return __float2int_rn(__uint_as_float(bits)); }
 
 __device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
 
@@ -113,7 +112,7 @@ struct Smem {
   static constexpr int kA = a_unit_bytes(S);
   static constexpr int kB = b_unit_bytes(S);
   static constexpr int kStage = kA + kB;
-  static constexpr int kBytes = 2 * kStage + 1024;  // + alignment slack
+  static constexpr int kBytes = kStages * kStage + 1024;  // + alignment slack
 };
 
 template <int S>
@@ -122,18 +121,18 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
                                                           const int* __restrict__ exps, Bases bases, int* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_accf, bar_acce, bar_drain;
+  __shared__ __align__(8) uint64_t bar_full[kStages], bar_empty[kStages], bar_accf, bar_acce, bar_drain;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int fmax_sh[kTN];
   __shared__ int cshift_sh[kMaxSegs];
   __shared__ int shb_sh[4][kTN];  // per epilogue warp: column shifts of the current segment
-  __shared__ int abort_sh;
+  __shared__ int abort_sh, loaded_sh, consumed_sh;
 
   const OzTile t = tiles[blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kStages; ++i) {
       mbar_init(smem_u32(&bar_full[i]), 1);
       mbar_init(smem_u32(&bar_empty[i]), 1);
     }
@@ -141,6 +140,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     mbar_init(smem_u32(&bar_acce), 4);
     mbar_init(smem_u32(&bar_drain), 1);
     abort_sh = 0;
+    loaded_sh = 0;
+    consumed_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -152,69 +153,71 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
+  volatile int* abort_v = &abort_sh;
+  auto stage_a = [&](int st) { return smem_u32(smem) + (uint32_t)(st * Smem<S>::kStage); };
 
   if (warp == 4) {
-    // ===================== producer + MMA issuer =====================
+    // ============================ producer ============================
     if (lane == 0) {
-      int total = 0;
-      for (int s = 0; s < t.nseg; ++s) total += segs[t.seg0 + s].nks;
-      const uint32_t sA[2] = {smem_u32(smem), smem_u32(smem + Smem<S>::kStage)};
-      const uint32_t sB[2] = {sA[0] + Smem<S>::kA, sA[1] + Smem<S>::kA};
-      // load cursor
-      int ls = 0, lks = 0;
-      auto load = [&](int it) -> bool {
-        const int st = it & 1;
-        if (it >= 2 && !mbar_wait(smem_u32(&bar_empty[st]), ((it >> 1) - 1) & 1)) return false;
-        const OzSeg g = segs[t.seg0 + ls];
-        const uint8_t* a = packed + g.a_unit + (int64_t)lks * a_unit_bytes(S) * 1;
-        const uint8_t* b = packed + g.b_unit + (int64_t)lks * b_unit_bytes(S) * 1;
-        mbar_expect_tx(smem_u32(&bar_full[st]), Smem<S>::kStage);
-        bulk_g2s(sA[st], a, Smem<S>::kA, smem_u32(&bar_full[st]));
-        bulk_g2s(sB[st], b, Smem<S>::kB, smem_u32(&bar_full[st]));
-        if (++lks == g.nks) {
-          lks = 0;
-          ++ls;
-        }
-        return true;
-      };
-      bool ok = true;
       int loaded = 0;
-      if (total > 0) ok = load(loaded++);
-      if (ok && total > 1) ok = load(loaded++);
+      bool ok = true;
+      for (int s = 0; s < t.nseg && ok; ++s) {
+        const OzSeg g = segs[t.seg0 + s];
+        for (int ks = 0; ks < g.nks; ++ks, ++loaded) {
+          const int st = loaded % kStages;
+          if (*abort_v) { ok = false; break; }
+          // the stage's previous contents must have been consumed by their MMAs
+          if (loaded >= kStages && !mbar_wait(smem_u32(&bar_empty[st]), ((loaded / kStages) - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t a_dst = stage_a(st), b_dst = a_dst + Smem<S>::kA;
+          mbar_expect_tx(smem_u32(&bar_full[st]), Smem<S>::kStage);
+          bulk_g2s(a_dst, packed + g.a_unit + (int64_t)ks * a_unit_bytes(S), Smem<S>::kA, smem_u32(&bar_full[st]));
+          bulk_g2s(b_dst, packed + g.b_unit + (int64_t)ks * b_unit_bytes(S), Smem<S>::kB, smem_u32(&bar_full[st]));
+        }
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        atomicExch(&abort_sh, 1);
+      }
+      loaded_sh = loaded;
+    }
+  } else if (warp == 5) {
+    // =========================== MMA issuer ===========================
+    if (lane == 0) {
       int it = 0, chunk = 0;
+      bool ok = true;
       for (int s = 0; s < t.nseg && ok; ++s) {
         const int nks = segs[t.seg0 + s].nks;
-        for (int ks = 0; ks < nks && ok; ++ks, ++it) {
-          const int st = it & 1;
-          if (!mbar_wait(smem_u32(&bar_full[st]), (it >> 1) & 1)) { ok = false; break; }
+        for (int ks = 0; ks < nks; ++ks, ++it) {
+          const int st = it % kStages;
+          if (*abort_v || !mbar_wait(smem_u32(&bar_full[st]), (it / kStages) & 1)) { ok = false; break; }
           const bool first = (ks % kChunkStages) == 0;
-          if (first && chunk > 0 && !mbar_wait(smem_u32(&bar_acce), (chunk - 1) & 1)) { ok = false; break; }
+          // a new chunk overwrites the group sums: the epilogue must have read them
+          if (first && chunk > 0 && !mbar_wait(smem_u32(&bar_acce), (chunk - 1) & 1)) {
+            ++it;  // this stage was waited for: it counts as consumed
+            ok = false;
+            break;
+          }
           tc_fence_after();
+          const uint32_t sa = stage_a(st), sb = sa + Smem<S>::kA;
 #pragma unroll
-          for (int kk = 0; kk < kKS / 16; ++kk) {
+          for (int g = 2; g <= S + 1; ++g) {
+            const int p0 = (g - S > 1) ? g - S : 1;
+            const int p1 = (g - 1 < S) ? g - 1 : S;
 #pragma unroll
-            for (int g = 2; g <= S + 1; ++g) {
-              const int p0 = (g - S > 1) ? g - S : 1;
-              const int p1 = (g - 1 < S) ? g - 1 : S;
-#pragma unroll
-              for (int p = p0; p <= p1; ++p) {
-                const int q = g - p;
-                const uint64_t ad = smem_desc(sA[st] + (p - 1) * (kTM * kKS * 2) + kk * 256);
-                const uint64_t bd = smem_desc(sB[st] + (q - 1) * (kTN * kKS * 2) + kk * 256);
-                const uint32_t acc = (first && kk == 0 && p == p0) ? 0u : 1u;
-                mma(tmem + (uint32_t)((g - 2) * kTN), ad, bd, acc);
-              }
+            for (int p = p0; p <= p1; ++p) {
+              const int q = g - p;
+              const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
+              const uint64_t bd = smem_desc(sb + (q - 1) * (kTN * kKS * 2));
+              mma(tmem + (uint32_t)((g - 2) * kTN), ad, bd, (first && p == p0) ? 0u : 1u);
             }
           }
           mma_commit(smem_u32(&bar_empty[st]));
-          const bool last = ((ks % kChunkStages) == kChunkStages - 1) || ks == nks - 1;
-          if (last) {
+          if ((ks % kChunkStages) == kChunkStages - 1 || ks == nks - 1) {
             mma_commit(smem_u32(&bar_accf));
             ++chunk;
-          }
-          if (loaded < total) {
-            if (!load(loaded)) { ok = false; break; }
-            ++loaded;
           }
         }
       }
@@ -222,14 +225,10 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
         atomicExch(err, 1);
         atomicExch(&abort_sh, 1);
       }
+      consumed_sh = it;
       // drain: every MMA issued so far has completed once this commit arrives
       mma_commit(smem_u32(&bar_drain));
       if (!mbar_wait(smem_u32(&bar_drain), 0)) atomicExch(err, 2);
-      // bulk copies still in flight (possible only after an abort) must land
-      // before the CTA exits: wait for every issued load's transaction count
-      if (!ok) {
-        for (int i = it; i < loaded; ++i) mbar_wait(smem_u32(&bar_full[i & 1]), (i >> 1) & 1);
-      }
     }
   } else {
     // ============================ epilogue ============================
@@ -338,6 +337,11 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     }
   }
   tc_fence_before();
+  __syncthreads();
+  // bulk copies still in flight (possible only after an abort) must land
+  // before the CTA exits: at most one unconsumed load per stage
+  if (warp == 4 && lane == 0 && abort_sh)
+    for (int i = consumed_sh; i < loaded_sh; ++i) mbar_wait(smem_u32(&bar_full[i % kStages]), (i / kStages) & 1);
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
 #pragma unroll
     for (int i = 0; i < 8; ++i) d[0][i] = __int2bfloat16_rn((int)N[i]);
     const int kt = kc / (kKS / 8), kin = kc % (kKS / 8);
-    uint8_t* base = dst + (int64_t)kt * unit_bytes + (r / 8) * 512 + kin * 128 + (r % 8) * 16;
+    uint8_t* base = dst + (int64_t)kt * unit_bytes + (r / 8) * kSBO + kin * 128 + (r % 8) * 16;
 #pragma unroll
     for (int q = 0; q < S; ++q) {
       uint4 v;
