@@ -70,6 +70,7 @@ struct PackJob {
   double alpha;
   int64_t dst;       // byte offset in the packed buffer (multiple of 1024)
   int64_t exp;       // int32 offset in the exponent buffer (nrt*rt entries)
+  int64_t texp;      // int32 offset of the per-row-tile maxima (nrt entries)
 };
 
 // One K segment of an output tile: both operands already packed.
@@ -78,6 +79,7 @@ struct OzSeg {
   int64_t b_unit;    // byte offset of this tile's B row tile, k tile 0
   int64_t a_exp;     // exponent index of the tile's first A row
   int64_t b_exp;     // exponent index of the tile's first B row
+  int64_t a_tmax;    // exponent index of the largest exponent of the A row tile
   int nks;           // k tiles (stages) of this segment
   int pad;
 };

@@ -1,20 +1,23 @@
 // Split-precision tile GEMM on the tcgen05 tensor cores (representation in
 // ozaki.hpp).  One CTA computes one 128 x 64 output tile with three roles:
 //
-//   warp 4, lane 0  producer: bulk-copies the packed A (S slices x 128 x 16)
+//   warp 16, lane 0 producer: bulk-copies the packed A (S slices x 128 x 16)
 //                   and B (S slices x 64 x 16) units of each K stage into a
 //                   kStages-deep shared-memory ring (cp.async.bulk + mbarrier
 //                   transaction counts), running ahead of the MMAs;
-//   warp 5, lane 0  MMA issuer: for every digit pair (p, q) with
+//   warp 17, lane 0 MMA issuer: for every digit pair (p, q) with
 //                   p + q <= S + 1, D[g = p+q] += A_p B_q^T (one BF16 MMA of
 //                   K = 16), one FP32 TMEM accumulator of 128 lanes x 64
 //                   columns per group g; frees each stage with a commit;
-//   warps 0-3       epilogue: after every K chunk of 512 (or segment end) they
-//                   read the S group sums from TMEM (tcgen05.ld, lane = tile
-//                   row), convert them exactly to integers, weight them by
-//                   2^(48 - 7g) and add them, aligned to the tile's largest
-//                   product exponents, into 64 int64 accumulators per thread;
-//                   at the end each thread scales its row to FP64 and stores it.
+//   warps 0-15      epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile
+//                   rows) and columns 16 (w / 4) .. + 15; after every K chunk
+//                   of 512 (or segment end) it reads the S group sums of its
+//                   16 columns (tcgen05.ld), converts them exactly to
+//                   integers, weights them by 2^(48 - 7g) and adds them,
+//                   aligned to the tile's largest product exponents, into 16
+//                   int64 accumulators per thread; at the end each thread
+//                   scales its 16 values to FP64 and stores them.  Four warps
+//                   per SM sub-partition hide the latency of these chains.
 //
 // Every mbarrier wait is bounded; on time-out the CTA records an error code
 // in *err, drains its outstanding tensor-core work and bulk copies (bounded)
@@ -30,7 +33,11 @@ namespace su2g {
 namespace oz {
 namespace {
 
-constexpr int kThreads = 192;  // 4 epilogue warps + producer warp + MMA warp
+constexpr int kEpiWarps = 16;                      // drain warps: 4 lane quarters x 4 column slices
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kCols = kTN / (kEpiWarps / 4);         // output columns per drain thread
+constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
+constexpr int kThreads = kEpiThreads + 64;           // + producer warp + MMA warp
 constexpr long long kWaitIters = 1ll << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -92,9 +99,9 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
 }
 
@@ -106,6 +113,29 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ int f32_to_int_exact(uint32_t bits) { return __float2int_rn(__uint_as_float(bits)); }
 
 __device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
+
+// v * 2^e rounded to nearest (ties to even), built with integer operations
+// only (GB300 has little FP64 throughput); equal to ldexp((double)v, e)
+// whenever the result is a normal number, and computed that way otherwise.
+__device__ __forceinline__ double scaled_to_double(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sign = (unsigned long long)v & 0x8000000000000000ull;
+  unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll(u);
+  u <<= lz;                        // leading one at bit 63
+  unsigned long long m = u >> 11;  // 53 significant bits, leading one at bit 52
+  const unsigned rem = (unsigned)(u & 0x7FFull);
+  if (rem > 0x400u || (rem == 0x400u && (m & 1ull))) ++m;
+  int ex = 63 - lz + e;  // value = m 2^-52 2^ex
+  if (m >> 53) {
+    m >>= 1;
+    ++ex;
+  }
+  const int biased = ex + 1023;
+  if (biased <= 0 || biased >= 2047) return ldexp((double)v, e);  // subnormal or overflowing: FP64 path
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)biased << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
 
 template <int S>
 struct Smem {
@@ -125,7 +155,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __shared__ uint32_t tmem_base_sh;
   __shared__ int fmax_sh[kTN];
   __shared__ int cshift_sh[kMaxSegs];
-  __shared__ int shb_sh[4][kTN];  // per epilogue warp: column shifts of the current segment
+  __shared__ int shb_sh[kEpiWarps][kCols];  // per drain warp: column shifts of the current segment
   __shared__ int abort_sh, loaded_sh, consumed_sh;
 
   const OzTile t = tiles[blockIdx.x];
@@ -137,7 +167,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       mbar_init(smem_u32(&bar_empty[i]), 1);
     }
     mbar_init(smem_u32(&bar_accf), 1);
-    mbar_init(smem_u32(&bar_acce), 4);
+    mbar_init(smem_u32(&bar_acce), kEpiWarps);
     mbar_init(smem_u32(&bar_drain), 1);
     abort_sh = 0;
     loaded_sh = 0;
@@ -156,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   volatile int* abort_v = &abort_sh;
   auto stage_a = [&](int st) { return smem_u32(smem) + (uint32_t)(st * Smem<S>::kStage); };
 
-  if (warp == 4) {
+  if (warp == kProducerWarp) {
     // ============================ producer ============================
     if (lane == 0) {
       int loaded = 0;
@@ -183,7 +213,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       }
       loaded_sh = loaded;
     }
-  } else if (warp == 5) {
+  } else if (warp == kMmaWarp) {
     // =========================== MMA issuer ===========================
     if (lane == 0) {
       int it = 0, chunk = 0;
@@ -232,8 +262,9 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     }
   } else {
     // ============================ epilogue ============================
-    const int row = warp * 32 + lane;  // TMEM lane == tile row
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const int lq = warp & 3, col0 = (warp >> 2) * kCols;
+    const int row = lq * 32 + lane;  // TMEM lane == tile row
+    const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
     // Exponent bookkeeping.  Segment s contributes 2^(eA_s(i) + eB_s(j)) times
     // its digit sums; moving c_s = max_i eA_s(i) (over the tile rows) from the
     // A side to the B side leaves every product unchanged but makes the
@@ -241,23 +272,21 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     // fmax(j) = max_s (eB_s(j) + c_s) track the largest actual product scale
     // (otherwise an O(1) x O(1e-3) segment and an O(1e-3) x O(1) segment would
     // set a reference 2^10 above both).
-    for (int s = tid; s < t.nseg; s += 128) cshift_sh[s] = kExpZero;
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    for (int s = 0; s < t.nseg; ++s) {
-      const int m = __reduce_max_sync(0xffffffffu, exps[segs[t.seg0 + s].a_exp + row]);
-      if (lane == 0) atomicMax(&cshift_sh[s], m);
+    // c_s = the A row tile's largest exponent, recorded by the pack kernel
+    for (int s = tid; s < t.nseg; s += kEpiThreads) {
+      const int m = exps[segs[t.seg0 + s].a_tmax];
+      cshift_sh[s] = (m == kExpZero) ? 0 : m;
     }
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    for (int s = tid; s < t.nseg; s += 128)
-      if (cshift_sh[s] == kExpZero) cshift_sh[s] = 0;
-    asm volatile("bar.sync 1, 128;" ::: "memory");
+    asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
     int emax = kExpZero;
+#pragma unroll 8
     for (int s = 0; s < t.nseg; ++s) {
       const int e = exps[segs[t.seg0 + s].a_exp + row];
       if (e != kExpZero) emax = max(emax, e - cshift_sh[s]);
     }
     if (tid < kTN) {
       int f = kExpZero;
+#pragma unroll 8
       for (int s = 0; s < t.nseg; ++s) {
         const int fb = exps[segs[t.seg0 + s].b_exp + tid];
         if (fb != kExpZero) f = max(f, fb + cshift_sh[s]);
@@ -266,10 +295,10 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     }
     // the only block-wide barrier of the epilogue, taken before any bounded
     // wait so that a time-out can never leave a warp stranded in it
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    long long acc[kTN];
+    asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+    long long acc[kCols];
 #pragma unroll
-    for (int j = 0; j < kTN; ++j) acc[j] = 0;
+    for (int j = 0; j < kCols; ++j) acc[j] = 0;
     int chunk = 0;
     bool ok = true;
     for (int s = 0; s < t.nseg && ok; ++s) {
@@ -279,11 +308,9 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       const int sha = (ea == kExpZero) ? 1000 : emax - (ea - cs);
       // column shifts of this segment, staged per warp (no block barrier)
       __syncwarp();
-#pragma unroll
-      for (int h = 0; h < kTN / 32; ++h) {
-        const int j = lane + 32 * h;
-        const int fj = exps[g.b_exp + j];
-        shb_sh[warp][j] = (fj == kExpZero) ? 1000 : fmax_sh[j] - (fj + cs);
+      if (lane < kCols) {
+        const int fj = exps[g.b_exp + col0 + lane];
+        shb_sh[warp][lane] = (fj == kExpZero) ? 1000 : fmax_sh[col0 + lane] - (fj + cs);
       }
       __syncwarp();
       const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
@@ -291,19 +318,20 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
         if (!mbar_wait(smem_u32(&bar_accf), chunk & 1)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
-        for (int cb = 0; cb < kTN / 8; ++cb) {
-          // all S group sums of 8 columns in flight, one wait
-          uint32_t r[S][8];
+        for (int cb = 0; cb < kCols / 4; ++cb) {
+          // all S group sums of 4 columns in flight, one wait
+          uint32_t r[S][4];
 #pragma unroll
-          for (int gg = 0; gg < S; ++gg) tmem_ld8(tmem + lane_base + (uint32_t)(gg * kTN + cb * 8), r[gg]);
+          for (int gg = 0; gg < S; ++gg)
+            tmem_ld4(tmem + lane_base + (uint32_t)(gg * kTN + col0 + cb * 4), r[gg]);
           tmem_wait_ld();
 #pragma unroll
-          for (int x = 0; x < 8; ++x) {
+          for (int x = 0; x < 4; ++x) {
             long long v = 0;
 #pragma unroll
             for (int gg = 0; gg < S; ++gg)
               v += shl_signed((long long)f32_to_int_exact(r[gg][x]), kFixedTop - kBits * (gg + 2));
-            const int j = cb * 8 + x;
+            const int j = cb * 4 + x;
             const int sh = sha + shb_sh[warp][j];
             if (sh == 0) {
               acc[j] += v;
@@ -321,16 +349,17 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       atomicExch(err, 3);
       atomicExch(&abort_sh, 1);
     }
-    // ---- store the row: C = acc * 2^(emax + fmax - kFixedTop) ----
+    // ---- store: C = acc * 2^(emax + fmax - kFixedTop) ----
     double* C = resolve(bases, t.c_buf, t.c);
     if (row < t.mlen) {
       const int ebase = emax - kFixedTop;
 #pragma unroll
-      for (int j = 0; j < kTN; ++j) {
+      for (int jj = 0; jj < kCols; ++jj) {
+        const int j = col0 + jj;
         if (j < t.nlen) {
           const int f = fmax_sh[j];
           double out = 0.0;
-          if (ok && emax != kExpZero && f != kExpZero && acc[j] != 0) out = ldexp((double)acc[j], ebase + f);
+          if (ok && emax != kExpZero && f != kExpZero) out = scaled_to_double(acc[jj], ebase + f);
           C[(int64_t)(t.m0 + row) + (int64_t)(t.n0 + j) * t.ldc] = out;
         }
       }
@@ -340,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __syncthreads();
   // bulk copies still in flight (possible only after an abort) must land
   // before the CTA exits: at most one unconsumed load per stage
-  if (warp == 4 && lane == 0 && abort_sh)
+  if (warp == kProducerWarp && lane == 0 && abort_sh)
     for (int i = consumed_sh; i < loaded_sh; ++i) mbar_wait(smem_u32(&bar_full[i % kStages]), (i / kStages) & 1);
   __syncthreads();
   if (warp == 0) {

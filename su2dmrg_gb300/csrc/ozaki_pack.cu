@@ -21,6 +21,7 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
                                                             uint8_t* __restrict__ packed, int* __restrict__ exps) {
   __shared__ double rmax[kPackThreads];
   __shared__ int rexp[kTM];
+  __shared__ int tmax;
   const int2 u = units[blockIdx.x];
   const PackJob job = jobs[u.x];
   const int rt = u.y;
@@ -38,6 +39,7 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
     for (int k = part; k < job.K; k += parts) m = fmax(m, fabs(p[(int64_t)k * job.ld_k]));
   }
   rmax[tid] = m;
+  if (tid == 0) tmax = kExpZero;
   __syncthreads();
   if (tid < RT) {
     double mm = rmax[tid];
@@ -47,8 +49,11 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __res
     const int e = (mm > 0.0) ? ilogb(mm) + 2 : kExpZero;
     rexp[tid] = e;
     exps[job.exp + r0 + tid] = e;
+    if (e != kExpZero) atomicMax(&tmax, e);
   }
   __syncthreads();
+  // the row tile's largest exponent (kExpZero for an all-zero tile)
+  if (tid == 0) exps[job.texp + rt] = tmax;
 
   // ---- digits: one (row, 8 consecutive k) core row per thread iteration ----
   const int ncore_k = job.nkt * (kKS / 8);

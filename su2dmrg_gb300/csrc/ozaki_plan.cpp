@@ -41,8 +41,9 @@ struct Builder {
     j.alpha = alpha;
     j.dst = w->packed_bytes;
     j.exp = w->exp_len;
+    j.texp = w->exp_len + (int64_t)j.nrt * rt;
     w->packed_bytes += (int64_t)j.nrt * j.nkt * S * rt * kKS * 2;
-    w->exp_len += (int64_t)j.nrt * rt;
+    w->exp_len += (int64_t)j.nrt * rt + j.nrt;
     lists[cls]->push_back(j);
     const int id = (int)lists[cls]->size() - 1;
     index[key] = {cls, id};
@@ -109,6 +110,7 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
           z.b_unit = b.dst + (int64_t)(n0 / kTN) * b.nkt * b_unit_bytes(S);
           z.a_exp = a.exp + m0;
           z.b_exp = b.exp + n0;
+          z.a_tmax = a.texp + m0 / kTM;
           z.nks = a.nkt;
           z.pad = 0;
           t.work += z.nks;
@@ -211,7 +213,8 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
     for (const PackJob& j : w.jobs[c]) {
       const int64_t bytes = (int64_t)j.nrt * j.nkt * w.S * j.rt * kKS * 2;
       if (j.dst < 0 || j.dst % 1024 || j.dst + bytes > w.packed_bytes || j.exp < 0 ||
-          j.exp + (int64_t)j.nrt * j.rt > w.exp_len || j.R <= 0 || j.K <= 0 || (j.rt != kTM && j.rt != kTN)) {
+          j.exp + (int64_t)j.nrt * j.rt > w.exp_len || j.texp < 0 || j.texp + j.nrt > w.exp_len || j.R <= 0 ||
+          j.K <= 0 || (j.rt != kTM && j.rt != kTN)) {
         *err = "split mode: pack job out of bounds";
         return SU2G_EINVAL;
       }
@@ -226,7 +229,8 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
         if (z.nks <= 0 || z.a_unit < 0 || z.b_unit < 0 ||
             z.a_unit + (int64_t)z.nks * a_unit_bytes(w.S) > w.packed_bytes ||
             z.b_unit + (int64_t)z.nks * b_unit_bytes(w.S) > w.packed_bytes || z.a_unit % 1024 || z.b_unit % 1024 ||
-            z.a_exp < 0 || z.a_exp + kTM > w.exp_len || z.b_exp < 0 || z.b_exp + kTN > w.exp_len)
+            z.a_exp < 0 || z.a_exp + kTM > w.exp_len || z.b_exp < 0 || z.b_exp + kTN > w.exp_len ||
+            z.a_tmax < 0 || z.a_tmax >= w.exp_len)
           return false;
       }
     }
