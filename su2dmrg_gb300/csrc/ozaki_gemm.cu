@@ -84,15 +84,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// kind::f16, BF16 x BF16 -> FP32, both K-major, M = 128, N = 64
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) |
-                            ((uint32_t)(kTM >> 4) << 24);
+// kind::f16, BF16 x BF16 -> FP32, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+}
 
-__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
           d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+      "l"(a), "l"(b), "r"(id), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -232,16 +233,21 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
           }
           tc_fence_after();
           const uint32_t sa = stage_a(st), sb = sa + Smem<S>::kA;
+          // The B digit slices lie back to back (64 rows each, same core-row
+          // stride) and so do the group accumulators in TMEM (64 columns
+          // each): the pairs (p, q) .. (p, q+n-1) are one MMA of N = 64 n that
+          // reads B_q .. B_{q+n-1} as one 64n-row operand and adds into groups
+          // p+q .. p+q+n-1.  Up to n = 4 (N = 256): 10 MMAs per stage for S = 7
+          // instead of 28, and A is read once per MMA.  p = 1 touches every
+          // group first, so only its MMAs start a chunk's sums from zero.
 #pragma unroll
-          for (int g = 2; g <= S + 1; ++g) {
-            const int p0 = (g - S > 1) ? g - S : 1;
-            const int p1 = (g - 1 < S) ? g - 1 : S;
+          for (int p = 1; p <= S; ++p) {
+            const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
 #pragma unroll
-            for (int p = p0; p <= p1; ++p) {
-              const int q = g - p;
-              const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
+            for (int q = 1; q <= S + 1 - p; q += 4) {
+              const int n = (S + 2 - p - q) < 4 ? (S + 2 - p - q) : 4;
               const uint64_t bd = smem_desc(sb + (q - 1) * (kTN * kKS * 2));
-              mma(tmem + (uint32_t)((g - 2) * kTN), ad, bd, (first && p == p0) ? 0u : 1u);
+              mma(tmem + (uint32_t)((p + q - 2) * kTN), ad, bd, idesc(kTN * n), (first && p == 1) ? 0u : 1u);
             }
           }
           mma_commit(smem_u32(&bar_empty[st]));
