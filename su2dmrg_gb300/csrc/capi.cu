@@ -151,7 +151,7 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   if (e == cudaSuccess) e = upload(w.red2, &p->d_red2);
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
-  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), b, p->d_packed, p->d_exps,
+  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0], b, p->d_packed, p->d_exps,
                             nullptr);
   if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
   return e;
@@ -504,11 +504,14 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
     return SU2G_OK;
   }
   const su2g::oz::OzWork& w = p->oz;
-  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), b, p->d_packed,
+  // the row maxima that phase 1 leaves for the intermediates' pack start at zero
+  if (w.rowmax_len > 0)
+    SU2G_CUDA(cudaMemsetAsync(p->d_exps + w.rowmax_base, 0, w.rowmax_len * sizeof(int), st));
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], b, p->d_packed,
                                   p->d_exps, st));
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile1, (int)w.tile1.size(), p->d_oseg1, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
-  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), b, p->d_packed,
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], b, p->d_packed,
                                   p->d_exps, st));
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
@@ -535,8 +538,10 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
     n = 2;
   } else {
     const su2g::oz::OzWork& w = p->oz;
+    if (e == cudaSuccess && w.rowmax_len > 0)
+      e = cudaMemsetAsync(p->d_exps + w.rowmax_base, 0, w.rowmax_len * sizeof(int), st);
     if (e == cudaSuccess)
-      e = su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), b, p->d_packed, p->d_exps,
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], b, p->d_packed, p->d_exps,
                                 st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
     if (e == cudaSuccess)
@@ -544,7 +549,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
                                       p->d_err, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
     if (e == cudaSuccess)
-      e = su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), b, p->d_packed, p->d_exps,
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], b, p->d_packed, p->d_exps,
                                 st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
     if (e == cudaSuccess)

@@ -54,6 +54,7 @@ constexpr int kExpZero = -(1 << 20);  // exponent of an all-zero row
 constexpr int kFixedTop = 48;         // fixed point: group g weighs 2^(kFixedTop - 7g)
 constexpr int kMaxSegs = 1024;        // segments feeding one output tile
 constexpr int kTargetCtas = 4 * 152;  // phase-2 tiles are split until about this many CTAs run
+constexpr int kRowmaxBias = 2048;     // row-maximum slots hold ilogb + 2048; 0 = no nonzero element
 
 SU2G_HD constexpr int pairs(int S) { return S * (S + 1) / 2; }
 SU2G_HD constexpr int a_unit_bytes(int S) { return S * kTM * kKS * 2; }
@@ -71,6 +72,8 @@ struct PackJob {
   int64_t dst;       // byte offset in the packed buffer (multiple of 1024)
   int64_t exp;       // int32 offset in the exponent buffer (nrt*rt entries)
   int64_t texp;      // int32 offset of the per-row-tile maxima (nrt entries)
+  int64_t rowmax;    // int32 offset of per-row ilogb maxima left by the GEMM that
+                     // produced the operand (R entries, kRowmaxBias-coded), -1: none
 };
 
 // One K segment of an output tile: both operands already packed.
@@ -101,6 +104,10 @@ struct OzTile {
   int m0, n0, mlen, nlen;
   int seg0, nseg;
   int64_t work;      // sum of nks over the segments (scheduling weight)
+  int64_t rowmax;    // phase-1 tiles: row-maximum slots of the operand this block
+                     // becomes in phase 2 (its row i = columns i*rms .. of the block), -1: none
+  int rms;
+  int pad2;
 };
 
 }  // namespace oz

@@ -115,6 +115,14 @@ __device__ __forceinline__ int f32_to_int_exact(uint32_t bits) { return __float2
 
 __device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
 
+// ilogb of a nonzero finite double given as its bit pattern (sign ignored)
+__device__ __forceinline__ int ilogb_bits(unsigned long long b) {
+  b &= 0x7FFFFFFFFFFFFFFFull;
+  const int E = (int)(b >> 52);
+  if (E > 0) return E - 1023;
+  return (63 - __clzll(b & 0xFFFFFFFFFFFFFull)) - 1074;
+}
+
 // v * 2^e rounded to nearest (ties to even), built with integer operations
 // only (GB300 has little FP64 throughput); equal to ldexp((double)v, e)
 // whenever the result is a normal number, and computed that way otherwise.
@@ -146,15 +154,19 @@ struct Smem {
   static constexpr int kBytes = kStages * kStage + 1024;  // + alignment slack
 };
 
+// rowmax_out is the exponent buffer again: the kernel writes only its
+// row-maximum region (OzWork::rowmax_base ..), which it never reads through exps.
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restrict__ tiles, const OzSeg* __restrict__ segs,
                                                           const uint8_t* __restrict__ packed,
-                                                          const int* __restrict__ exps, Bases bases, int* err) {
+                                                          const int* __restrict__ exps, int* rowmax_out,
+                                                          Bases bases, int* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t bar_full[kStages], bar_empty[kStages], bar_accf, bar_acce, bar_drain;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int fmax_sh[kTN];
+  __shared__ int colmax_sh[kTN];  // row maxima handed to the next pack: per tile column
   __shared__ int cshift_sh[kMaxSegs];
   __shared__ int shb_sh[kEpiWarps][kCols];  // per drain warp: column shifts of the current segment
   __shared__ int abort_sh, loaded_sh, consumed_sh;
@@ -283,6 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       const int m = exps[segs[t.seg0 + s].a_tmax];
       cshift_sh[s] = (m == kExpZero) ? 0 : m;
     }
+    if (tid < kTN) colmax_sh[tid] = 0;
     asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
     int emax = kExpZero;
 #pragma unroll 8
@@ -356,19 +369,42 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
       atomicExch(&abort_sh, 1);
     }
     // ---- store: C = acc * 2^(emax + fmax - kFixedTop) ----
+    // A phase-1 block that becomes a phase-2 operand also leaves, per operand
+    // row (block columns i*rms ..), the largest ilogb of its values, so that
+    // the pack needs no pass of its own over the block.
     double* C = resolve(bases, t.c_buf, t.c);
+    const int ebase = emax - kFixedTop;
+    int lg[kCols];  // kRowmaxBias-coded ilogb |value|, 0 for a zero or absent value
     if (row < t.mlen) {
-      const int ebase = emax - kFixedTop;
 #pragma unroll
       for (int jj = 0; jj < kCols; ++jj) {
         const int j = col0 + jj;
+        lg[jj] = 0;
         if (j < t.nlen) {
           const int f = fmax_sh[j];
           double out = 0.0;
           if (ok && emax != kExpZero && f != kExpZero) out = scaled_to_double(acc[jj], ebase + f);
           C[(int64_t)(t.m0 + row) + (int64_t)(t.n0 + j) * t.ldc] = out;
+          const unsigned long long ob = (unsigned long long)__double_as_longlong(out);
+          if (t.rowmax >= 0 && (ob & 0x7FFFFFFFFFFFFFFFull)) lg[jj] = ilogb_bits(ob) + kRowmaxBias;
         }
       }
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < kCols; ++jj) lg[jj] = 0;
+    }
+    if (t.rowmax >= 0) {  // uniform over the CTA
+      // column maxima: over the warp's rows (lane jj keeps column jj), over the
+      // four lane quarters (shared memory), then one global atomic per column
+      int mine = 0;
+#pragma unroll
+      for (int jj = 0; jj < kCols; ++jj) {
+        const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)lg[jj]);
+        if (lane == jj) mine = m;
+      }
+      if (lane < kCols && mine > 0) atomicMax(&colmax_sh[col0 + lane], mine);
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      if (tid < t.nlen && colmax_sh[tid] > 0) atomicMax(&rowmax_out[t.rowmax + (t.n0 + tid) / t.rms], colmax_sh[tid]);
     }
   }
   tc_fence_before();
@@ -396,18 +432,18 @@ int gemm_smem_bytes(int S) {
 }
 
 cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
-                              const int* exps, const Bases& bases, int* err, cudaStream_t stream) {
+                              int* exps, const Bases& bases, int* err, cudaStream_t stream) {
   if (ntiles <= 0) return cudaSuccess;
   const int smem = gemm_smem_bytes(S);
   cudaError_t e = cudaSuccess;
   switch (S) {
     case 6:
       e = cudaFuncSetAttribute(ozaki_gemm<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess) ozaki_gemm<6><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, bases, err);
+      if (e == cudaSuccess) ozaki_gemm<6><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, exps, bases, err);
       break;
     case 7:
       e = cudaFuncSetAttribute(ozaki_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess) ozaki_gemm<7><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, bases, err);
+      if (e == cudaSuccess) ozaki_gemm<7><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, exps, bases, err);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -1,6 +1,7 @@
-// Splitting of FP64 operands into BF16 digit slices (layout in ozaki.hpp).
-// One CTA per (job, row tile): a row-max pass sets the per-row exponent, then
-// every thread turns 8 consecutive k of one row into S 16-byte core rows.
+// Splitting of FP64 operands into BF16 digit slices (layout in ozaki.hpp), in
+// two launches: the row exponents (one warp per row), then the digits (one CTA
+// per row tile and 64 k).  The scaling and rounding to integers use integer
+// operations only (FP64 throughput is scarce on GB300).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -15,85 +16,181 @@ namespace {
 
 constexpr int kPackThreads = 256;
 
+// round(x 2^s) to the nearest integer, ties to even (llrint of the exactly
+// scaled value), with integer operations only.  The caller guarantees
+// |x| 2^s < 2^48.
+__device__ __forceinline__ long long scale_round(double x, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  int E = (int)((b >> 52) & 0x7FF);
+  unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+  if (E == 0) {
+    if (M == 0) return 0;
+    E = 1;  // subnormal
+  } else {
+    M |= 1ull << 52;
+  }
+  const int sh = E - 1075 + s;  // |x| 2^s = M 2^sh
+  unsigned long long q;
+  if (sh >= 0) {
+    q = M << sh;
+  } else {
+    const int r = -sh;
+    if (r > 63) return 0;  // below 2^53 2^-64 < 1/2
+    q = M >> r;
+    const unsigned long long rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+  }
+  return (b >> 63) ? -(long long)q : (long long)q;
+}
+
+// ilogb of a positive finite double given as its bit pattern
+__device__ __forceinline__ int ilogb_bits(unsigned long long b) {
+  const int E = (int)(b >> 52);
+  if (E > 0) return E - 1023;
+  return (63 - __clzll(b & 0xFFFFFFFFFFFFFull)) - 1074;
+}
+
+// sum_{q<S} 64 * 128^q: added to N it turns balanced digits into plain ones
 template <int S>
-__global__ void __launch_bounds__(kPackThreads) pack_kernel(const PackJob* __restrict__ jobs,
-                                                            const int2* __restrict__ units, Bases bases,
-                                                            uint8_t* __restrict__ packed, int* __restrict__ exps) {
-  __shared__ double rmax[kPackThreads];
+constexpr long long kDigitBias = S == 0 ? 0 : 64ll + 128ll * kDigitBias<(S > 0 ? S - 1 : 0)>;
+template <>
+constexpr long long kDigitBias<0> = 0;
+
+constexpr int kRowsPerUnit = kTM;  // row slots per unit in the row kernel (RT <= 128)
+constexpr int kDigitKt = 4;        // k tiles (16 k each) per CTA of the digit kernel
+
+// Row exponents: one warp per row of every unit, lanes along k (coalesced):
+// |alpha X| 2^-e < 1/2 with e = ilogb(max |alpha X|) + 2, kExpZero for a zero row.
+__global__ void __launch_bounds__(kPackThreads) pack_rows_kernel(const PackJob* __restrict__ jobs,
+                                                                 const int2* __restrict__ units, int nunits,
+                                                                 Bases bases, int* __restrict__ exps) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * (kPackThreads / 32) + warp;
+  const int ui = (int)(gw / kRowsPerUnit), row = (int)(gw % kRowsPerUnit);
+  if (ui >= nunits) return;
+  const int2 u = units[ui];
+  const PackJob& job = jobs[u.x];
+  if (row >= job.rt || job.rowmax >= 0) return;  // row maxima left by the producing GEMM
+  const int r = u.y * job.rt + row;
+  unsigned long long m = 0;  // max |x| as a bit pattern (order-preserving for |x|)
+  if (r < job.R) {
+    const double* p = resolve(bases, job.src_buf, job.src) + (int64_t)r * job.ld_r;
+    int k = lane;
+    for (; k + 96 < job.K; k += 128) {  // four loads in flight
+      const unsigned long long a = __double_as_longlong(p[(int64_t)k * job.ld_k]);
+      const unsigned long long b = __double_as_longlong(p[(int64_t)(k + 32) * job.ld_k]);
+      const unsigned long long c = __double_as_longlong(p[(int64_t)(k + 64) * job.ld_k]);
+      const unsigned long long d = __double_as_longlong(p[(int64_t)(k + 96) * job.ld_k]);
+      m = max(m, max(max(a & 0x7FFFFFFFFFFFFFFFull, b & 0x7FFFFFFFFFFFFFFFull),
+                     max(c & 0x7FFFFFFFFFFFFFFFull, d & 0x7FFFFFFFFFFFFFFFull)));
+    }
+    for (; k < job.K; k += 32)
+      m = max(m, (unsigned long long)__double_as_longlong(p[(int64_t)k * job.ld_k]) & 0x7FFFFFFFFFFFFFFFull);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) {
+    int e = kExpZero;
+    if (m != 0) {
+      if (job.alpha == 1.0 || job.alpha == -1.0) {
+        e = ilogb_bits(m) + 2;
+      } else {
+        const double mm = __longlong_as_double((long long)m) * fabs(job.alpha);
+        if (mm > 0.0) e = ilogb(mm) + 2;
+      }
+    }
+    exps[job.exp + r] = e;
+  }
+}
+
+// Digits: one CTA per (unit, kDigitKt k tiles); a warp converts 8 rows x 32 k,
+// a thread one row x 8 k into S 16-byte core rows, so that a warp's stores
+// fill whole 256-byte core-row groups.  The k-chunk-0 CTA also records the
+// row tile's largest exponent.
+template <int S>
+__global__ void __launch_bounds__(kPackThreads) pack_digits_kernel(const PackJob* __restrict__ jobs,
+                                                                   const int2* __restrict__ units, Bases bases,
+                                                                   uint8_t* __restrict__ packed,
+                                                                   int* __restrict__ exps) {
   __shared__ int rexp[kTM];
   __shared__ int tmax;
   const int2 u = units[blockIdx.x];
   const PackJob job = jobs[u.x];
-  const int rt = u.y;
-  const int RT = job.rt;
-  const int r0 = rt * RT;
+  const int kt0 = blockIdx.y * kDigitKt;
+  if (kt0 >= job.nkt) return;
+  const int rt = u.y, RT = job.rt, r0 = rt * RT;
   const double* src = resolve(bases, job.src_buf, job.src);
-  const int tid = threadIdx.x;
-
-  // ---- per-row max |X| ----
-  const int parts = kPackThreads / RT;  // 2 (RT=128) or 4 (RT=64)
-  const int row = tid % RT, part = tid / RT;
-  double m = 0.0;
-  if (r0 + row < job.R) {
-    const double* p = src + (int64_t)(r0 + row) * job.ld_r;
-    for (int k = part; k < job.K; k += parts) m = fmax(m, fabs(p[(int64_t)k * job.ld_k]));
-  }
-  rmax[tid] = m;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) tmax = kExpZero;
   __syncthreads();
   if (tid < RT) {
-    double mm = rmax[tid];
-    for (int q = 1; q < parts; ++q) mm = fmax(mm, rmax[tid + q * RT]);
-    mm *= fabs(job.alpha);
-    // |X| 2^-e < 1/2 : e = ilogb(max) + 2
-    const int e = (mm > 0.0) ? ilogb(mm) + 2 : kExpZero;
+    int e;
+    if (job.rowmax >= 0) {  // |X| 2^-e < 1/2 from the producer's ilogb maxima
+      const int v = (r0 + tid < job.R) ? exps[job.rowmax + r0 + tid] : 0;
+      e = v > 0 ? v - kRowmaxBias + 2 : kExpZero;
+      if (blockIdx.y == 0) exps[job.exp + r0 + tid] = e;
+    } else {
+      e = exps[job.exp + r0 + tid];
+    }
     rexp[tid] = e;
-    exps[job.exp + r0 + tid] = e;
-    if (e != kExpZero) atomicMax(&tmax, e);
+    if (blockIdx.y == 0 && e != kExpZero) atomicMax(&tmax, e);
   }
   __syncthreads();
-  // the row tile's largest exponent (kExpZero for an all-zero tile)
-  if (tid == 0) exps[job.texp + rt] = tmax;
+  if (blockIdx.y == 0 && tid == 0) exps[job.texp + rt] = tmax;
 
-  // ---- digits: one (row, 8 consecutive k) core row per thread iteration ----
-  const int ncore_k = job.nkt * (kKS / 8);
+  const bool unit_alpha = job.alpha == 1.0 || job.alpha == -1.0;
+  const int ncore_k = min(job.nkt - kt0, kDigitKt) * (kKS / 8);
+  const int nkq = (ncore_k + 3) / 4;  // groups of 4 core columns (32 k)
   const int64_t unit_bytes = (int64_t)S * RT * kKS * 2;
   const int64_t slice_bytes = (int64_t)RT * kKS * 2;
-  uint8_t* dst = packed + job.dst + (int64_t)rt * job.nkt * unit_bytes;
-  for (int w = tid; w < RT * ncore_k; w += kPackThreads) {
-    const int r = w % RT, kc = w / RT;
+  uint8_t* dst = packed + job.dst + ((int64_t)rt * job.nkt + kt0) * unit_bytes;
+  const int r8 = lane & 7, kq = lane >> 3;
+  for (int item = warp; item < (RT / 8) * nkq; item += kPackThreads / 32) {
+    const int rg = item % (RT / 8), kc = (item / (RT / 8)) * 4 + kq;
+    if (kc >= ncore_k) continue;
+    const int r = rg * 8 + r8;
     const int e = rexp[r];
     const bool live = (r0 + r < job.R) && e != kExpZero;
+    const int s = kBits * S - e;
     long long N[8];
-    const double scale = live ? ldexp(job.alpha, kBits * S - e) : 0.0;
     const double* p = src + (int64_t)(r0 + r) * job.ld_r;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int k = kc * 8 + i;
-      N[i] = (live && k < job.K) ? llrint(p[(int64_t)k * job.ld_k] * scale) : 0ll;
-    }
-    // balanced base-128 digits, least significant first
-    __nv_bfloat16 d[S][8];
-#pragma unroll
-    for (int q = S - 1; q >= 1; --q) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const long long lo = ((N[i] + 64) & 127) - 64;
-        N[i] = (N[i] - lo) >> kBits;
-        d[q][i] = __int2bfloat16_rn((int)lo);
+      const int k = (kt0 * (kKS / 8) + kc) * 8 + i;
+      N[i] = 0;
+      if (live && k < job.K) {
+        const double x = p[(int64_t)k * job.ld_k];
+        N[i] = scale_round(unit_alpha ? (job.alpha < 0 ? -x : x) : x * job.alpha, s);
       }
     }
+    // Balanced base-128 digits d_q in [-64, 63] (the leading one takes the
+    // rest): N + sum_q 64 * 128^q has the plain base-128 digits d_q + 64, so
+    // each digit is one shift and mask.  A digit's BF16 bits are the upper
+    // half of the exact FP32 value (2^23 + u) - (2^23 + 64).
 #pragma unroll
-    for (int i = 0; i < 8; ++i) d[0][i] = __int2bfloat16_rn((int)N[i]);
+    for (int i = 0; i < 8; ++i) N[i] += kDigitBias<S>;
     const int kt = kc / (kKS / 8), kin = kc % (kKS / 8);
     uint8_t* base = dst + (int64_t)kt * unit_bytes + (r / 8) * kSBO + kin * 128 + (r % 8) * 16;
 #pragma unroll
     for (int q = 0; q < S; ++q) {
+      uint32_t fb[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float f;
+        if (q == 0) {  // leading digit: (N' >> 7(S-1)) - 64 in [-65, 65]
+          const int u0 = (int)(N[i] >> (kBits * (S - 1))) + 1;
+          f = __int_as_float(0x4B000000 + u0) - 8388673.0f;
+        } else {
+          const uint32_t uq = (uint32_t)(N[i] >> (kBits * (S - 1 - q))) & 127u;
+          f = __int_as_float(0x4B000000 | uq) - 8388672.0f;
+        }
+        fb[i] = __float_as_uint(f);
+      }
       uint4 v;
-      v.x = (uint32_t)__bfloat16_as_ushort(d[q][0]) | ((uint32_t)__bfloat16_as_ushort(d[q][1]) << 16);
-      v.y = (uint32_t)__bfloat16_as_ushort(d[q][2]) | ((uint32_t)__bfloat16_as_ushort(d[q][3]) << 16);
-      v.z = (uint32_t)__bfloat16_as_ushort(d[q][4]) | ((uint32_t)__bfloat16_as_ushort(d[q][5]) << 16);
-      v.w = (uint32_t)__bfloat16_as_ushort(d[q][6]) | ((uint32_t)__bfloat16_as_ushort(d[q][7]) << 16);
+      v.x = __byte_perm(fb[0], fb[1], 0x7632);
+      v.y = __byte_perm(fb[2], fb[3], 0x7632);
+      v.z = __byte_perm(fb[4], fb[5], 0x7632);
+      v.w = __byte_perm(fb[6], fb[7], 0x7632);
       *reinterpret_cast<uint4*>(base + q * slice_bytes) = v;
     }
   }
@@ -121,13 +218,17 @@ cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, const Bases& bases,
+cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, const Bases& bases,
                         uint8_t* packed, int* exps, cudaStream_t stream) {
   if (nunits <= 0) return cudaSuccess;
+  const int64_t warps = (int64_t)nunits * kRowsPerUnit;
+  const int rows_blocks = (int)((warps + kPackThreads / 32 - 1) / (kPackThreads / 32));
+  pack_rows_kernel<<<rows_blocks, kPackThreads, 0, stream>>>(jobs, units, nunits, bases, exps);
+  const dim3 grid(nunits, (max_nkt + kDigitKt - 1) / kDigitKt);
   switch (S) {
-    case 6: pack_kernel<6><<<nunits, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
-    case 7: pack_kernel<7><<<nunits, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
-    case 8: pack_kernel<8><<<nunits, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
+    case 6: pack_digits_kernel<6><<<grid, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
+    case 7: pack_digits_kernel<7><<<grid, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
+    case 8: pack_digits_kernel<8><<<grid, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

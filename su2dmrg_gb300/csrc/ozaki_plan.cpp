@@ -42,6 +42,7 @@ struct Builder {
     j.dst = w->packed_bytes;
     j.exp = w->exp_len;
     j.texp = w->exp_len + (int64_t)j.nrt * rt;
+    j.rowmax = -1;
     w->packed_bytes += (int64_t)j.nrt * j.nkt * S * rt * kKS * 2;
     w->exp_len += (int64_t)j.nrt * rt + j.nrt;
     lists[cls]->push_back(j);
@@ -102,6 +103,9 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
         t.seg0 = (int)oseg->size();
         t.nseg = ob.nseg;
         t.work = 0;
+        t.rowmax = -1;
+        t.rms = 1;
+        t.pad2 = 0;
         for (int s = 0; s < ob.nseg; ++s) {
           const PackJob& a = B.get(bufs[s].first, ids[s].first);
           const PackJob& b = B.get(bufs[s].second, ids[s].second);
@@ -196,14 +200,46 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   if (rc) return rc;
   rc = build_phase(B, hw.seg2, hw.blk2, &w.seg2, &w.tile2, err);
   if (rc) return rc;
+  // Phase-1 outputs become phase-2 operands: when a phase-1 block feeds exactly
+  // one unit-scaled pack job as its rows (row i = block columns i*rms ..
+  // (i+1)*rms - 1, all block rows), the phase-1 tiles leave the row maxima
+  // and the pack skips its own pass over the block.
+  {
+    std::map<int64_t, std::vector<int>> by_src;
+    for (int j = 0; j < (int)w.jobs[2].size(); ++j)
+      if (w.jobs[2][j].src_buf == kBufScratch) by_src[w.jobs[2][j].src].push_back(j);
+    w.rowmax_base = w.exp_len;
+    std::map<int64_t, std::pair<int64_t, int>> slots;  // block origin -> (slots, rms)
+    for (const OutBlock& ob : hw.blk1) {
+      auto it = by_src.find(ob.c);
+      if (ob.c_buf != kBufScratch || it == by_src.end() || it->second.size() != 1) continue;
+      PackJob& j = w.jobs[2][it->second[0]];
+      if (j.alpha != 1.0 || j.ld_k != 1 || j.R <= 0 || ob.N % j.R != 0) continue;
+      const int rms = ob.N / j.R;
+      if (j.ld_r != (int64_t)ob.ldc * rms || j.K != ob.M * rms || ob.ldc != ob.M) continue;
+      j.rowmax = w.exp_len;
+      w.exp_len += j.R;
+      slots[ob.c] = {j.rowmax, rms};
+    }
+    w.rowmax_len = w.exp_len - w.rowmax_base;
+    for (OzTile& t : w.tile1) {
+      auto it = slots.find(t.c);
+      if (it == slots.end()) continue;
+      t.rowmax = it->second.first;
+      t.rms = it->second.second;
+    }
+  }
   split_phase2(w);
   auto heavier = [](const OzTile& x, const OzTile& y) { return x.work > y.work; };
   std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
   std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
   for (int c = 0; c < 3; ++c) {
     w.units[c].clear();
-    for (int j = 0; j < (int)w.jobs[c].size(); ++j)
+    w.max_nkt[c] = 0;
+    for (int j = 0; j < (int)w.jobs[c].size(); ++j) {
+      w.max_nkt[c] = std::max(w.max_nkt[c], w.jobs[c][j].nkt);
       for (int r = 0; r < w.jobs[c][j].nrt; ++r) w.units[c].push_back(Unit{j, r});
+    }
   }
   return validate_ozaki_work(w, err);
 }
@@ -213,7 +249,8 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
     for (const PackJob& j : w.jobs[c]) {
       const int64_t bytes = (int64_t)j.nrt * j.nkt * w.S * j.rt * kKS * 2;
       if (j.dst < 0 || j.dst % 1024 || j.dst + bytes > w.packed_bytes || j.exp < 0 ||
-          j.exp + (int64_t)j.nrt * j.rt > w.exp_len || j.texp < 0 || j.texp + j.nrt > w.exp_len || j.R <= 0 ||
+          j.exp + (int64_t)j.nrt * j.rt > w.exp_len || j.texp < 0 || j.texp + j.nrt > w.exp_len ||
+          (j.rowmax >= 0 && (j.rowmax < w.rowmax_base || j.rowmax + j.R > w.rowmax_base + w.rowmax_len)) || j.R <= 0 ||
           j.K <= 0 || (j.rt != kTM && j.rt != kTN)) {
         *err = "split mode: pack job out of bounds";
         return SU2G_EINVAL;
@@ -223,6 +260,9 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
     for (const OzTile& t : tiles) {
       if (t.seg0 < 0 || t.nseg < 0 || t.seg0 + t.nseg > (int)segs.size() || t.mlen <= 0 || t.mlen > kTM ||
           t.nlen <= 0 || t.nlen > kTN || t.ldc < t.m0 + t.mlen)
+        return false;
+      if (t.rowmax >= 0 && (t.rms <= 0 || t.rowmax < w.rowmax_base ||
+                            t.rowmax + (t.n0 + t.nlen - 1) / t.rms >= w.rowmax_base + w.rowmax_len))
         return false;
       for (int s = t.seg0; s < t.seg0 + t.nseg; ++s) {
         const OzSeg& z = segs[s];

@@ -20,11 +20,14 @@ struct OzWork {
   // 2 = phase-1 intermediates (packed between the two phases)
   std::vector<PackJob> jobs[3];
   std::vector<Unit> units[3];
+  int max_nkt[3] = {0, 0, 0};  // largest k-tile count of a job of each class
   std::vector<OzSeg> seg1, seg2;
   std::vector<OzTile> tile1, tile2;
   std::vector<RedTile> red2;  // phase-2 tiles split across CTAs: fixed-order sums
   int64_t packed_bytes = 0;   // bytes of all packed operands
   int64_t exp_len = 0;        // int32 row exponents of all packed operands
+  int64_t rowmax_base = 0;    // the row-maximum slots: exps[rowmax_base, + rowmax_len),
+  int64_t rowmax_len = 0;     // zeroed before phase 1 of every application
   int64_t scratch_base = 0;   // doubles of the plan scratch before the partial tiles
   int64_t partial_len = 0;    // doubles of partial tiles after scratch_base
 };
