@@ -1,5 +1,5 @@
 // Split-precision tile GEMM on the tcgen05 tensor cores (representation in
-// ozaki.hpp).  One CTA computes one 128 x 64 output tile with three roles:
+// ozaki.hpp).  A CTA computes 128 x 64 output tiles with three roles:
 //
 //   warp 16, lane 0 producer: bulk-copies the packed A (S slices x 128 x 16)
 //                   and B (S slices x 64 x 16) units of each K stage into a
@@ -156,8 +156,14 @@ struct Smem {
 
 // rowmax_out is the exponent buffer again: the kernel writes only its
 // row-maximum region (OzWork::rowmax_base ..), which it never reads through exps.
+//
+// Persistent: CTA b computes tiles b, b + gridDim.x, ... (heaviest first, as
+// the planner sorts them).  The producer runs ahead across tile boundaries,
+// the MMAs of tile i+1 start as soon as the drain warps have read tile i's
+// last chunk, and the conversion and stores of tile i overlap them.
 template <int S>
-__global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restrict__ tiles, const OzSeg* __restrict__ segs,
+__global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restrict__ tiles, int ntiles,
+                                                          const OzSeg* __restrict__ segs,
                                                           const uint8_t* __restrict__ packed,
                                                           const int* __restrict__ exps, int* rowmax_out,
                                                           Bases bases, int* err) {
@@ -171,7 +177,6 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
   __shared__ int shb_sh[kEpiWarps][kCols];  // per drain warp: column shifts of the current segment
   __shared__ int abort_sh, loaded_sh, consumed_sh;
 
-  const OzTile t = tiles[blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
@@ -204,20 +209,25 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     if (lane == 0) {
       int loaded = 0;
       bool ok = true;
-      for (int s = 0; s < t.nseg && ok; ++s) {
-        const OzSeg g = segs[t.seg0 + s];
-        for (int ks = 0; ks < g.nks; ++ks, ++loaded) {
-          const int st = loaded % kStages;
-          if (*abort_v) { ok = false; break; }
-          // the stage's previous contents must have been consumed by their MMAs
-          if (loaded >= kStages && !mbar_wait(smem_u32(&bar_empty[st]), ((loaded / kStages) - 1) & 1)) {
-            ok = false;
-            break;
+      for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        const OzTile t = tiles[ti];
+        for (int s = 0; s < t.nseg && ok; ++s) {
+          const OzSeg g = segs[t.seg0 + s];
+          for (int ks = 0; ks < g.nks; ++ks, ++loaded) {
+            const int st = loaded % kStages;
+            if (*abort_v) { ok = false; break; }
+            // the stage's previous contents must have been consumed by their MMAs
+            if (loaded >= kStages && !mbar_wait(smem_u32(&bar_empty[st]), ((loaded / kStages) - 1) & 1)) {
+              ok = false;
+              break;
+            }
+            const uint32_t a_dst = stage_a(st), b_dst = a_dst + Smem<S>::kA;
+            mbar_expect_tx(smem_u32(&bar_full[st]), Smem<S>::kStage);
+            bulk_g2s(a_dst, packed + g.a_unit + (int64_t)ks * a_unit_bytes(S), Smem<S>::kA,
+                     smem_u32(&bar_full[st]));
+            bulk_g2s(b_dst, packed + g.b_unit + (int64_t)ks * b_unit_bytes(S), Smem<S>::kB,
+                     smem_u32(&bar_full[st]));
           }
-          const uint32_t a_dst = stage_a(st), b_dst = a_dst + Smem<S>::kA;
-          mbar_expect_tx(smem_u32(&bar_full[st]), Smem<S>::kStage);
-          bulk_g2s(a_dst, packed + g.a_unit + (int64_t)ks * a_unit_bytes(S), Smem<S>::kA, smem_u32(&bar_full[st]));
-          bulk_g2s(b_dst, packed + g.b_unit + (int64_t)ks * b_unit_bytes(S), Smem<S>::kB, smem_u32(&bar_full[st]));
         }
       }
       if (!ok) {
@@ -231,41 +241,44 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     if (lane == 0) {
       int it = 0, chunk = 0;
       bool ok = true;
-      for (int s = 0; s < t.nseg && ok; ++s) {
-        const int nks = segs[t.seg0 + s].nks;
-        for (int ks = 0; ks < nks; ++ks, ++it) {
-          const int st = it % kStages;
-          if (*abort_v || !mbar_wait(smem_u32(&bar_full[st]), (it / kStages) & 1)) { ok = false; break; }
-          const bool first = (ks % kChunkStages) == 0;
-          // a new chunk overwrites the group sums: the epilogue must have read them
-          if (first && chunk > 0 && !mbar_wait(smem_u32(&bar_acce), (chunk - 1) & 1)) {
-            ++it;  // this stage was waited for: it counts as consumed
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t sa = stage_a(st), sb = sa + Smem<S>::kA;
-          // The B digit slices lie back to back (64 rows each, same core-row
-          // stride) and so do the group accumulators in TMEM (64 columns
-          // each): the pairs (p, q) .. (p, q+n-1) are one MMA of N = 64 n that
-          // reads B_q .. B_{q+n-1} as one 64n-row operand and adds into groups
-          // p+q .. p+q+n-1.  Up to n = 4 (N = 256): 10 MMAs per stage for S = 7
-          // instead of 28, and A is read once per MMA.  p = 1 touches every
-          // group first, so only its MMAs start a chunk's sums from zero.
-#pragma unroll
-          for (int p = 1; p <= S; ++p) {
-            const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
-#pragma unroll
-            for (int q = 1; q <= S + 1 - p; q += 4) {
-              const int n = (S + 2 - p - q) < 4 ? (S + 2 - p - q) : 4;
-              const uint64_t bd = smem_desc(sb + (q - 1) * (kTN * kKS * 2));
-              mma(tmem + (uint32_t)((p + q - 2) * kTN), ad, bd, idesc(kTN * n), (first && p == 1) ? 0u : 1u);
+      for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        const OzTile t = tiles[ti];
+        for (int s = 0; s < t.nseg && ok; ++s) {
+          const int nks = segs[t.seg0 + s].nks;
+          for (int ks = 0; ks < nks; ++ks, ++it) {
+            const int st = it % kStages;
+            if (*abort_v || !mbar_wait(smem_u32(&bar_full[st]), (it / kStages) & 1)) { ok = false; break; }
+            const bool first = (ks % kChunkStages) == 0;
+            // a new chunk overwrites the group sums: the epilogue must have read them
+            if (first && chunk > 0 && !mbar_wait(smem_u32(&bar_acce), (chunk - 1) & 1)) {
+              ++it;  // this stage was waited for: it counts as consumed
+              ok = false;
+              break;
             }
-          }
-          mma_commit(smem_u32(&bar_empty[st]));
-          if ((ks % kChunkStages) == kChunkStages - 1 || ks == nks - 1) {
-            mma_commit(smem_u32(&bar_accf));
-            ++chunk;
+            tc_fence_after();
+            const uint32_t sa = stage_a(st), sb = sa + Smem<S>::kA;
+            // The B digit slices lie back to back (64 rows each, same core-row
+            // stride) and so do the group accumulators in TMEM (64 columns
+            // each): the pairs (p, q) .. (p, q+n-1) are one MMA of N = 64 n that
+            // reads B_q .. B_{q+n-1} as one 64n-row operand and adds into groups
+            // p+q .. p+q+n-1.  Up to n = 4 (N = 256): 10 MMAs per stage for S = 7
+            // instead of 28, and A is read once per MMA.  p = 1 touches every
+            // group first, so only its MMAs start a chunk's sums from zero.
+#pragma unroll
+            for (int p = 1; p <= S; ++p) {
+              const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
+#pragma unroll
+              for (int q = 1; q <= S + 1 - p; q += 4) {
+                const int n = (S + 2 - p - q) < 4 ? (S + 2 - p - q) : 4;
+                const uint64_t bd = smem_desc(sb + (q - 1) * (kTN * kKS * 2));
+                mma(tmem + (uint32_t)((p + q - 2) * kTN), ad, bd, idesc(kTN * n), (first && p == 1) ? 0u : 1u);
+              }
+            }
+            mma_commit(smem_u32(&bar_empty[st]));
+            if ((ks % kChunkStages) == kChunkStages - 1 || ks == nks - 1) {
+              mma_commit(smem_u32(&bar_accf));
+              ++chunk;
+            }
           }
         }
       }
@@ -280,131 +293,140 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
     }
   } else {
     // ============================ epilogue ============================
+    // Every drain warp walks the same tiles, segments and chunks and takes the
+    // same named barriers whatever happens: after a wait that gave up it goes
+    // on without waiting or reading TMEM, so no warp is ever left at a barrier.
     const int lq = warp & 3, col0 = (warp >> 2) * kCols;
     const int row = lq * 32 + lane;  // TMEM lane == tile row
     const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
-    // Exponent bookkeeping.  Segment s contributes 2^(eA_s(i) + eB_s(j)) times
-    // its digit sums; moving c_s = max_i eA_s(i) (over the tile rows) from the
-    // A side to the B side leaves every product unchanged but makes the
-    // tile's reference exponents emax(i) = max_s (eA_s(i) - c_s) and
-    // fmax(j) = max_s (eB_s(j) + c_s) track the largest actual product scale
-    // (otherwise an O(1) x O(1e-3) segment and an O(1e-3) x O(1) segment would
-    // set a reference 2^10 above both).
-    // c_s = the A row tile's largest exponent, recorded by the pack kernel
-    for (int s = tid; s < t.nseg; s += kEpiThreads) {
-      const int m = exps[segs[t.seg0 + s].a_tmax];
-      cshift_sh[s] = (m == kExpZero) ? 0 : m;
-    }
-    if (tid < kTN) colmax_sh[tid] = 0;
-    asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
-    int emax = kExpZero;
-#pragma unroll 8
-    for (int s = 0; s < t.nseg; ++s) {
-      const int e = exps[segs[t.seg0 + s].a_exp + row];
-      if (e != kExpZero) emax = max(emax, e - cshift_sh[s]);
-    }
-    if (tid < kTN) {
-      int f = kExpZero;
-#pragma unroll 8
-      for (int s = 0; s < t.nseg; ++s) {
-        const int fb = exps[segs[t.seg0 + s].b_exp + tid];
-        if (fb != kExpZero) f = max(f, fb + cshift_sh[s]);
-      }
-      fmax_sh[tid] = f;
-    }
-    // the only block-wide barrier of the epilogue, taken before any bounded
-    // wait so that a time-out can never leave a warp stranded in it
-    asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
-    long long acc[kCols];
-#pragma unroll
-    for (int j = 0; j < kCols; ++j) acc[j] = 0;
     int chunk = 0;
     bool ok = true;
-    for (int s = 0; s < t.nseg && ok; ++s) {
-      const OzSeg g = segs[t.seg0 + s];
-      const int ea = exps[g.a_exp + row];
-      const int cs = cshift_sh[s];
-      const int sha = (ea == kExpZero) ? 1000 : emax - (ea - cs);
-      // column shifts of this segment, staged per warp (no block barrier)
-      __syncwarp();
-      if (lane < kCols) {
-        const int fj = exps[g.b_exp + col0 + lane];
-        shb_sh[warp][lane] = (fj == kExpZero) ? 1000 : fmax_sh[col0 + lane] - (fj + cs);
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+      const OzTile t = tiles[ti];
+      // Exponent bookkeeping.  Segment s contributes 2^(eA_s(i) + eB_s(j))
+      // times its digit sums; moving c_s = max_i eA_s(i) (over the tile rows)
+      // from the A side to the B side leaves every product unchanged but makes
+      // the tile's reference exponents emax(i) = max_s (eA_s(i) - c_s) and
+      // fmax(j) = max_s (eB_s(j) + c_s) track the largest actual product scale
+      // (otherwise an O(1) x O(1e-3) segment and an O(1e-3) x O(1) segment
+      // would set a reference 2^10 above both).  c_s = the A row tile's largest
+      // exponent, recorded by the pack kernel.
+      for (int s = tid; s < t.nseg; s += kEpiThreads) {
+        const int m = exps[segs[t.seg0 + s].a_tmax];
+        cshift_sh[s] = (m == kExpZero) ? 0 : m;
       }
-      __syncwarp();
-      const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
-      for (int c = 0; c < nchunks; ++c, ++chunk) {
-        if (!mbar_wait(smem_u32(&bar_accf), chunk & 1)) { ok = false; break; }
-        tc_fence_after();
+      if (tid < kTN) colmax_sh[tid] = 0;
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      int emax = kExpZero;
+#pragma unroll 8
+      for (int s = 0; s < t.nseg; ++s) {
+        const int e = exps[segs[t.seg0 + s].a_exp + row];
+        if (e != kExpZero) emax = max(emax, e - cshift_sh[s]);
+      }
+      if (tid < kTN) {
+        int f = kExpZero;
+#pragma unroll 8
+        for (int s = 0; s < t.nseg; ++s) {
+          const int fb = exps[segs[t.seg0 + s].b_exp + tid];
+          if (fb != kExpZero) f = max(f, fb + cshift_sh[s]);
+        }
+        fmax_sh[tid] = f;
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      long long acc[kCols];
 #pragma unroll
-        for (int cb = 0; cb < kCols / 4; ++cb) {
-          // all S group sums of 4 columns in flight, one wait
-          uint32_t r[S][4];
+      for (int j = 0; j < kCols; ++j) acc[j] = 0;
+      for (int s = 0; s < t.nseg; ++s) {
+        const OzSeg g = segs[t.seg0 + s];
+        const int ea = exps[g.a_exp + row];
+        const int cs = cshift_sh[s];
+        const int sha = (ea == kExpZero) ? 1000 : emax - (ea - cs);
+        // column shifts of this segment, staged per warp (no block barrier)
+        __syncwarp();
+        if (lane < kCols) {
+          const int fj = exps[g.b_exp + col0 + lane];
+          shb_sh[warp][lane] = (fj == kExpZero) ? 1000 : fmax_sh[col0 + lane] - (fj + cs);
+        }
+        __syncwarp();
+        const int nchunks = (g.nks + kChunkStages - 1) / kChunkStages;
+        for (int c = 0; c < nchunks; ++c, ++chunk) {
+          if (ok && !mbar_wait(smem_u32(&bar_accf), chunk & 1)) ok = false;
+          if (!ok) continue;
+          tc_fence_after();
 #pragma unroll
-          for (int gg = 0; gg < S; ++gg)
-            tmem_ld4(tmem + lane_base + (uint32_t)(gg * kTN + col0 + cb * 4), r[gg]);
-          tmem_wait_ld();
-#pragma unroll
-          for (int x = 0; x < 4; ++x) {
-            long long v = 0;
+          for (int cb = 0; cb < kCols / 4; ++cb) {
+            // all S group sums of 4 columns in flight, one wait
+            uint32_t r[S][4];
 #pragma unroll
             for (int gg = 0; gg < S; ++gg)
-              v += shl_signed((long long)f32_to_int_exact(r[gg][x]), kFixedTop - kBits * (gg + 2));
-            const int j = cb * 4 + x;
-            const int sh = sha + shb_sh[warp][j];
-            if (sh == 0) {
-              acc[j] += v;
-            } else if (sh < 63) {
-              acc[j] += (v + (1ll << (sh - 1))) >> sh;  // round to nearest
+              tmem_ld4(tmem + lane_base + (uint32_t)(gg * kTN + col0 + cb * 4), r[gg]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+              long long v = 0;
+#pragma unroll
+              for (int gg = 0; gg < S; ++gg)
+                v += shl_signed((long long)f32_to_int_exact(r[gg][x]), kFixedTop - kBits * (gg + 2));
+              const int j = cb * 4 + x;
+              const int sh = sha + shb_sh[warp][j];
+              if (sh == 0) {
+                acc[j] += v;
+              } else if (sh < 63) {
+                acc[j] += (v + (1ll << (sh - 1))) >> sh;  // round to nearest
+              }
             }
           }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&bar_acce));
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&bar_acce));
       }
+      // ---- store: C = acc * 2^(emax + fmax - kFixedTop) ----
+      // A phase-1 block that becomes a phase-2 operand also leaves, per
+      // operand row (block columns i*rms ..), the largest ilogb of its values,
+      // so that the pack needs no pass of its own over the block.
+      double* C = resolve(bases, t.c_buf, t.c);
+      const int ebase = emax - kFixedTop;
+      int lg[kCols];  // kRowmaxBias-coded ilogb |value|, 0 for a zero or absent value
+      if (row < t.mlen) {
+#pragma unroll
+        for (int jj = 0; jj < kCols; ++jj) {
+          const int j = col0 + jj;
+          lg[jj] = 0;
+          if (j < t.nlen) {
+            const int f = fmax_sh[j];
+            double out = 0.0;
+            if (ok && emax != kExpZero && f != kExpZero) out = scaled_to_double(acc[jj], ebase + f);
+            C[(int64_t)(t.m0 + row) + (int64_t)(t.n0 + j) * t.ldc] = out;
+            const unsigned long long ob = (unsigned long long)__double_as_longlong(out);
+            if (t.rowmax >= 0 && (ob & 0x7FFFFFFFFFFFFFFFull)) lg[jj] = ilogb_bits(ob) + kRowmaxBias;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < kCols; ++jj) lg[jj] = 0;
+      }
+      if (t.rowmax >= 0) {  // uniform over the CTA
+        // column maxima: over the warp's rows (lane jj keeps column jj), over
+        // the four lane quarters (shared memory), then one global atomic per
+        // column
+        int mine = 0;
+#pragma unroll
+        for (int jj = 0; jj < kCols; ++jj) {
+          const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)lg[jj]);
+          if (lane == jj) mine = m;
+        }
+        if (lane < kCols && mine > 0) atomicMax(&colmax_sh[col0 + lane], mine);
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+        if (tid < t.nlen && colmax_sh[tid] > 0)
+          atomicMax(&rowmax_out[t.rowmax + (t.n0 + tid) / t.rms], colmax_sh[tid]);
+      }
+      // the next tile's bookkeeping rewrites the shared tile state
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
     }
     if (!ok) {
       atomicExch(err, 3);
       atomicExch(&abort_sh, 1);
-    }
-    // ---- store: C = acc * 2^(emax + fmax - kFixedTop) ----
-    // A phase-1 block that becomes a phase-2 operand also leaves, per operand
-    // row (block columns i*rms ..), the largest ilogb of its values, so that
-    // the pack needs no pass of its own over the block.
-    double* C = resolve(bases, t.c_buf, t.c);
-    const int ebase = emax - kFixedTop;
-    int lg[kCols];  // kRowmaxBias-coded ilogb |value|, 0 for a zero or absent value
-    if (row < t.mlen) {
-#pragma unroll
-      for (int jj = 0; jj < kCols; ++jj) {
-        const int j = col0 + jj;
-        lg[jj] = 0;
-        if (j < t.nlen) {
-          const int f = fmax_sh[j];
-          double out = 0.0;
-          if (ok && emax != kExpZero && f != kExpZero) out = scaled_to_double(acc[jj], ebase + f);
-          C[(int64_t)(t.m0 + row) + (int64_t)(t.n0 + j) * t.ldc] = out;
-          const unsigned long long ob = (unsigned long long)__double_as_longlong(out);
-          if (t.rowmax >= 0 && (ob & 0x7FFFFFFFFFFFFFFFull)) lg[jj] = ilogb_bits(ob) + kRowmaxBias;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int jj = 0; jj < kCols; ++jj) lg[jj] = 0;
-    }
-    if (t.rowmax >= 0) {  // uniform over the CTA
-      // column maxima: over the warp's rows (lane jj keeps column jj), over the
-      // four lane quarters (shared memory), then one global atomic per column
-      int mine = 0;
-#pragma unroll
-      for (int jj = 0; jj < kCols; ++jj) {
-        const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)lg[jj]);
-        if (lane == jj) mine = m;
-      }
-      if (lane < kCols && mine > 0) atomicMax(&colmax_sh[col0 + lane], mine);
-      asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
-      if (tid < t.nlen && colmax_sh[tid] > 0) atomicMax(&rowmax_out[t.rowmax + (t.n0 + tid) / t.rms], colmax_sh[tid]);
     }
   }
   tc_fence_before();
@@ -434,16 +456,26 @@ int gemm_smem_bytes(int S) {
 cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
                               int* exps, const Bases& bases, int* err, cudaStream_t stream) {
   if (ntiles <= 0) return cudaSuccess;
+  static int sms = 0;  // one resident CTA per SM (shared memory and TMEM): a persistent grid
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      sms = n;
+    if (sms <= 0) sms = 148;
+  }
+  const int grid = ntiles < sms ? ntiles : sms;
   const int smem = gemm_smem_bytes(S);
   cudaError_t e = cudaSuccess;
   switch (S) {
     case 6:
       e = cudaFuncSetAttribute(ozaki_gemm<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess) ozaki_gemm<6><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, exps, bases, err);
+      if (e == cudaSuccess)
+        ozaki_gemm<6><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
       break;
     case 7:
       e = cudaFuncSetAttribute(ozaki_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess) ozaki_gemm<7><<<ntiles, kThreads, smem, stream>>>(tiles, segs, packed, exps, exps, bases, err);
+      if (e == cudaSuccess)
+        ozaki_gemm<7><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
       break;
     default:
       return cudaErrorInvalidValue;
