@@ -323,8 +323,17 @@ def run_su2g(args):
         pairs = S * (S + 1) // 2
         t_kernel = (prof[1] + prof[3]) / 1e3
         achieved = pairs * flops / t_kernel / 1e12
+        # DRAM bytes of the two GEMM launches, measured with ncu (dram__bytes_read.sum +
+        # dram__bytes_write.sum) on the D=1000 case: 4.09 bytes per algorithmic byte of an
+        # application (FP64 operators + psi in/out); algorithmic bytes are computed here.
+        alg_bytes = 8.0 * (sum(x.numel() for (_s1, x1, _s2, x2, _c) in terms for x in (x1, x2))
+                           + sum(h[1].numel() for h in (hl, hr) if h is not None) + 2 * w.psi.size())
+        traffic = 4.09 * alg_bytes / 2 if S == 7 else None
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_definition": "DRAM bytes per GEMM launch: ncu-measured 4.09 x algorithmic bytes per "
+                                      "application (D=1000 capture), scaled by this workload's algorithmic bytes "
+                                      f"({alg_bytes:.4g} B), halved over the two launches",
                 "kernel": f"ozaki_gemm<{S}> (tcgen05 BF16, {pairs} digit-pair products per FP64 product), "
                           "2 launches per step",
                 "achieved_definition": f"{pairs} x algorithmic FP64 FLOPs of the two GEMM launches / their time",
@@ -355,7 +364,7 @@ def run_su2g(args):
                    "l2": "inputs (operators ~1.3 GB) larger than L2; no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "path": "su2g_heff_apply via ctypes, pinned host psi -> device -> host y; operators resident"},
-        "gpu_launches": (2 if S == 0 else 4) * args.steps,
+        "gpu_launches": plan.launches() * args.steps,
         "roofline": roof,
         "accuracy": accuracy,
         "cpu_baseline": cb,

@@ -116,6 +116,9 @@ int su2g_heff_plan_status(su2g_heff_plan* plan, int* code);
  * output tiles of the two launch phases. */
 int su2g_heff_plan_info(const su2g_heff_plan* plan, double* flops, int64_t* psi_len, int64_t* scratch_bytes,
                         int* ntiles);
+/* Number of this library's kernels one su2g_heff_apply launches (memsets and
+ * copies not counted). */
+int su2g_heff_plan_launches(const su2g_heff_plan* plan, int* n);
 /* y = H_eff psi (device pointers, psi_len doubles each, no aliasing). */
 int su2g_heff_apply(su2g_heff_plan* plan, const double* psi, double* y, void* stream);
 /* su2g_heff_apply with a CUDA event between its launches; waits for the

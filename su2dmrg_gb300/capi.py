@@ -73,6 +73,7 @@ _PROTOS = {
     "su2g_heff_plan_status": (_i, [_vp, _vp]),
     "su2g_heff_plan_info": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "su2g_heff_plan_launches": (_i, [_vp, _vp]),
     "su2g_heff_apply_profile": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_plan_destroy": (_i, [_vp]),
     "su2g_heff_plan_add_projector": (_i, [_vp, _vp, _d]),

@@ -151,7 +151,7 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   if (e == cudaSuccess) e = upload(w.red2, &p->d_red2);
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
-  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0], b, p->d_packed, p->d_exps,
+  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0], w.rows_pass[0], b, p->d_packed, p->d_exps,
                             nullptr);
   if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
   return e;
@@ -442,6 +442,25 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
   return SU2G_OK;
 }
 
+int su2g_heff_plan_launches(const su2g_heff_plan* p, int* n) {
+  if (!p || !n) return fail(SU2G_EINVAL, "plan_launches: bad arguments");
+  int c = 0;
+  if (p->S == 0) {
+    c += p->work.tile1.empty() ? 0 : 1;
+    c += p->work.tile2.empty() ? 0 : 1;
+  } else {
+    const su2g::oz::OzWork& w = p->oz;
+    for (int k = 1; k <= 2; ++k)
+      if (!w.units[k].empty()) c += w.rows_pass[k] ? 2 : 1;
+    c += w.tile1.empty() ? 0 : 1;
+    c += w.tile2.empty() ? 0 : 1;
+    c += w.red2.empty() ? 0 : 1;
+  }
+  c += 2 * (int)p->proj_vec.size();
+  *n = c;
+  return SU2G_OK;
+}
+
 int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
   if (!p || !code) return fail(SU2G_EINVAL, "plan_status: bad arguments");
   *code = 0;
@@ -507,11 +526,11 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
   // the row maxima that phase 1 leaves for the intermediates' pack start at zero
   if (w.rowmax_len > 0)
     SU2G_CUDA(cudaMemsetAsync(p->d_exps + w.rowmax_base, 0, w.rowmax_len * sizeof(int), st));
-  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], b, p->d_packed,
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], w.rows_pass[1], b, p->d_packed,
                                   p->d_exps, st));
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile1, (int)w.tile1.size(), p->d_oseg1, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
-  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], b, p->d_packed,
+  SU2G_CUDA(su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], w.rows_pass[2], b, p->d_packed,
                                   p->d_exps, st));
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
@@ -541,7 +560,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
     if (e == cudaSuccess && w.rowmax_len > 0)
       e = cudaMemsetAsync(p->d_exps + w.rowmax_base, 0, w.rowmax_len * sizeof(int), st);
     if (e == cudaSuccess)
-      e = su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], b, p->d_packed, p->d_exps,
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[1], p->d_units[1], (int)w.units[1].size(), w.max_nkt[1], w.rows_pass[1], b, p->d_packed, p->d_exps,
                                 st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
     if (e == cudaSuccess)
@@ -549,7 +568,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
                                       p->d_err, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
     if (e == cudaSuccess)
-      e = su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], b, p->d_packed, p->d_exps,
+      e = su2g::oz::launch_pack(p->S, p->d_jobs[2], p->d_units[2], (int)w.units[2].size(), w.max_nkt[2], w.rows_pass[2], b, p->d_packed, p->d_exps,
                                 st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
     if (e == cudaSuccess)

@@ -31,8 +31,9 @@ struct OzSeg;
 struct OzTile;
 struct RedTile;
 cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaStream_t stream);
-cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, const Bases& bases,
-                        uint8_t* packed, int* exps, cudaStream_t stream);
+// row-exponent pass (when rows_pass) + digit pass: 1 or 2 kernels, none for nunits == 0
+cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, bool rows_pass,
+                        const Bases& bases, uint8_t* packed, int* exps, cudaStream_t stream);
 cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
                               int* exps, const Bases& bases, int* err, cudaStream_t stream);
 int gemm_smem_bytes(int S);

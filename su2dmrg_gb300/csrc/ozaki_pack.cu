@@ -218,12 +218,14 @@ cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, const Bases& bases,
-                        uint8_t* packed, int* exps, cudaStream_t stream) {
+cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, bool rows_pass,
+                        const Bases& bases, uint8_t* packed, int* exps, cudaStream_t stream) {
   if (nunits <= 0) return cudaSuccess;
-  const int64_t warps = (int64_t)nunits * kRowsPerUnit;
-  const int rows_blocks = (int)((warps + kPackThreads / 32 - 1) / (kPackThreads / 32));
-  pack_rows_kernel<<<rows_blocks, kPackThreads, 0, stream>>>(jobs, units, nunits, bases, exps);
+  if (rows_pass) {
+    const int64_t warps = (int64_t)nunits * kRowsPerUnit;
+    const int rows_blocks = (int)((warps + kPackThreads / 32 - 1) / (kPackThreads / 32));
+    pack_rows_kernel<<<rows_blocks, kPackThreads, 0, stream>>>(jobs, units, nunits, bases, exps);
+  }
   const dim3 grid(nunits, (max_nkt + kDigitKt - 1) / kDigitKt);
   switch (S) {
     case 6: pack_digits_kernel<6><<<grid, kPackThreads, 0, stream>>>(jobs, units, bases, packed, exps); break;

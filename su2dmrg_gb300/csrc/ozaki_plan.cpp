@@ -236,8 +236,10 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   for (int c = 0; c < 3; ++c) {
     w.units[c].clear();
     w.max_nkt[c] = 0;
+    w.rows_pass[c] = false;
     for (int j = 0; j < (int)w.jobs[c].size(); ++j) {
       w.max_nkt[c] = std::max(w.max_nkt[c], w.jobs[c][j].nkt);
+      if (w.jobs[c][j].rowmax < 0) w.rows_pass[c] = true;
       for (int r = 0; r < w.jobs[c][j].nrt; ++r) w.units[c].push_back(Unit{j, r});
     }
   }

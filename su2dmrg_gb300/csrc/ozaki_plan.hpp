@@ -21,6 +21,7 @@ struct OzWork {
   std::vector<PackJob> jobs[3];
   std::vector<Unit> units[3];
   int max_nkt[3] = {0, 0, 0};  // largest k-tile count of a job of each class
+  bool rows_pass[3] = {true, true, true};  // some job of the class needs the row-exponent pass
   std::vector<OzSeg> seg1, seg2;
   std::vector<OzTile> tile1, tile2;
   std::vector<RedTile> red2;  // phase-2 tiles split across CTAs: fixed-order sums

@@ -209,6 +209,12 @@ class HeffPlan:
                                         ctypes.addressof(nt)))
         return {"flops": fl.value, "psi_len": n.value, "scratch_bytes": sb.value, "ntiles": nt.value}
 
+    def launches(self) -> int:
+        """Kernels of this library one apply() launches."""
+        n = ctypes.c_int()
+        check(lib().su2g_heff_plan_launches(self._h, ctypes.addressof(n)))
+        return n.value
+
     def apply(self, psi, y, stream=None) -> None:
         check(lib().su2g_heff_apply(self._h, ptr(psi), ptr(y), stream_handle(stream)))
 
