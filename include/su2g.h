@@ -278,7 +278,10 @@ int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const 
  * eigenvector check every 4 steps with early exit.  psi (device) is the start
  * vector on entry and the normalised ground state on exit; *energy receives
  * the eigenvalue (without the reference's -1000 print offset); *nmatvec, if
- * not NULL, the number of H_eff applications. */
+ * not NULL, the number of H_eff applications.  Each Lanczos step (matvec,
+ * orthogonalisation, normalisation, every scalar on the device) runs as a CUDA
+ * graph captured on the plan's first solve and replayed by later ones; the
+ * host reads back the step's coefficients only (one copy per step). */
 int su2g_lanczos(su2g_heff_plan* plan, double* psi, int mlanc, double* energy, int* nmatvec, void* stream);
 
 /* -------------------------------------------------------------- BLAS-1 -- */

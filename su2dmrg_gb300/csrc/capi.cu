@@ -75,6 +75,22 @@ struct su2g_heff_plan {
   std::vector<const double*> proj_vec;
   std::vector<double> proj_w;
   double* d_proj = nullptr;  // dot scratch, reduction_scratch_doubles() per projector
+  // graph-captured Lanczos steps: lanc_step[m] produces Krylov vector m
+  // (matvec, orthogonalisation, normalisation), lanc_last[m] the final
+  // matvec and alpha; captured on cap_stream for this plan's Krylov buffers
+  std::vector<cudaGraphExec_t> lanc_step, lanc_last;
+  cudaStream_t cap_stream = nullptr;
+  double* d_lcoef = nullptr;  // alpha[0..), beta[0..), reorthogonalisation and norm scratch
+  int lcoef_m = 0;            // largest mlanc the coefficient layout serves
+
+  void drop_graphs() {
+    for (cudaGraphExec_t g : lanc_step)
+      if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t g : lanc_last)
+      if (g) cudaGraphExecDestroy(g);
+    lanc_step.clear();
+    lanc_last.clear();
+  }
 
   void release() {
     cudaFree(d_seg1);
@@ -100,6 +116,11 @@ struct su2g_heff_plan {
     cudaFree(d_err);
     cudaFree(d_proj);
     d_proj = nullptr;
+    drop_graphs();
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
+    cudaFree(d_lcoef);
+    d_lcoef = nullptr;
     d_seg1 = d_seg2 = nullptr;
     d_tile1 = d_tile2 = nullptr;
     d_scratch = d_krylov = d_red = nullptr;
@@ -154,6 +175,8 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0], w.rows_pass[0], b, p->d_packed, p->d_exps,
                             nullptr);
   if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  // the GEMM's one-time setup happens here, never inside a graph capture
+  if (e == cudaSuccess) e = su2g::oz::prepare_ozaki_gemm(p->S);
   return e;
 }
 }  // namespace
@@ -503,6 +526,7 @@ int su2g_heff_plan_add_projector(su2g_heff_plan* p, const double* o, double weig
   const int ns = su2g::reduction_scratch_doubles();
   double* d = nullptr;
   SU2G_CUDA(cudaMalloc((void**)&d, (p->proj_vec.size() + 1) * ns * sizeof(double)));
+  p->drop_graphs();  // captured Lanczos steps lack the new projector
   cudaFree(p->d_proj);
   p->d_proj = d;
   p->proj_vec.push_back(o);
@@ -678,6 +702,69 @@ struct LanczosCtx {
     cudaError_t e = cudaMemcpyAsync(y, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
     return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos copy");
   }
+
+  // ---- device-side coefficients: alpha[j], beta[j], q[j] (reorthogonalisation), nn ----
+  int M() const { return p->lcoef_m; }
+  double* alpha(int j) { return p->d_lcoef + j; }
+  double* beta(int j) { return p->d_lcoef + M() + 1 + j; }
+  double* q(int j) { return p->d_lcoef + 2 * (M() + 1) + j; }
+  double* nnd() { return p->d_lcoef + 3 * (M() + 1); }
+
+  // Enqueues the Lanczos step that produces ff[m] on stream s (lanczos_su2.cpp:136-142
+  // for m = 1, :156-173 for m >= 2): matvec, alpha[m-1], the two three-term
+  // updates, full reorthogonalisation against ff[0..m-1], beta[m] and the
+  // normalisation -- the same kernels in the same order as the host-driven
+  // sequence, with every scalar kept on the device.
+  cudaError_t enqueue_step(int m, cudaStream_t s) {
+    if (su2g_heff_apply(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
+    cudaError_t e = su2g::launch_dot_to(ff(m - 1), ff(m), n, p->d_red, alpha(m - 1), s);
+    if (e == cudaSuccess) e = su2g::launch_axpy_neg_dev(alpha(m - 1), ff(m - 1), ff(m), n, s);
+    if (m >= 2) {
+      if (e == cudaSuccess) e = su2g::launch_axpy_neg_dev(beta(m - 1), ff(m - 2), ff(m), n, s);
+      for (int j = 0; j < m && e == cudaSuccess; ++j) {
+        e = su2g::launch_dot_to(ff(m), ff(j), n, p->d_red, q(j), s);
+        if (e == cudaSuccess) e = su2g::launch_axpy_neg_dev(q(j), ff(j), ff(m), n, s);
+      }
+    }
+    if (e == cudaSuccess) e = su2g::launch_dot_to(ff(m), ff(m), n, p->d_red, nnd(), s);
+    if (e == cudaSuccess) e = su2g::launch_normalize_dev(nnd(), ff(m), n, beta(m), s);
+    return e;
+  }
+  // the final matvec and its alpha (lanczos_su2.cpp:189-194)
+  cudaError_t enqueue_last(int m, cudaStream_t s) {
+    if (su2g_heff_apply(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
+    return su2g::launch_dot_to(ff(m - 1), ff(m), n, p->d_red, alpha(m - 1), s);
+  }
+  // runs a step as a CUDA graph, captured on first use
+  int run_graph(bool last, int m) {
+    std::vector<cudaGraphExec_t>& v = last ? p->lanc_last : p->lanc_step;
+    if ((int)v.size() <= m) v.resize(m + 1, nullptr);
+    if (!v[m]) {
+      if (!p->cap_stream) SU2G_CUDA(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+      SU2G_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t e = last ? enqueue_last(m, p->cap_stream) : enqueue_step(m, p->cap_stream);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(p->cap_stream, &g);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e != cudaSuccess ? e : e2, "lanczos graph capture");
+      }
+      const cudaError_t e3 = cudaGraphInstantiate(&v[m], g, 0);
+      cudaGraphDestroy(g);
+      if (e3 != cudaSuccess) {
+        v[m] = nullptr;
+        return cuda_fail(e3, "lanczos graph instantiate");
+      }
+    }
+    ++nmatvec;
+    SU2G_CUDA(cudaGraphLaunch(v[m], st));
+    return SU2G_OK;
+  }
+  int fetch(const double* d, double* h, int count) {
+    cudaError_t e = cudaMemcpyAsync(h, d, count * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos fetch");
+  }
   // vout = sum_j z[j] ff[j]  (lanczos_su2::compute_eigenvector, lanczos_su2.cpp:262-279)
   int combine(const std::vector<double>& z, int m, double* vout) {
     int rc = copy(ff(0), vout);
@@ -712,6 +799,7 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
   if (mlanc > n) mlanc = (int)n + 1;  // dmrg_su2.cpp:532
   const int need = mlanc + 2;         // ff[0..mlanc] + one work vector
   if (p->krylov_vectors < need) {
+    p->drop_graphs();  // captured with the old buffers
     cudaFree(p->d_krylov);
     p->d_krylov = nullptr;
     p->krylov_vectors = 0;
@@ -719,10 +807,24 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
     p->krylov_vectors = need;
   }
   if (!p->d_red) SU2G_CUDA(cudaMalloc((void**)&p->d_red, su2g::reduction_scratch_doubles() * sizeof(double)));
+  if (p->lcoef_m < mlanc) {
+    p->drop_graphs();
+    cudaFree(p->d_lcoef);
+    p->d_lcoef = nullptr;
+    p->lcoef_m = 0;
+    SU2G_CUDA(cudaMalloc((void**)&p->d_lcoef, (size_t)(3 * (mlanc + 1) + 1) * sizeof(double)));
+    p->lcoef_m = mlanc;
+  }
   LanczosCtx L{p, (cudaStream_t)stream, n};
   const double tol = 1.e-6;  // lanczos_su2.cpp:128
   std::vector<double> aal(mlanc, 0.0), nnl(mlanc + 1, 0.0), eig, z;
   int rc;
+  // alpha[0..m-1] and beta[1..m] to the host (one copy each)
+  auto fetch_coefs = [&](int m) -> int {
+    int r = L.fetch(L.alpha(0), aal.data(), m);
+    if (!r && m >= 1) r = L.fetch(L.beta(1), nnl.data() + 1, m);
+    return r;
+  };
   auto tridiag = [&](int m) {  // lanczos_su2::diatridiag (lanczos_su2.cpp:237-259)
     std::vector<double> d(aal.begin(), aal.begin() + m), e(m > 1 ? m - 1 : 0);
     for (int i = 0; i + 1 < m; ++i) e[i] = nnl[i + 1];
@@ -745,39 +847,24 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
 
   // ff[0] = normalised start vector (lanczos_su2.cpp:45-46)
   if ((rc = L.copy(psi, L.ff(0)))) return rc;
-  double nn;
-  if ((rc = L.dot(L.ff(0), L.ff(0), &nn))) return rc;
-  if ((rc = L.scale(1.0 / std::sqrt(nn), L.ff(0)))) return rc;
+  SU2G_CUDA(su2g::launch_dot_to(L.ff(0), L.ff(0), n, p->d_red, L.nnd(), L.st));
+  SU2G_CUDA(su2g::launch_normalize_dev(L.nnd(), L.ff(0), n, L.beta(0), L.st));
   // first step (lanczos_su2.cpp:136-142)
-  if ((rc = L.matvec(L.ff(0), L.ff(1)))) return rc;
-  if ((rc = L.dot(L.ff(0), L.ff(1), &aal[0]))) return rc;
-  if ((rc = L.axpy(-aal[0], L.ff(0), L.ff(1)))) return rc;
-  if ((rc = L.dot(L.ff(1), L.ff(1), &nn))) return rc;
-  nnl[1] = std::sqrt(nn);
-  if ((rc = L.scale(1.0 / nnl[1], L.ff(1)))) return rc;
+  if ((rc = L.run_graph(false, 1))) return rc;
   if (mlanc == 2) {  // lanczos_su2.cpp:143-154
+    if ((rc = fetch_coefs(1))) return rc;
     if (nnl[1] < tol) {
       tridiag(1);
       return finish(1, false);
     }
-    if ((rc = L.matvec(L.ff(1), L.ff(2)))) return rc;
-    if ((rc = L.dot(L.ff(1), L.ff(2), &aal[1]))) return rc;
+    if ((rc = L.run_graph(true, 2))) return rc;
+    if ((rc = fetch_coefs(2))) return rc;
     tridiag(2);
     return finish(2, false);
   }
   for (int m = 2; m < mlanc; ++m) {  // lanczos_su2.cpp:155-188
-    if ((rc = L.matvec(L.ff(m - 1), L.ff(m)))) return rc;
-    if ((rc = L.dot(L.ff(m - 1), L.ff(m), &aal[m - 1]))) return rc;
-    if ((rc = L.axpy(-aal[m - 1], L.ff(m - 1), L.ff(m)))) return rc;
-    if ((rc = L.axpy(-nnl[m - 1], L.ff(m - 2), L.ff(m)))) return rc;
-    for (int j = 0; j < m; ++j) {  // full reorthogonalisation
-      double q;
-      if ((rc = L.dot(L.ff(m), L.ff(j), &q))) return rc;
-      if ((rc = L.axpy(-q, L.ff(j), L.ff(m)))) return rc;
-    }
-    if ((rc = L.dot(L.ff(m), L.ff(m), &nn))) return rc;
-    nnl[m] = std::sqrt(nn);
-    if ((rc = L.scale(1.0 / nnl[m], L.ff(m)))) return rc;
+    if ((rc = L.run_graph(false, m))) return rc;
+    if ((rc = fetch_coefs(m))) return rc;
     tridiag(m);
     if (nnl[m] < tol) return finish(m, true);
     if (m % 4 == 0) {
@@ -794,8 +881,8 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
     }
   }
   // final step (lanczos_su2.cpp:189-194)
-  if ((rc = L.matvec(L.ff(mlanc - 1), L.ff(mlanc)))) return rc;
-  if ((rc = L.dot(L.ff(mlanc - 1), L.ff(mlanc), &aal[mlanc - 1]))) return rc;
+  if ((rc = L.run_graph(true, mlanc))) return rc;
+  if ((rc = fetch_coefs(mlanc))) return rc;
   tridiag(mlanc);
   return finish(mlanc, true);
 }

@@ -20,6 +20,12 @@ cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* se
 int reduction_scratch_doubles();
 cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* scratch, cudaStream_t stream);
 cudaError_t launch_axpy(double alpha, const double* x, double* y, int64_t n, cudaStream_t stream);
+// the same reductions and updates with their scalars on the device (graph-captured Lanczos):
+// *out = x . y;  y -= (*c) x;  b = sqrt(*nn), *b_out = b, x *= 1 / b
+cudaError_t launch_dot_to(const double* x, const double* y, int64_t n, double* scratch, double* out,
+                          cudaStream_t stream);
+cudaError_t launch_axpy_neg_dev(const double* c, const double* x, double* y, int64_t n, cudaStream_t stream);
+cudaError_t launch_normalize_dev(const double* nn, double* x, int64_t n, double* b_out, cudaStream_t stream);
 cudaError_t launch_scale(double alpha, double* x, int64_t n, cudaStream_t stream);
 // y += alpha * (*scale) * x with the scale read on the device (combine.cu)
 cudaError_t launch_axpy_dev(double alpha, const double* scale, const double* x, double* y, int64_t n,
@@ -31,6 +37,9 @@ struct OzSeg;
 struct OzTile;
 struct RedTile;
 cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaStream_t stream);
+// one-time per-process setup of the GEMM kernel (function attributes, SM count),
+// done before any launch is captured into a graph
+cudaError_t prepare_ozaki_gemm(int S);
 // row-exponent pass (when rows_pass) + digit pass: 1 or 2 kernels, none for nunits == 0
 cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, bool rows_pass,
                         const Bases& bases, uint8_t* packed, int* exps, cudaStream_t stream);

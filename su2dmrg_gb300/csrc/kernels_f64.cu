@@ -186,6 +186,49 @@ cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* scra
   return cudaGetLastError();
 }
 
+cudaError_t launch_dot_to(const double* x, const double* y, int64_t n, double* scratch, double* out,
+                          cudaStream_t stream) {
+  dot_partial<<<kRedBlocks, kRedThreads, 0, stream>>>(x, y, n, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dot_final<<<1, kRedThreads, 0, stream>>>(scratch, kRedBlocks, out);
+  return cudaGetLastError();
+}
+
+// y -= (*c) x, the coefficient read on the device
+__global__ void axpy_neg_dev_kernel(const double* __restrict__ c, const double* __restrict__ x, double* __restrict__ y,
+                                    int64_t n) {
+  const double a = -*c;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+
+// b = sqrt(*nn), *b_out = b, x *= 1 / b
+__global__ void normalize_dev_kernel(const double* __restrict__ nn, double* __restrict__ x, int64_t n,
+                                     double* __restrict__ b_out) {
+  const double b = sqrt(*nn);
+  const double f = 1.0 / b;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *b_out = b;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= f;
+}
+
+cudaError_t launch_axpy_neg_dev(const double* c, const double* x, double* y, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4 * 152 * 4) blocks = 4 * 152 * 4;
+  axpy_neg_dev_kernel<<<blocks, 256, 0, stream>>>(c, x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_normalize_dev(const double* nn, double* x, int64_t n, double* b_out, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4 * 152 * 4) blocks = 4 * 152 * 4;
+  normalize_dev_kernel<<<blocks, 256, 0, stream>>>(nn, x, n, b_out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_axpy(double alpha, const double* x, double* y, int64_t n, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   int blocks = (int)((n + 255) / 256);

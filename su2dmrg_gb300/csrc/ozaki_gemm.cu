@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.hpp"
 #include "ozaki.hpp"
@@ -453,34 +454,39 @@ int gemm_smem_bytes(int S) {
   return 0;
 }
 
+namespace {
+int g_sms = 0;            // one resident CTA per SM (shared memory and TMEM): a persistent grid
+bool g_prepared[9] = {};  // per S
+std::mutex g_prep_mu;
+}  // namespace
+
+cudaError_t prepare_ozaki_gemm(int S) {
+  if (S != 6 && S != 7) return cudaErrorInvalidValue;
+  std::lock_guard<std::mutex> lock(g_prep_mu);
+  if (g_prepared[S]) return cudaSuccess;
+  int dev = 0, n = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  g_sms = n > 0 ? n : 148;
+  const int smem = gemm_smem_bytes(S);
+  e = S == 6 ? cudaFuncSetAttribute(ozaki_gemm<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+             : cudaFuncSetAttribute(ozaki_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) g_prepared[S] = true;
+  return e;
+}
+
 cudaError_t launch_ozaki_gemm(int S, const OzTile* tiles, int ntiles, const OzSeg* segs, const uint8_t* packed,
                               int* exps, const Bases& bases, int* err, cudaStream_t stream) {
   if (ntiles <= 0) return cudaSuccess;
-  static int sms = 0;  // one resident CTA per SM (shared memory and TMEM): a persistent grid
-  if (sms == 0) {
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-      sms = n;
-    if (sms <= 0) sms = 148;
-  }
-  const int grid = ntiles < sms ? ntiles : sms;
-  const int smem = gemm_smem_bytes(S);
-  cudaError_t e = cudaSuccess;
-  switch (S) {
-    case 6:
-      e = cudaFuncSetAttribute(ozaki_gemm<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess)
-        ozaki_gemm<6><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
-      break;
-    case 7:
-      e = cudaFuncSetAttribute(ozaki_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e == cudaSuccess)
-        ozaki_gemm<7><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
-      break;
-    default:
-      return cudaErrorInvalidValue;
-  }
+  cudaError_t e = prepare_ozaki_gemm(S);
   if (e != cudaSuccess) return e;
+  const int grid = ntiles < g_sms ? ntiles : g_sms;
+  const int smem = gemm_smem_bytes(S);
+  if (S == 6)
+    ozaki_gemm<6><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
+  else
+    ozaki_gemm<7><<<grid, kThreads, smem, stream>>>(tiles, ntiles, segs, packed, exps, exps, bases, err);
   return cudaGetLastError();
 }
 

@@ -107,3 +107,36 @@ def test_idmrg_projector(oracle, torch_cuda, path):
     plan.apply(psi, y)
     want = yref - w * np.dot(o, vx) * o
     assert np.linalg.norm(y.cpu().numpy() - want) <= 1e-12 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("path", PATHS[:1])
+def test_lanczos_graph_replay_and_projector(oracle, torch_cuda, path):
+    """su2g_lanczos runs each Lanczos step as a captured CUDA graph: a second
+    solve on the same plan replays the graphs and is bit-identical; a
+    projector added afterwards invalidates them, and the new solve matches
+    the oracle's lanczos1 on H - w |o><o| (1e-10 relative)."""
+    g = np.load(path)
+    plan, vs, vx, yref = _plan(oracle, torch_cuda, g, 0)
+    rng = np.random.default_rng(11)
+    start = rng.standard_normal(vx.size)
+    runs = []
+    for _ in range(2):
+        psi = _dev(torch_cuda, start)
+        e, nmv = plan.lanczos(psi, mlanc=5)
+        runs.append((e, nmv, psi.cpu().numpy()))
+    assert runs[0][0] == runs[1][0] and runs[0][1] == runs[1][1]
+    assert np.array_equal(runs[0][2], runs[1][2])
+
+    o = vx / np.linalg.norm(vx)
+    w = 7.5
+    plan.add_projector(_dev(torch_cuda, o), w)
+    psi = _dev(torch_cuda, start)
+    e, _ = plan.lanczos(psi, mlanc=5)
+    _, _, _, _, T, terms, hl, hr = idmrg_case.load(oracle, g)
+    tl = []
+    for coef, left, right in terms:
+        L, R = idmrg_case.combine_host(oracle, T, left), idmrg_case.combine_host(oracle, T, right)
+        tl.append((L[0], L[1], R[0], R[1], coef))
+    prob = oracle.HeffProblem(vs, tl, hl, hr)
+    e_or, _, _ = oracle.lanczos1(lambda v: oracle.heff_apply(prob, v) - w * np.dot(o, v) * o, start.copy(), 5)
+    assert abs(e - e_or) <= 1e-10 * abs(e_or)
