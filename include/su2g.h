@@ -270,6 +270,36 @@ int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const 
              const int* tv_desc, double p2, int max_dcut, int* bond, int bond_cap, double* wout, int wout_cap,
              int* dout, double* tu, int64_t tu_cap, double* tv, int64_t tv_cap, void* stream);
 
+/* ------------------------------------------------------ between steps -- */
+/* wavefunc_transformation(i, flag) (dmrg_su2_omp.cpp:1864-1876) on one MPS
+ * tensor: tensor_su2::right2left_vectran (flag 0, legs (0,1,2) -> (2,0,1))
+ * or left2right_vectran (flag 1, -> (1,2,0)) (tensor_su2.cpp:749-837).  Every
+ * stored block moves to its rotated place with its legs rotated, numbers
+ * unchanged (the canonical CG of the rotated spins, no factor); directions
+ * become (+1, +1, -1).  out (device) has the layout su2g_vectran_layout
+ * reports and the same length as u; out == u.data rotates in place, as the
+ * reference does.  Apply it to uu[i] and to each orth[j][i].  Blocks until
+ * done. */
+int su2g_vectran_layout(su2g_tensor u, int flag, int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap,
+                        int64_t* out_len);
+int su2g_vectran(su2g_tensor u, int flag, double* out, void* stream);
+
+/* dmrg_su2::prepare_input_vector(il, ir, vec) (dmrg_su2_omp.cpp:229-254):
+ * the initial two-site vector of a step from ul = uu[il] and ur = uu[ir]
+ * (device data; legs 0 and 1 of each of one direction, leg 2 the same bond
+ * in both).  vec has two legs, fuse(ul legs 0, 1) and fuse(ur legs 0, 1)
+ * (su2bond::fuse) with the directions of ul leg 0 and ur leg 0, and every
+ * block of equal spins (tensor_su2::makeup_input_vector,
+ * tensor_su2.cpp:2334-2350): block (c, c) = U_L,c U_R,c^T, U the rows of an
+ * MPS tensor's centre-spin-c blocks stacked in the order tensor_su2::fuse
+ * places them, zero where no stored block reaches.  The same call gives the
+ * excited-state vectors overlapvec[j] from ovlp[j][il], ovlp[j][ir].  mode:
+ * SU2G_MODE_* for the block products.  out (device) has the layout
+ * su2g_input_vector_layout reports.  Blocks until done. */
+int su2g_input_vector_layout(su2g_tensor ul, su2g_tensor ur, int* out_desc, int out_desc_cap, int* out_flag,
+                             int out_flag_cap, int64_t* out_len);
+int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double* out, int mode, void* stream);
+
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme
  * (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195, driven as in

@@ -860,3 +860,65 @@ def site_update(kind: str, flag: int, su: Struct, xu, sv: Struct, xv, x=None, si
     for b, mat in acc.items():
         y[off[b]: off[b] + mat.size] = np.asarray(mat).ravel(order="F")
     return Y, y
+
+
+# --------------------------------------------------------------------------
+# Initial vector of a step and the vectran leg rotations
+# (dmrg_su2::prepare_input_vector dmrg_su2_omp.cpp:229-254,
+#  tensor_su2::right2left_vectran / left2right_vectran tensor_su2.cpp)
+# --------------------------------------------------------------------------
+def prepare_input_vector(sl: Struct, xl, sr: Struct, xr):
+    """The two-site vector psi(F_L, F_R) of uu[il] (sl) and uu[ir] (sr): per
+    spin sector c of their shared leg 2, psi_cc = U_L,c U_R,c^T with U the
+    fused-row placements of the blocks (legs 0, 1 fused as tensor_su2::fuse
+    orders them); every diagonal block present (makeup_input_vector, zeros
+    where c is no sector of the shared leg).  Returns (Struct, data)."""
+    fl = fuse(sl.bonds[0], sl.bonds[1])
+    fr = fuse(sr.bonds[0], sr.bonds[1])
+    V = Struct([Bond(sl.bonds[0].dir, fl.angm, fl.dim), Bond(sr.bonds[0].dir, fr.angm, fr.dim)], 0).with_legal_flags()
+    UL, UR = mps_sector_matrices(sl, xl), mps_sector_matrices(sr, xr)
+    off, tot = V.offsets()
+    y = np.zeros(tot)
+    for b in range(V.nten):
+        if not V.flag[b]:
+            continue
+        c = V.block_angm(b)[0]
+        if c in UL and c in UR:
+            blk = UL[c] @ UR[c].T
+            y[off[b]: off[b] + blk.size] = blk.ravel(order="F")
+    return V, y
+
+
+def vectran(s: Struct, x, direction: int):
+    """right2left_vectran (direction 0: legs (0,1,2) -> (2,0,1)) or
+    left2right_vectran (1: -> (1,2,0)): each block's legs rotated, the
+    directions set to (+1, +1, -1), canonical CG kept."""
+    shift = 1 if direction == 0 else 2  # new position of old leg q: (q + shift) % 3
+    bonds = [None] * 3
+    for q in range(3):
+        bonds[(q + shift) % 3] = s.bonds[q]
+    bonds = [Bond(d, list(b.angm), list(b.dim)) for d, b in zip((1, 1, -1), bonds)]
+    out = Struct(bonds, s.locspin)
+    out.flag = np.zeros(out.nten, np.int32)
+    src = _blocks(s, x)
+    dst = {}
+    for b, blk in src.items():
+        secs = []
+        i = b
+        for q in range(3):
+            secs.append(i % len(s.bonds[q].angm))
+            i //= len(s.bonds[q].angm)
+        ns = [0] * 3
+        for q in range(3):
+            ns[(q + shift) % 3] = secs[q]
+        nb = ns[0] + len(bonds[0].angm) * (ns[1] + len(bonds[1].angm) * ns[2])
+        axes = [0] * 3  # new axis k takes old axis axes[k]
+        for q in range(3):
+            axes[(q + shift) % 3] = q
+        dst[nb] = np.transpose(blk, axes)
+        out.flag[nb] = 1
+    off, tot = out.offsets()
+    y = np.zeros(tot)
+    for b, blk in dst.items():
+        y[off[b]: off[b] + blk.size] = blk.ravel(order="F")
+    return out, y

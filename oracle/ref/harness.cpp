@@ -336,6 +336,40 @@ int ref_idmrg_terms(int* ints, int ncap_i, double* dbls, int ncap_d) {
   return (int)g_term_i.size();
 }
 
+// The initial two-site vector of a step from the MPS tensors uu[il] (ul) and
+// uu[ir] (ur): the sequence of dmrg_su2::prepare_input_vector
+// (dmrg_su2_omp.cpp:229-245) on the reference's own objects.
+int ref_prepare_input_vector(const int* dl, const int* fl, const double* xl, const int* dr, const int* fr,
+                             const double* xr) {
+  tensor_su2 ul, ur, tmp1, tmp2, left, rght;
+  build_tensor(ul, dl, fl, xl);
+  build_tensor(ur, dr, fr, xr);
+  su2bond bb[4];
+  ul.get_su2bond(0, bb[0]);
+  ul.get_su2bond(1, bb[1]);
+  ur.get_su2bond(0, bb[2]);
+  ur.get_su2bond(1, bb[3]);
+  tmp1.fuse(bb[0], bb[1]);
+  tmp2.fuse(bb[2], bb[3]);
+  left.overlap_initial(ul, tmp1, 0);
+  rght.overlap_initial(ur, tmp2, 1);
+  rght.take_conjugate(0);
+  g_result.contract(left, 0, rght, 0);
+  g_result.makeup_input_vector();
+  g_sel = &g_result;
+  return g_result.get_nten();
+}
+
+// uu.right2left_vectran() (dir 0) / uu.left2right_vectran() (dir 1), the
+// step of dmrg_su2::wavefunc_transformation (dmrg_su2_omp.cpp:1864-1877)
+int ref_vectran(const int* du, const int* fu, const double* xu, int dir) {
+  build_tensor(g_result, du, fu, xu);
+  if (dir == 0) g_result.right2left_vectran();
+  else g_result.left2right_vectran();
+  g_sel = &g_result;
+  return g_result.get_nten();
+}
+
 // fac_operator_transformation_{left,rght}[j][m][l][i][k][p] (dmrg_su2.cpp:857-890)
 double ref_fac_operator_transformation(int side, int j, int m, int l, int i, int k, int p) {
   return side == 0 ? fac_operator_transformation_left[j][m][l][i][k][p]

@@ -91,6 +91,10 @@ _PROTOS = {
     "su2g_env_validate": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _i, _vp, _vp]),
     "su2g_fac_table": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "su2g_svd": (_i, [_vp, _vp, _vp, _vp, _d, _vp, _d, _i, _vp, _i, _vp, _i, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "su2g_vectran_layout": (_i, [Tensor, _i, _vp, _i, _vp, _i, _vp]),
+    "su2g_vectran": (_i, [Tensor, _i, _vp, _vp]),
+    "su2g_input_vector_layout": (_i, [Tensor, Tensor, _vp, _i, _vp, _i, _vp]),
+    "su2g_prepare_input_vector": (_i, [Tensor, Tensor, _vp, _i, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),
     "su2g_vec_scale": (_i, [_d, _vp, _i64, _vp]),

@@ -293,7 +293,26 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
   return SU2G_OK;
 }
 
-// one-shot environment update: build, run, wait, check, free
+}  // namespace
+
+// one application of a work list on absolute addresses: build, run, wait,
+// check, free
+int su2g::run_work_once(HeffWork&& w, int mode, void* stream) {
+  if (w.tile1.empty() && w.tile2.empty()) return SU2G_OK;
+  su2g_heff_plan* p = nullptr;
+  int rc = plan_from_work(std::move(w), mode, &p);
+  if (rc) return rc;
+  rc = su2g_heff_apply(p, nullptr, nullptr, stream);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  int code = 0;
+  if (!rc && e == cudaSuccess) rc = su2g_heff_plan_status(p, &code);
+  su2g_heff_plan_destroy(p);
+  if (e != cudaSuccess) return cuda_fail(e, "work list");
+  return rc;
+}
+
+namespace {
+// one-shot environment update
 int env_batch_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
                   double* const* outs, int mode, void* stream) {
   if (!outs && nslots > 0) return fail(SU2G_EINVAL, "env: missing output pointers");
@@ -303,16 +322,7 @@ int env_batch_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2
   std::string err;
   int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs, &w, &ys, &err);
   if (rc) return fail(rc, err);
-  su2g_heff_plan* p = nullptr;
-  rc = plan_from_work(std::move(w), mode, &p);
-  if (rc) return rc;
-  rc = su2g_heff_apply(p, nullptr, nullptr, stream);
-  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
-  int code = 0;
-  if (!rc && e == cudaSuccess) rc = su2g_heff_plan_status(p, &code);
-  su2g_heff_plan_destroy(p);
-  if (e != cudaSuccess) return cuda_fail(e, "env update");
-  return rc;
+  return su2g::run_work_once(std::move(w), mode, stream);
 }
 
 int env_batch_layout(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int slot,

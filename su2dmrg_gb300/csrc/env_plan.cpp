@@ -30,7 +30,7 @@ namespace {
 bool same_sectors(const Bond& a, const Bond& b) { return a.angm == b.angm && a.dim == b.dim; }
 bool same_bond(const Bond& a, const Bond& b) { return a.dir == b.dir && same_sectors(a, b); }
 
-int parse(const su2g_tensor& t, int legs, Struct* s, const char* what, std::string* err) {
+int parse(const su2g_tensor& t, int legs, Struct* s, const char* what, std::string* err, bool need_data = true) {
   if (!t.desc) {
     *err = std::string(what) + ": missing desc";
     return SU2G_EINVAL;
@@ -45,15 +45,16 @@ int parse(const su2g_tensor& t, int legs, Struct* s, const char* what, std::stri
     return SU2G_EINVAL;
   }
   s->set_layout(t.flag);
-  if (s->total > 0 && !t.data) {
+  if (need_data && s->total > 0 && !t.data) {
     *err = std::string(what) + ": missing data pointer";
     return SU2G_EINVAL;
   }
   return SU2G_OK;
 }
 
-int parse_dev(const su2g_tensor& t, int legs, Struct* s, uintptr_t* base, const char* what, std::string* err) {
-  int rc = parse(t, legs, s, what, err);
+int parse_dev(const su2g_tensor& t, int legs, Struct* s, uintptr_t* base, const char* what, std::string* err,
+              bool need_data = true) {
+  int rc = parse(t, legs, s, what, err, need_data);
   if (rc) return rc;
   *base = reinterpret_cast<uintptr_t>(t.data);
   if (*base % 8) {
@@ -485,6 +486,91 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
   std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
   std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
   return validate_heff_work(w, err);
+}
+
+int build_input_vector(const su2g_tensor& ul, const su2g_tensor& ur, const double* urt, double* out, Struct* vec,
+                       HeffWork* w, std::string* err) {
+  Struct L, R;
+  uintptr_t lb = 0, rb = 0;
+  int rc = parse_dev(ul, 3, &L, &lb, "input vector: ul", err, out != nullptr);
+  if (!rc) rc = parse_dev(ur, 3, &R, &rb, "input vector: ur", err, out != nullptr);
+  if (rc) return rc;
+  // su2bond::fuse refuses legs of different directions (su2bond.cpp:159-162)
+  if (L.legs[0].dir != L.legs[1].dir || R.legs[0].dir != R.legs[1].dir) {
+    *err = "input vector: legs 0 and 1 of an MPS tensor have different directions";
+    return SU2G_EINVAL;
+  }
+  // vec.contract(left, 0, rght, 0) joins the two centre bonds
+  if (!same_bond(L.legs[2], R.legs[2])) {
+    *err = "input vector: ul and ur do not share their leg 2";
+    return SU2G_EINVAL;
+  }
+  const Bond FL = fuse(L.legs[0], L.legs[1]), FR = fuse(R.legs[0], R.legs[1]);
+  Struct& V = *vec;
+  V = Struct();
+  V.nbond = 2;
+  V.locspin = 0;
+  V.legs[0] = FL;
+  V.legs[0].dir = L.legs[0].dir;
+  V.legs[1] = FR;
+  V.legs[1].dir = R.legs[0].dir;
+  V.nten = FL.n() * FR.n();
+  V.set_layout(nullptr);  // makeup_input_vector: every block of equal spins
+  *w = HeffWork();
+  if (!out) return SU2G_OK;
+  const uintptr_t ob = reinterpret_cast<uintptr_t>(out), tb = reinterpret_cast<uintptr_t>(urt);
+  if (ob % 8 || tb % 8 || (R.total > 0 && !urt)) {
+    *err = "input vector: misaligned or missing buffer";
+    return SU2G_EINVAL;
+  }
+  const Bond& C = L.legs[2];
+  for (int k = 0; k < C.n(); ++k) {
+    const int c = C.angm[k], dc = C.dim[k];
+    const int i = FL.sector_of(c), j = FR.sector_of(c);
+    if (i < 0 || j < 0) continue;
+    const int vb = i + FL.n() * j, ldc = FL.dim[i];
+    for (int r1 = 0; r1 < R.legs[1].n(); ++r1)
+      for (int r0 = 0; r0 < R.legs[0].n(); ++r0) {
+        const int br = r0 + R.legs[0].n() * (r1 + R.legs[1].n() * k);
+        if (!R.flag[br]) continue;
+        const int col = fused_row(R.legs[0], R.legs[1], c, r0, r1);
+        const int nr = R.legs[0].dim[r0] * R.legs[1].dim[r1];
+        for (int l1 = 0; l1 < L.legs[1].n(); ++l1)
+          for (int l0 = 0; l0 < L.legs[0].n(); ++l0) {
+            const int bl = l0 + L.legs[0].n() * (l1 + L.legs[1].n() * k);
+            if (!L.flag[bl]) continue;
+            const int row = fused_row(L.legs[0], L.legs[1], c, l0, l1);
+            const int ml = L.legs[0].dim[l0] * L.legs[1].dim[l1];
+            if (row < 0 || col < 0) {
+              *err = "input vector: stored block outside its fused sector";
+              return SU2G_EINVAL;
+            }
+            GemmSeg g;
+            g.a = abs_off(lb, L.offset[bl]);
+            g.a_buf = kBufAbs;
+            g.a_len = (int64_t)ml * dc;
+            g.lda = ml;
+            g.transA = 0;
+            g.b = abs_off(tb, R.offset[br]);
+            g.b_buf = kBufAbs;
+            g.b_len = (int64_t)dc * nr;
+            g.ldb = dc;
+            g.K = dc;
+            g.alpha = 1.0;
+            const int seg0 = (int)w->seg2.size();
+            w->seg2.push_back(g);
+            const int64_t coff = abs_off(ob, V.offset[vb] + row + (int64_t)col * ldc);
+            const int64_t clen = (int64_t)(nr - 1) * ldc + ml;
+            add_tiles(w->tile2, coff, clen, kBufAbs, ldc, ml, nr, seg0, 1, dc);
+            w->blk2.push_back(OutBlock{coff, clen, kBufAbs, ldc, ml, nr, seg0, 1});
+            w->flops += 2.0 * ml * (double)nr * dc;
+            w->max_k = std::max<int64_t>(w->max_k, dc);
+          }
+      }
+  }
+  auto heavier = [](const GemmTile& x, const GemmTile& y) { return x.kwork > y.kwork; };
+  std::stable_sort(w->tile2.begin(), w->tile2.end(), heavier);
+  return validate_heff_work(*w, err);
 }
 
 }  // namespace su2g

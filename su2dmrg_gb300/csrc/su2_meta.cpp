@@ -525,4 +525,16 @@ void dsort2(int n, double* key, int* tag) {
       }
 }
 
+int fused_row(const Bond& b0, const Bond& b1, int c, int j0, int j1) {
+  int pos = 0;
+  for (int q1 = 0; q1 < b1.n(); ++q1)
+    for (int q0 = 0; q0 < b0.n(); ++q0) {
+      const int a = b0.angm[q0], s = b1.angm[q1];
+      if (c < std::abs(a - s) || c > a + s || (a + s - c) % 2) continue;
+      if (q0 == j0 && q1 == j1) return pos;
+      pos += b0.dim[q0] * b1.dim[q1];
+    }
+  return -1;
+}
+
 }  // namespace su2g

@@ -95,6 +95,12 @@ double fac_operator_transformation(int side, int j, int m, int l, int i, int k, 
 double fac_operator_onsite(int side, int j, int m, int l, int i, int q);
 double fac_operator_pairup(int side, int j, int i, int k, int m, int q);
 double fac_permutation(int side, int i, int j, int k, int l, int t);
+// First row of the (b0 sector j0, b1 sector j1) sub-block inside the fused
+// sector 2j = c of fuse(b0, b1), in the order tensor_su2::fuse places them
+// (tensor_su2.cpp:878-900): b1 sectors outer, b0 sectors inner, dim0 * dim1
+// rows each (b0 fastest); -1 if the pair does not reach c.
+int fused_row(const Bond& b0, const Bond& b1, int c, int j0, int j1);
+
 // tensor::make_singlet (tensor.cpp:1331-1350), (j+1) x (j+1) column-major
 void make_singlet(int j, double* out);
 

@@ -221,21 +221,6 @@ void sector_svd(Ctx& c, const double* blk, int m, int n, double p1, double p2, i
 
 }  // namespace
 
-// first row of the (a, sigma) sub-block inside fused sector 2j = c, in the
-// order tensor_su2::fuse places them (tensor_su2.cpp:878-900): sigma sectors
-// outer, bond sectors inner, d_a * d_sigma rows each
-int fused_row(const su2g::Bond& b0, const su2g::Bond& b1, int c, int j0, int j1) {
-  int pos = 0;
-  for (int q1 = 0; q1 < b1.n(); ++q1)
-    for (int q0 = 0; q0 < b0.n(); ++q0) {
-      const int a = b0.angm[q0], s = b1.angm[q1];
-      if (c < std::abs(a - s) || c > a + s || (a + s - c) % 2) continue;
-      if (q0 == j0 && q1 == j1) return pos;
-      pos += b0.dim[q0] * b1.dim[q1];
-    }
-  return -1;
-}
-
 bool same_sectors(const su2g::Bond& a, const su2g::Bond& b) { return a.angm == b.angm && a.dim == b.dim; }
 
 extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const int* tu_desc, double p1,
@@ -339,7 +324,7 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
       const Sector* src = nullptr;
       for (const Sector& s : secs)
         if (P.legs[0].angm[s.i] == ang) src = &s;
-      const int r0 = fused_row(O.legs[0], O.legs[1], ang, sec[0], sec[1]);
+      const int r0 = su2g::fused_row(O.legs[0], O.legs[1], ang, sec[0], sec[1]);
       const int rows = O.legs[0].dim[sec[0]] * O.legs[1].dim[sec[1]];
       if (!src || r0 < 0) return fail(SU2G_EINVAL, "svd: internal placement error");
       const int ld = side ? src->n : src->m;

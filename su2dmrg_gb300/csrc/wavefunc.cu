@@ -1,0 +1,283 @@
+// The wave-function moves between two steps of a sweep:
+//   * wavefunc_transformation (dmrg_su2_omp.cpp:1864-1876): the MPS tensor
+//     next to the new centre changes which of its legs are fused into the
+//     third, tensor_su2::right2left_vectran / left2right_vectran
+//     (tensor_su2.cpp:749-837).  Each block keeps its numbers: its legs are
+//     rotated and its CG is replaced by the canonical one of the rotated spins
+//     (make_cgc), with no recoupling factor, then the directions are set to
+//     (+1, +1, -1).  A rotation of the legs of a column-major block is a
+//     matrix transpose: right2left sees a block as (d0 d1) x d2, left2right
+//     as d0 x (d1 d2).
+//   * prepare_input_vector (dmrg_su2_omp.cpp:229-254): the initial two-site
+//     vector of the step, per centre spin c the product U_L,c U_R,c^T of the
+//     two MPS tensors' fused-row matrices (the fuse, overlap_initial and
+//     contract of the reference meet in this one product, with canonical CG
+//     and factor 1).  U_R,c^T is the right2left rotation of ur's blocks, so
+//     the call transposes ur once and runs the products as a work list of the
+//     block-sparse engine (FP64 or split BF16).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "env_plan.hpp"
+#include "kernels.hpp"
+#include "su2_meta.hpp"
+#include "su2g.h"
+
+namespace {
+
+int fail(int code, const std::string& msg) { return su2g::set_last_error(code, msg); }
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? SU2G_ENOMEM : SU2G_ECUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      n = v;
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+// one block to transpose: src rows x cols (column-major) -> dst cols x rows
+struct TrItem {
+  const double* src;
+  double* dst;
+  int rows, cols;
+  int tiles_r;     // 32-row tiles along rows
+  int64_t tile0;   // first global tile index of this block
+};
+
+constexpr int kTr = 32;          // tile edge
+constexpr int kTrThreads = 256;  // 32 x 8
+
+// Global tiles are walked with a grid-stride loop; a CTA finds its block by a
+// binary search of the tile prefix.  Reads are coalesced along the source
+// column, writes along the destination column, through a padded 32 x 33 tile.
+__global__ void __launch_bounds__(kTrThreads) transpose_blocks_kernel(const TrItem* __restrict__ items, int nitems,
+                                                                      int64_t ntiles) {
+  __shared__ double tile[kTr][kTr + 1];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].tile0 <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const TrItem it = items[lo];
+    const int64_t local = t - it.tile0;
+    const int r0 = (int)(local % it.tiles_r) * kTr, c0 = (int)(local / it.tiles_r) * kTr;
+    __syncthreads();  // the previous tile's reads of `tile` are done
+#pragma unroll
+    for (int q = 0; q < kTr; q += 8) {
+      const int r = r0 + tx, c = c0 + ty + q;
+      if (r < it.rows && c < it.cols) tile[ty + q][tx] = it.src[r + (int64_t)c * it.rows];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kTr; q += 8) {
+      const int c = c0 + tx, r = r0 + ty + q;  // dst (c, r) at dst[c + r * cols]
+      if (r < it.rows && c < it.cols) it.dst[c + (int64_t)r * it.cols] = tile[tx][ty + q];
+    }
+  }
+}
+
+// Runs the transposes of `items` (host list; tile0 filled here) on `st`.
+cudaError_t launch_transposes(std::vector<TrItem>& items, cudaStream_t st) {
+  std::vector<TrItem> live;
+  int64_t ntiles = 0;
+  for (TrItem it : items) {
+    if (it.rows <= 0 || it.cols <= 0) continue;
+    it.tiles_r = (it.rows + kTr - 1) / kTr;
+    it.tile0 = ntiles;
+    ntiles += (int64_t)it.tiles_r * ((it.cols + kTr - 1) / kTr);
+    live.push_back(it);
+  }
+  if (live.empty()) return cudaSuccess;
+  TrItem* d_items = nullptr;
+  const size_t bytes = live.size() * sizeof(TrItem);
+  cudaError_t e = cudaMallocAsync((void**)&d_items, bytes, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(d_items, live.data(), bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 8);
+    transpose_blocks_kernel<<<grid, kTrThreads, 0, st>>>(d_items, (int)live.size(), ntiles);
+    e = cudaGetLastError();
+  }
+  // the host list must outlive the copy
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(d_items, st);
+  return e;
+}
+
+int write_layout(const su2g::Struct& s, int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap,
+                 int64_t* out_len, const char* what) {
+  std::vector<int> d = {s.nbond, s.locspin};
+  for (int l = 0; l < s.nbond; ++l) {
+    d.push_back(s.legs[l].dir);
+    d.push_back(s.legs[l].n());
+    for (int a : s.legs[l].angm) d.push_back(a);
+    for (int x : s.legs[l].dim) d.push_back(x);
+  }
+  if (!out_desc || !out_flag || (int)d.size() > out_desc_cap || s.nten > out_flag_cap)
+    return fail(SU2G_EINVAL, std::string(what) + ": output arrays too small");
+  std::copy(d.begin(), d.end(), out_desc);
+  std::copy(s.flag.begin(), s.flag.end(), out_flag);
+  if (out_len) *out_len = s.total;
+  return SU2G_OK;
+}
+
+// Structure of the rotated tensor and, per stored block, its transpose.
+// flag 0 = right2left (legs (0,1,2) -> (2,0,1)), 1 = left2right (-> (1,2,0)).
+int vectran_struct(const su2g_tensor& u, int flag, su2g::Struct* in, su2g::Struct* out, std::string* err) {
+  if (flag != 0 && flag != 1) {
+    *err = "vectran: flag must be 0 (right2left) or 1 (left2right)";
+    return SU2G_EINVAL;
+  }
+  if (!u.desc || !in->parse(u.desc, err)) {
+    *err = "vectran: " + *err;
+    return SU2G_EINVAL;
+  }
+  if (in->nbond != 3) {
+    *err = "vectran: a 3-leg tensor expected";
+    return SU2G_EINVAL;
+  }
+  in->set_layout(u.flag);
+  const int shift = flag == 0 ? 1 : 2;  // old leg q -> new leg (q + shift) % 3
+  *out = su2g::Struct();
+  out->nbond = 3;
+  out->locspin = in->locspin;
+  for (int q = 0; q < 3; ++q) out->legs[(q + shift) % 3] = in->legs[q];
+  out->legs[0].dir = 1;
+  out->legs[1].dir = 1;
+  out->legs[2].dir = -1;
+  out->nten = in->nten;
+  std::vector<int> f(out->nten, 0);
+  for (int b = 0; b < in->nten; ++b) {
+    if (!in->flag[b]) continue;
+    int sec[3], ns[3];
+    in->sectors(b, sec);
+    for (int q = 0; q < 3; ++q) ns[(q + shift) % 3] = sec[q];
+    f[out->index(ns)] = 1;
+  }
+  out->set_layout(f.data());
+  return SU2G_OK;
+}
+
+// transposes of every stored block of `in` into its rotated place in `out`
+std::vector<TrItem> vectran_items(const su2g::Struct& in, const su2g::Struct& out, int flag, const double* src,
+                                  double* dst) {
+  const int shift = flag == 0 ? 1 : 2;
+  std::vector<TrItem> items;
+  for (int b = 0; b < in.nten; ++b) {
+    if (!in.flag[b]) continue;
+    int sec[3], ns[3];
+    in.sectors(b, sec);
+    for (int q = 0; q < 3; ++q) ns[(q + shift) % 3] = sec[q];
+    const int d0 = in.block_dim(b, 0), d1 = in.block_dim(b, 1), d2 = in.block_dim(b, 2);
+    TrItem it{};
+    it.src = src + in.offset[b];
+    it.dst = dst + out.offset[out.index(ns)];
+    it.rows = flag == 0 ? d0 * d1 : d0;
+    it.cols = flag == 0 ? d2 : d1 * d2;
+    items.push_back(it);
+  }
+  return items;
+}
+
+}  // namespace
+
+extern "C" int su2g_vectran_layout(su2g_tensor u, int flag, int* out_desc, int out_desc_cap, int* out_flag,
+                                   int out_flag_cap, int64_t* out_len) {
+  su2g::Struct in, out;
+  std::string err;
+  int rc = vectran_struct(u, flag, &in, &out, &err);
+  if (rc) return fail(rc, err);
+  return write_layout(out, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len, "vectran_layout");
+}
+
+extern "C" int su2g_vectran(su2g_tensor u, int flag, double* out, void* stream) {
+  su2g::Struct in, o;
+  std::string err;
+  int rc = vectran_struct(u, flag, &in, &o, &err);
+  if (rc) return fail(rc, err);
+  if (in.total == 0) return SU2G_OK;
+  if (!u.data || !out) return fail(SU2G_EINVAL, "vectran: null data");
+  cudaStream_t st = (cudaStream_t)stream;
+  // in place (the reference rotates uu[i] itself): transpose from a copy
+  const double* src = u.data;
+  double* copy = nullptr;
+  cudaError_t e = cudaSuccess;
+  const bool overlap = out < u.data + in.total && u.data < out + in.total;
+  if (overlap) {
+    e = cudaMallocAsync((void**)&copy, in.total * sizeof(double), st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(copy, u.data, in.total * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    src = copy;
+  }
+  if (e == cudaSuccess) {
+    std::vector<TrItem> items = vectran_items(in, o, flag, src, out);
+    e = launch_transposes(items, st);
+  }
+  if (copy) cudaFreeAsync(copy, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "vectran");
+  return SU2G_OK;
+}
+
+extern "C" int su2g_input_vector_layout(su2g_tensor ul, su2g_tensor ur, int* out_desc, int out_desc_cap,
+                                        int* out_flag, int out_flag_cap, int64_t* out_len) {
+  su2g::Struct v;
+  su2g::HeffWork w;
+  std::string err;
+  int rc = su2g::build_input_vector(ul, ur, nullptr, nullptr, &v, &w, &err);
+  if (rc) return fail(rc, err);
+  return write_layout(v, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len, "input_vector_layout");
+}
+
+extern "C" int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double* out, int mode, void* stream) {
+  su2g::Struct v, R, Rt;
+  su2g::HeffWork w;
+  std::string err;
+  // structures first (argument errors before any device work)
+  int rc = su2g::build_input_vector(ul, ur, nullptr, nullptr, &v, &w, &err);
+  if (rc) return fail(rc, err);
+  if (v.total == 0) return SU2G_OK;
+  if (!out) return fail(SU2G_EINVAL, "prepare_input_vector: null output");
+  rc = vectran_struct(ur, 0, &R, &Rt, &err);
+  if (rc) return fail(rc, err);
+  cudaStream_t st = (cudaStream_t)stream;
+  double* urt = nullptr;  // ur's blocks transposed, at ur's own offsets
+  cudaError_t e = cudaMemsetAsync(out, 0, v.total * sizeof(double), st);
+  if (e == cudaSuccess && R.total > 0) e = cudaMallocAsync((void**)&urt, R.total * sizeof(double), st);
+  if (e == cudaSuccess && R.total > 0) {
+    std::vector<TrItem> items;
+    for (int b = 0; b < R.nten; ++b) {
+      if (!R.flag[b]) continue;
+      TrItem it{};
+      it.src = ur.data + R.offset[b];
+      it.dst = urt + R.offset[b];
+      it.rows = R.block_dim(b, 0) * R.block_dim(b, 1);
+      it.cols = R.block_dim(b, 2);
+      items.push_back(it);
+    }
+    e = launch_transposes(items, st);
+  }
+  if (e == cudaSuccess) {
+    rc = su2g::build_input_vector(ul, ur, urt, out, &v, &w, &err);
+    if (rc) rc = fail(rc, err);
+    else rc = su2g::run_work_once(std::move(w), mode, stream);
+  }
+  if (urt) cudaFreeAsync(urt, st);
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "prepare_input_vector");
+  return rc;
+}

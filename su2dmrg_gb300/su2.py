@@ -484,3 +484,52 @@ def operator_combine(ops, coefs, stream=None):
     y = torch.empty(max(1, n.value), dtype=torch.float64, device=dev)
     check(lib().su2g_operator_combine(len(ops), ctypes.addressof(arr), ptr(c), ptr(y), stream_handle(stream)))
     return out, y
+
+
+def _layout_out(fn, *args) -> Su2Struct:
+    """Calls a *_layout entry point and returns its structure."""
+    desc = np.zeros(4 + 3 * (2 + 2 * 64), np.int32)
+    flags = np.zeros(64 ** 3, np.int32)
+    n = ctypes.c_int64()
+    check(fn(*args, ptr(desc), len(desc), ptr(flags), len(flags), ctypes.addressof(n)))
+    out = _parse_desc(desc)
+    out.flag = flags[: out.nten].copy()
+    return out
+
+
+def vectran_layout(u: Su2Struct, flag: int) -> Su2Struct:
+    """Structure after right2left_vectran (flag 0) / left2right_vectran (1)."""
+    keep = []
+    return _layout_out(lib().su2g_vectran_layout, _tensor(u, None, keep), int(flag))
+
+
+def vectran(u: Su2Struct, xu, flag: int, out=None, stream=None):
+    """wavefunc_transformation of one MPS tensor (device data xu): returns
+    (rotated Su2Struct, device tensor); out=xu rotates in place."""
+    import torch
+
+    keep = []
+    s = vectran_layout(u, flag)
+    y = out if out is not None else torch.empty(max(1, s.size()), dtype=torch.float64, device=xu.device)
+    check(lib().su2g_vectran(_tensor(u, xu, keep), int(flag), ptr(y), stream_handle(stream)))
+    return s, y
+
+
+def input_vector_layout(ul: Su2Struct, ur: Su2Struct) -> Su2Struct:
+    """Structure of prepare_input_vector's two-site vector."""
+    keep = []
+    return _layout_out(lib().su2g_input_vector_layout, _tensor(ul, None, keep), _tensor(ur, None, keep))
+
+
+def prepare_input_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, mode: int = capi.MODE_F64, stream=None):
+    """dmrg_su2::prepare_input_vector from uu[il] = (ul, xl) and uu[ir] =
+    (ur, xr) (device data): returns (Su2Struct, device tensor)."""
+    import torch
+
+    keep = []
+    s = input_vector_layout(ul, ur)
+    y = torch.empty(max(1, s.size()), dtype=torch.float64, device=xl.device)
+    check(lib().su2g_prepare_input_vector(_tensor(ul, xl, keep), _tensor(ur, xr, keep), ptr(y), int(mode),
+                                          stream_handle(stream)))
+    return s, y
+

@@ -414,6 +414,39 @@ def dmrg_runs(L):
     return out
 
 
+def input_vector_cases(L, rng):
+    """prepare_input_vector (the initial two-site vector of a step) and the
+    vectran permutations of wavefunc_transformation, on random MPS tensors."""
+    cases = []
+    specs = [([0, 1, 2, 3], [0, 1, 2, 3, 4], [0, 1, 2, 3], 0.0), ([0, 2, 4, 6], [1, 3, 5, 7], [0, 2, 4, 6], 0.1),
+             ([1, 3, 5], [0, 2, 4, 6], [1, 3, 5], 0.0)]
+    ph = (1, [1], [1])
+    for ci, (sa, sc, sb, drop) in enumerate(specs):
+        da = [int(rng.integers(1, 7)) for _ in sa]
+        dc = [int(rng.integers(1, 7)) for _ in sc]
+        db = [int(rng.integers(1, 7)) for _ in sb]
+        ulb = [(1, sa, da), ph, (-1, sc, dc)]   # uu[il]: (bond, spin, centre bond)
+        urb = [ph, (1, sb, db), (-1, sc, dc)]   # uu[ir]: (spin, bond, centre bond)
+        dl, dr = desc_of(ulb), desc_of(urb)
+        fl = (legal_flags(L, dl) * (rng.random(nten_of(ulb)) >= drop)).astype(np.int32)
+        fr = (legal_flags(L, dr) * (rng.random(nten_of(urb)) >= drop)).astype(np.int32)
+        xl, xr = random_data(ulb, fl, rng), random_data(urb, fr, rng)
+        L.ref_prepare_input_vector(p(dl), p(fl), p(xl), p(dr), p(fr), p(xr))
+        d = np.zeros(1024, np.int32)
+        nd = L.ref_result_desc(p(d))
+        rflag, rx, _ = read_result(L)
+        cases.append(dict(name=f"inputvec_{ci}", dl=dl, fl=fl, xl=xl, dr=dr, fr=fr, xr=xr, rdesc=d[:nd].copy(),
+                          rflag=rflag, rx=rx))
+        for direction in (0, 1):
+            L.ref_vectran(p(dl), p(fl), p(xl), direction)
+            d = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(d))
+            rflag, rx, _ = read_result(L)
+            cases.append(dict(name=f"vectran_{ci}_{direction}", du=dl, fu=fl, xu=xl, dir=np.int32(direction),
+                              rdesc=d[:nd].copy(), rflag=rflag, rx=rx))
+    return cases
+
+
 def idmrg_cases(L):
     """The engine's own H_eff (hamiltonian_vector_multiplication_idmrg) at the
     last two-site step of short runs: real environments, the input vector the
@@ -476,7 +509,8 @@ def main():
     np.savez(os.path.join(HERE, "meta.npz"), **meta_cases(L, rng))
     np.savez_compressed(os.path.join(HERE, "fac_optrans.npz"), **fac_optrans(L))
     np.savez_compressed(os.path.join(HERE, "fac_site.npz"), **fac_site_tables(L))
-    for c in heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng) + site_cases(L, rng):
+    for c in (heff_cases(L, rng) + spin0_cases(L, rng) + env_cases(L, rng) + svd_cases(L, rng) + site_cases(L, rng)
+              + input_vector_cases(L, rng)):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-idmrg" not in sys.argv:

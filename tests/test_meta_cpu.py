@@ -260,3 +260,59 @@ def test_idmrg_work_lists_on_cpu(su2lib, oracle, mode):
             tl.append((L[0], L[1], R[0], R[1], coef))
         r = HeffPlan.validate(vs, tl, (hl[0], hl[1], 1.0), (hr[0], hr[1], 1.0), mode=mode)
         assert r["flops"] > 0
+
+
+def _su2(oracle_struct_desc, flags):
+    from su2dmrg_gb300.su2 import _parse_desc
+
+    s = _parse_desc(oracle_struct_desc)
+    s.flag = np.ascontiguousarray(flags, np.int32)
+    return s
+
+
+@pytest.mark.parametrize("ci", [0, 1, 2])
+def test_input_vector_layout_matches_reference(su2lib, ci):
+    """su2g_input_vector_layout gives the reference's vec structure: fused
+    legs, every equal-spin block present (makeup_input_vector)."""
+    from su2dmrg_gb300.su2 import input_vector_layout
+
+    g = np.load(os.path.join(GOLDEN, f"inputvec_{ci}.npz"))
+    s = input_vector_layout(_su2(g["dl"], g["fl"]), _su2(g["dr"], g["fr"]))
+    assert s.desc().tolist() == g["rdesc"].tolist()
+    assert s.flag.tolist() == g["rflag"].tolist()
+    assert s.size() == len(g["rx"])
+
+
+@pytest.mark.parametrize("ci", [0, 1, 2])
+@pytest.mark.parametrize("direction", [0, 1])
+def test_vectran_layout_matches_reference(su2lib, ci, direction):
+    from su2dmrg_gb300.su2 import vectran_layout
+
+    g = np.load(os.path.join(GOLDEN, f"vectran_{ci}_{direction}.npz"))
+    s = vectran_layout(_su2(g["du"], g["fu"]), direction)
+    assert s.desc().tolist() == g["rdesc"].tolist()
+    assert s.flag.tolist() == g["rflag"].tolist()
+
+
+def test_wavefunc_argument_checks_without_gpu(su2lib):
+    """Structures the reference refuses (fuse of legs of different
+    directions, centre bonds that differ) and a bad vectran flag give
+    SU2G_EINVAL before any device work."""
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300.capi import Su2gError as CheckError
+    from su2dmrg_gb300.su2 import input_vector_layout, vectran_layout
+
+    g = np.load(os.path.join(GOLDEN, "inputvec_0.npz"))
+    ul, ur = _su2(g["dl"], g["fl"]), _su2(g["dr"], g["fr"])
+    bad = _su2(g["dl"], g["fl"])
+    bad.bonds[1] = bad.bonds[1].inverted()
+    with pytest.raises(CheckError, match="directions"):
+        input_vector_layout(bad, ur)
+    other = _su2(g["dr"], g["fr"])
+    b2 = other.bonds[2]
+    other.bonds[2] = type(b2)(b2.dir, list(b2.angm), [d + 1 for d in b2.dim])
+    with pytest.raises(CheckError, match="leg 2"):
+        input_vector_layout(ul, other)
+    with pytest.raises(CheckError, match="flag"):
+        vectran_layout(ul, 2)
+    assert capi.SU2G_EINVAL == 1

@@ -232,3 +232,22 @@ def test_idmrg_heff_matches_reference(oracle, path):
     prob = oracle.HeffProblem(vs, tl, hl, hr)
     y = oracle.heff_apply(prob, vx)
     assert np.linalg.norm(y - yref) <= 1e-12 * np.linalg.norm(yref)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "inputvec_*.npz"))))
+def test_input_vector_matches_reference(oracle, path):
+    g = np.load(path)
+    sl, sr = oracle.struct_from_desc(g["dl"], g["fl"]), oracle.struct_from_desc(g["dr"], g["fr"])
+    out, y = oracle.prepare_input_vector(sl, g["xl"], sr, g["xr"])
+    assert out.desc().tolist() == g["rdesc"].tolist()
+    assert out.flag.tolist() == g["rflag"].tolist()
+    assert np.linalg.norm(y - g["rx"]) <= 1e-14 * np.linalg.norm(g["rx"])
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "vectran_*.npz"))))
+def test_vectran_matches_reference(oracle, path):
+    g = np.load(path)
+    out, y = oracle.vectran(oracle.struct_from_desc(g["du"], g["fu"]), g["xu"], int(g["dir"]))
+    assert out.desc().tolist() == g["rdesc"].tolist()
+    assert out.flag.tolist() == g["rflag"].tolist()
+    assert np.array_equal(y, g["rx"])
