@@ -16,10 +16,17 @@ Printed JSON (rank 0, one line):
   roofline, cpu_baseline, clocks, gpu_launches as documented in DESIGN.md.
 --impl reference times the CPU restatement of the reference's hot path (the
 reference itself is not built on the GPU host) on all host cores.
+
+--row input_vector | vectran | env | svd times one other operation of a site
+step instead, on workloads.synthetic_site_step at the same D, through its C
+ABI call with arguments prepared once (each call blocks; its host planning is
+inside the timed region), with L2 flushed before every call; same JSON keys,
+its own metric.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -46,6 +53,9 @@ def parse():
     ap.add_argument("--D", type=int, default=2000)
     ap.add_argument("--nspin1", type=int, default=18)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--row", default="heff", choices=["heff", "input_vector", "vectran", "env", "svd"],
+                    help="heff (the headline) or another operation of the site step, timed on the "
+                         "D-multiplet site-step workload (workloads.synthetic_site_step)")
     return ap.parse_args()
 
 
@@ -374,10 +384,217 @@ def run_su2g(args):
     return 0
 
 
+def _time_calls(torch, fn, steps, warmup):
+    """Device time of `steps` blocking calls, L2 flushed (256 MB written) before each."""
+    buf = torch.zeros(32 << 20, dtype=torch.float64, device="cuda")
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ts = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(steps):
+            buf.add_(1.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            ts.append(s.elapsed_time(e) / 1e3)
+    return ts, clk.summary()
+
+
+def _cpu_sample(fn, seconds=10.0, max_steps=10):
+    fn()
+    ts, t0 = [], time.perf_counter()
+    while time.perf_counter() - t0 < seconds and len(ts) < max_steps:
+        a = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - a)
+    return float(np.median(ts)), len(ts)
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as o
+
+    o.build()
+    o.set_blas_threads(os.cpu_count() or 1)
+    return o
+
+
+def _oracle_struct(o, s):
+    st = o.Struct([o.Bond(b.dir, list(b.angm), list(b.dim)) for b in s.bonds], s.locspin)
+    st.flag = np.ascontiguousarray(s.flag, np.int32)
+    return st
+
+
+def _gemm_roofline(torch, flops, t, slices, what):
+    if slices:
+        pk, src = bf16_peak()
+        pairs = slices * (slices + 1) // 2
+        ach = pairs * flops / t / 1e12
+        return {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk,
+                "traffic": None, "peak_source": src,
+                "achieved_definition": f"{pairs} BF16 products per FP64 product over the whole call ({what})"}
+    pk = fp64_peak_tflops(torch)
+    ach = flops / t / 1e12
+    return {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk, "traffic": None,
+            "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU",
+            "achieved_definition": f"FP64 FLOPs over the whole call ({what})"}
+
+
+def run_row(args):
+    """One other operation of the site step (--row), single GPU."""
+    import torch
+
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300 import su2 as S
+    from su2dmrg_gb300.workloads import synthetic_heff, synthetic_site_step
+
+    capi.lib()
+    torch.cuda.set_device(0)
+    w = synthetic_site_step(D=args.D, nops=args.nspin1)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    mode = MODES[args.mode]
+    slices = SLICES[args.mode]
+    o = None if args.no_cpu_baseline else _oracle()
+    cores = os.cpu_count() or 1
+    cb = None
+    extra = {}
+    dtype = "f64" if not slices else f"f64 emulated by bf16 x{slices} (fp32 accumulate)"
+    if args.row == "input_vector":
+        (sl, xl), (sr, xr) = w.ul, w.ur
+        dl, dr = dev(xl), dev(xr)
+        vs = S.input_vector_layout(sl, sr)
+        fl, fr = vs.bonds
+        flops = 0.0
+        for k, c in enumerate(sl.bonds[2].angm):
+            if c in fl.angm and c in fr.angm:
+                flops += 2.0 * fl.dim[fl.angm.index(c)] * fr.dim[fr.angm.index(c)] * sl.bonds[2].dim[k]
+        keep = []
+        tl, tr = S._tensor(sl, dl, keep), S._tensor(sr, dr, keep)
+        yv = torch.empty(vs.size(), dtype=torch.float64, device="cuda")
+        # the C-ABI call alone, its arguments prepared once (the structure is known to the caller)
+        ts, clk = _time_calls(torch, lambda: capi.check(capi.lib().su2g_prepare_input_vector(
+            tl, tr, capi.ptr(yv), mode, None)), args.steps, args.warmup)
+        t = float(np.median(ts))
+        metric, unit, hib = f"initial two-site vector TFLOP/s (FP64-equivalent), SU(2) D={args.D}", "TFLOP/s", True
+        value = flops / t / 1e12
+        roof = _gemm_roofline(torch, flops, t, slices, "transpose of ur, planning, pack and GEMM launches")
+        _, yg = S.prepare_input_vector(sl, dl, sr, dr, mode=mode)
+        if o is not None:
+            osl, osr = _oracle_struct(o, sl), _oracle_struct(o, sr)
+            ref = {}
+            tc, n = _cpu_sample(lambda: ref.__setitem__("y", o.prepare_input_vector(osl, xl, osr, xr)[1]))
+            cb = {"value": flops / tc / 1e12, "unit": unit, "cores": cores, "kind": "port",
+                  "sample": f"the full call, oracle (numpy BLAS), median of {n}"}
+            got = yg[: vs.size()].cpu().numpy()
+            extra["rel_err_vs_oracle"] = float(np.linalg.norm(got - ref["y"]) / np.linalg.norm(ref["y"]))
+        config = {"workload": f"synthetic SU(2) MPS pair, D={args.D}, spin-1/2 sites", "mode": args.mode,
+                  "flops_per_step": flops, "vector_doubles": vs.size()}
+    elif args.row == "vectran":
+        su, xu = w.ul
+        d = dev(xu)
+        out = torch.empty_like(d)
+        keep = []
+        tu = S._tensor(su, d, keep)
+        ts, clk = _time_calls(torch, lambda: capi.check(capi.lib().su2g_vectran(tu, 0, capi.ptr(out), None)),
+                              args.steps, args.warmup)
+        nbytes = 16.0 * su.size()
+        t = float(np.median(ts))
+        metric, unit, hib = f"vectran GB/s (right2left, read + write), SU(2) MPS tensor D={args.D}", "GB/s", True
+        value = nbytes / t / 1e9
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        roof = {"bound": "hbm", "achieved": value, "peak": peak, "unit": "GB/s", "frac": value / peak,
+                "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                "achieved_definition": "16 bytes per element over the whole call (one transpose launch)"}
+        dtype = "f64"
+        if o is not None:
+            osu = _oracle_struct(o, su)
+            tc, n = _cpu_sample(lambda: o.vectran(osu, xu, 0))
+            cb = {"value": nbytes / tc / 1e9, "unit": unit, "cores": 1, "kind": "port",
+                  "sample": f"the full call, oracle (numpy), median of {n}"}
+            extra["bit_exact_vs_oracle"] = bool(np.array_equal(out[: su.size()].cpu().numpy(),
+                                                               o.vectran(osu, xu, 0)[1]))
+        config = {"workload": f"synthetic SU(2) MPS tensor, D={args.D}", "elements": su.size()}
+    elif args.row == "env":
+        su, xu = w.uu
+        du = dev(xu)
+        jobs = [{"kind": "transform", "slot": i, "coef": 1.0, "x": (s_, dev(x_))} for i, (s_, x_) in enumerate(w.ops)]
+        jobs.append({"kind": "overlap", "slot": len(w.ops), "coef": 1.0, "x": (w.hh[0], dev(w.hh[1]))})
+        flops = S.env_validate(su, du, su, du, 0, jobs, mode=mode)["flops"]
+        outs = [torch.empty(max(1, S.env_layout(su, du, su, du, 0, jobs, k).size()), dtype=torch.float64,
+                            device="cuda") for k in range(len(jobs))]
+        keep = []
+        J = S._EnvJobs(jobs)
+        tuu = S._tensor(su, du, keep)
+        optr = (ctypes.c_void_p * len(outs))(*[capi.ptr(x) for x in outs])
+        ts, clk = _time_calls(torch, lambda: capi.check(capi.lib().su2g_env_run(
+            tuu, tuu, 0, J.n, J.ptr, len(outs), ctypes.addressof(optr), mode, None)), args.steps, args.warmup)
+        t = float(np.median(ts))
+        metric, unit, hib = (f"environment update TFLOP/s (FP64-equivalent), SU(2) D={args.D}, "
+                             f"{len(w.ops)} spin-1 operators + block Hamiltonian"), "TFLOP/s", True
+        value = flops / t / 1e12
+        roof = _gemm_roofline(torch, flops, t, slices, "planning, pack and GEMM launches")
+        if o is not None:
+            # the oracle's operator_transformation costs minutes at full D: one operator at D/4
+            ws = synthetic_site_step(D=args.D // 4, nops=1)
+            su_s, xu_s = ws.uu
+            s0, x0 = ws.ops[0]
+            osu, os0 = _oracle_struct(o, su_s), _oracle_struct(o, s0)
+            res = {}
+            tc, n = _cpu_sample(lambda: res.__setitem__("y", o.env_transform(1, osu, xu_s, osu, xu_s, os0, x0, 0)[1]),
+                                max_steps=3)
+            du_s = dev(xu_s)
+            job = [{"kind": "transform", "slot": 0, "coef": 1.0, "x": (s0, dev(x0))}]
+            f1 = S.env_validate(su_s, du_s, su_s, du_s, 0, job, mode=0)["flops"]
+            cb = {"value": f1 / tc / 1e12, "unit": unit, "cores": 1, "kind": "port",
+                  "sample": f"one operator_transformation at D={args.D // 4}, oracle (C loops), median of {n}"}
+            (_, ys), = S.env_batch(su_s, du_s, su_s, du_s, 0, job, mode=mode)
+            got = ys[: len(res["y"])].cpu().numpy()
+            extra["rel_err_vs_oracle_sample"] = float(np.linalg.norm(got - res["y"]) / np.linalg.norm(res["y"]))
+        config = {"workload": f"synthetic SU(2) site update, D={args.D}, {len(w.ops)} spin-1 operators + "
+                              "block Hamiltonian", "mode": args.mode, "flops_per_step": flops}
+    else:  # svd
+        h = synthetic_heff(D=args.D, nspin1=0, seed=1234, spin0=False)
+        psi = dev(h.psi_data)
+        tu = w.ul[0]
+        ts, clk = _time_calls(torch, lambda: S.svd(h.psi, psi, tu, 1.0, tu, 0.0, args.D), args.steps, args.warmup)
+        t = float(np.median(ts))
+        metric, unit, hib = f"truncation ms per two-site vector, SU(2) D={args.D} -> {args.D} multiplets", "ms", False
+        value = t * 1e3
+        gram = 0.0
+        for i in range(h.psi.nten):
+            if h.psi.flag[i]:
+                a, b = h.psi.block_shape(i)
+                m, n = min(a, b), max(a, b)
+                gram += 4.0 * m * m * n  # Gram matrix + the other factor
+        roof = _gemm_roofline(torch, gram, t, 0, "Gram and second-factor products only; the eigendecompositions "
+                                                 "and host sorting are not counted")
+        dtype = "f64"
+        if o is not None:
+            ops_ = _oracle_struct(o, h.psi)
+            tc, n = _cpu_sample(lambda: o.svd_truncate(ops_, h.psi_data, 1.0, 0.0, args.D), max_steps=3)
+            cb = {"value": tc * 1e3, "unit": unit, "cores": cores, "kind": "port",
+                  "sample": f"the same truncation, oracle (numpy LAPACK per sector + dsort2), median of {n}"}
+        config = {"workload": f"synthetic SU(2) two-site vector, D={args.D}, spin-1/2 sites", "max_dcut": args.D}
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.median(ts)) * 1e3, "higher_is_better": hib,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {**config, "row": args.row, "l2": "flushed (256 MB write) before every call"},
+            "roofline": roof, "cpu_baseline": cb, "clocks": clk, **extra}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.row != "heff":
+        return run_row(args)
     return run_su2g(args)
 
 

@@ -265,7 +265,9 @@ int su2g_fac_table(int table, int side, int a, int b, int c, int d, int e, doubl
  *                     of [3, 0, tu leg 0, tu leg 1, (-1, bond)] (resp. tv)
  *                     with every legal block present (su2g_layout with a NULL
  *                     flag array); at most tu_cap / tv_cap doubles
- * Blocks until done. */
+ * The sectors run concurrently (one stream, handle pair and host thread
+ * each, kept per device across calls); calls from several host threads take
+ * turns.  Blocks until done. */
 int su2g_svd(const int* psi_desc, const int* psi_flag, const double* psi, const int* tu_desc, double p1,
              const int* tv_desc, double p2, int max_dcut, int* bond, int bond_cap, double* wout, int wout_cap,
              int* dout, double* tu, int64_t tu_cap, double* tv, int64_t tv_cap, void* stream);

@@ -8,6 +8,9 @@
 //   * the other factor by one more product, singular values = sqrt of the
 //     eigenvalues above 1e-100 of the largest, columns scaled by s^(p1-1) and
 //     s^p2 (or the mirror for wide blocks);
+//   * the sectors are independent: each runs on its own stream, cuBLAS /
+//     cuSOLVER handles and host thread (the refinement reads eigenvalues back
+//     between steps), so their eigendecompositions overlap on the GPU;
 //   * on the host: all kept singular values sorted by the Shell sort of
 //     sort2.f (dsort2, whose handling of equal values decides ties), the
 //     largest max_dcut multiplets kept (no (2j+1) weighting), and the
@@ -18,7 +21,11 @@
 #include <cusolverDn.h>
 
 #include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kernels.hpp"
@@ -37,18 +44,77 @@ __global__ void scale_columns(double* a, int rows, int c0, int ncol, int ld, con
   }
 }
 
+// Per-device resources kept across calls: one stream and one pair of
+// cuBLAS / cuSOLVER handles per concurrently processed sector (creating
+// handles costs milliseconds), and a library-private memory pool whose freed
+// blocks stay reserved (stream-ordered allocation without device-wide
+// synchronisation, unlike cudaMalloc).  One su2g_svd call holds them at a
+// time.
+struct Lane {
+  cudaStream_t st = nullptr;
+  cublasHandle_t blas = nullptr;
+  cusolverDnHandle_t sol = nullptr;
+  cudaEvent_t done = nullptr;
+};
+struct DeviceRes {
+  cudaMemPool_t pool = nullptr;
+  std::vector<Lane> lanes;
+};
+std::mutex g_res_mutex;
+std::map<int, DeviceRes> g_res;
+
+// Grows the device's lanes to n; returns an error message or "".
+std::string acquire_lanes(DeviceRes& r, int dev, int n) {
+  if (!r.pool) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    if (cudaMemPoolCreate(&r.pool, &props) != cudaSuccess) {
+      r.pool = nullptr;
+      return "cannot create a memory pool";
+    }
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool
+    cudaMemPoolSetAttribute(r.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  while ((int)r.lanes.size() < n) {
+    Lane l;
+    if (cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking) != cudaSuccess) return "cannot create a stream";
+    if (cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(l.st);
+      return "cannot create an event";
+    }
+    if (cublasCreate(&l.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&l.sol) != CUSOLVER_STATUS_SUCCESS) {
+      if (l.blas) cublasDestroy(l.blas);
+      cudaEventDestroy(l.done);
+      cudaStreamDestroy(l.st);
+      return "cannot create cuBLAS/cuSOLVER handles";
+    }
+    cublasSetStream(l.blas, l.st);
+    cusolverDnSetStream(l.sol, l.st);
+    r.lanes.push_back(l);
+  }
+  return "";
+}
+
+// The work of one sector: its lane, its allocations (from the pool, on the
+// lane's stream; released on `free_st` once the caller's stream has used
+// them) and its error state.
 struct Ctx {
-  cudaStream_t st;
+  cudaStream_t st = nullptr;
+  cudaStream_t free_st = nullptr;
+  cudaMemPool_t pool = nullptr;
   cublasHandle_t blas = nullptr;
   cusolverDnHandle_t sol = nullptr;
   std::vector<void*> allocs;
   std::string err;
   int code = SU2G_OK;
 
+  Ctx() = default;
+  Ctx(const Ctx&) = delete;
+  Ctx& operator=(const Ctx&) = delete;
   ~Ctx() {
-    for (void* p : allocs) cudaFree(p);
-    if (blas) cublasDestroy(blas);
-    if (sol) cusolverDnDestroy(sol);
+    for (void* p : allocs) cudaFreeAsync(p, free_st);
   }
   bool ok() const { return code == SU2G_OK; }
   void set(int c, const std::string& m) {
@@ -59,7 +125,7 @@ struct Ctx {
   }
   double* dalloc(int64_t n) {
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(double));
+    cudaError_t e = cudaMallocFromPoolAsync(&p, std::max<int64_t>(n, 1) * sizeof(double), pool, st);
     if (e != cudaSuccess) {
       set(e == cudaErrorMemoryAllocation ? SU2G_ENOMEM : SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
       return nullptr;
@@ -240,26 +306,67 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
     return fail(SU2G_EINVAL, "svd: psi legs are not the fused legs 0, 1 of tu / tv");
   P.set_layout(psi_flag);
   if (P.total > 0 && !psi) return fail(SU2G_EINVAL, "svd: null psi");
-  Ctx c;
-  c.st = (cudaStream_t)stream;
-  if (cublasCreate(&c.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&c.sol) != CUSOLVER_STATUS_SUCCESS)
-    return fail(SU2G_ECUDA, "svd: cannot create cuBLAS/cuSOLVER handles");
-  cublasSetStream(c.blas, c.st);
-  cusolverDnSetStream(c.sol, c.st);
+  cudaStream_t cst = (cudaStream_t)stream;
   const int n0 = P.legs[0].n(), n1 = P.legs[1].n();
-  std::vector<Sector> secs;
   // sectors in the reference's loop order: leg-0 sector, then the leg-1 sector of equal spin
-  for (int i = 0; i < n0 && c.ok(); ++i)
-    for (int j = 0; j < n1 && c.ok(); ++j) {
+  struct Job {
+    int i, b, m, n;
+  };
+  std::vector<Job> jobs;
+  for (int i = 0; i < n0; ++i)
+    for (int j = 0; j < n1; ++j) {
       if (P.legs[0].angm[i] != P.legs[1].angm[j]) continue;
       const int b = i + j * n0;
-      if (!P.flag[b]) continue;
-      Sector s;
-      s.i = i;
-      sector_svd(c, psi + P.offset[b], P.legs[0].dim[i], P.legs[1].dim[j], p1, p2, max_dcut, &s);
-      secs.push_back(s);
+      if (P.flag[b]) jobs.push_back(Job{i, b, P.legs[0].dim[i], P.legs[1].dim[j]});
     }
-  if (!c.ok()) return fail(c.code, c.err);
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+  std::unique_lock<std::mutex> lock(g_res_mutex);
+  DeviceRes& res = g_res[dev];
+  const std::string rerr = acquire_lanes(res, dev, (int)jobs.size());
+  if (!rerr.empty()) return fail(SU2G_ECUDA, "svd: " + rerr);
+  // every sector on its own lane (stream + handles) and host thread: the
+  // eigendecompositions and the refinement loops of all sectors overlap
+  cudaEvent_t ready = nullptr;
+  ce = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventRecord(ready, cst);
+  if (ce != cudaSuccess) {
+    if (ready) cudaEventDestroy(ready);
+    return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+  }
+  std::vector<std::unique_ptr<Ctx>> ctx(jobs.size());
+  std::vector<Sector> secs(jobs.size());
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    ctx[q].reset(new Ctx());
+    Ctx& c = *ctx[q];
+    c.st = res.lanes[q].st;
+    c.free_st = cst;
+    c.pool = res.pool;
+    c.blas = res.lanes[q].blas;
+    c.sol = res.lanes[q].sol;
+    const cudaError_t we = cudaStreamWaitEvent(c.st, ready, 0);  // psi is written on the caller's stream
+    if (we != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(we));
+  }
+  auto run = [&](size_t q) {
+    Ctx& c = *ctx[q];
+    if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
+    if (c.ok()) {
+      secs[q].i = jobs[q].i;
+      sector_svd(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, p1, p2, max_dcut, &secs[q]);
+    }
+    const cudaError_t e = cudaEventRecord(res.lanes[q].done, c.st);
+    if (e != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+  };
+  std::vector<std::thread> threads;
+  for (size_t q = 1; q < jobs.size(); ++q) threads.emplace_back(run, q);
+  if (!jobs.empty()) run(0);
+  for (std::thread& t : threads) t.join();
+  // the caller's stream continues after every sector (placement copies, frees)
+  for (size_t q = 0; q < jobs.size(); ++q) cudaStreamWaitEvent(cst, res.lanes[q].done, 0);
+  cudaEventDestroy(ready);
+  for (const auto& c : ctx)
+    if (!c->ok()) return fail(c->code, c->err);
   // global selection of the max_dcut largest multiplets (tensor_su2.cpp:1686-1695)
   std::vector<double> ws;
   std::vector<int> is;
@@ -329,12 +436,13 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
       if (!src || r0 < 0) return fail(SU2G_EINVAL, "svd: internal placement error");
       const int ld = side ? src->n : src->m;
       const double* col0 = (side ? src->v : src->u) + (int64_t)ld * (src->dc - d) + r0;
-      cudaError_t ce = cudaMemcpy2DAsync(out + O.offset[b], rows * sizeof(double), col0, ld * sizeof(double),
-                                         rows * sizeof(double), d, cudaMemcpyDeviceToDevice, c.st);
-      if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+      const cudaError_t me = cudaMemcpy2DAsync(out + O.offset[b], rows * sizeof(double), col0,
+                                               ld * sizeof(double), rows * sizeof(double), d,
+                                               cudaMemcpyDeviceToDevice, cst);
+      if (me != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(me));
     }
   }
-  cudaError_t ce = cudaStreamSynchronize(c.st);
+  ce = cudaStreamSynchronize(cst);
   if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
   return SU2G_OK;
 }

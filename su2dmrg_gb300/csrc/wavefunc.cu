@@ -57,11 +57,17 @@ struct TrItem {
 constexpr int kTr = 32;          // tile edge
 constexpr int kTrThreads = 256;  // 32 x 8
 
+// Up to kParamItems blocks travel in the kernel's parameters (no upload);
+// longer lists are copied to the device first.
+constexpr int kParamItems = 160;  // 160 x 40 bytes: within the 32 KB parameter space
+struct TrList {
+  TrItem item[kParamItems];
+};
+
 // Global tiles are walked with a grid-stride loop; a CTA finds its block by a
 // binary search of the tile prefix.  Reads are coalesced along the source
 // column, writes along the destination column, through a padded 32 x 33 tile.
-__global__ void __launch_bounds__(kTrThreads) transpose_blocks_kernel(const TrItem* __restrict__ items, int nitems,
-                                                                      int64_t ntiles) {
+__device__ __forceinline__ void transpose_tiles(const TrItem* __restrict__ items, int nitems, int64_t ntiles) {
   __shared__ double tile[kTr][kTr + 1];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -89,6 +95,16 @@ __global__ void __launch_bounds__(kTrThreads) transpose_blocks_kernel(const TrIt
   }
 }
 
+__global__ void __launch_bounds__(kTrThreads) transpose_blocks_kernel(const TrItem* __restrict__ items, int nitems,
+                                                                      int64_t ntiles) {
+  transpose_tiles(items, nitems, ntiles);
+}
+
+__global__ void __launch_bounds__(kTrThreads) transpose_blocks_param_kernel(const __grid_constant__ TrList list,
+                                                                            int nitems, int64_t ntiles) {
+  transpose_tiles(list.item, nitems, ntiles);
+}
+
 // Runs the transposes of `items` (host list; tile0 filled here) on `st`.
 cudaError_t launch_transposes(std::vector<TrItem>& items, cudaStream_t st) {
   std::vector<TrItem> live;
@@ -101,13 +117,19 @@ cudaError_t launch_transposes(std::vector<TrItem>& items, cudaStream_t st) {
     live.push_back(it);
   }
   if (live.empty()) return cudaSuccess;
+  const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 8);
+  if ((int)live.size() <= kParamItems) {
+    TrList list;
+    std::copy(live.begin(), live.end(), list.item);
+    transpose_blocks_param_kernel<<<grid, kTrThreads, 0, st>>>(list, (int)live.size(), ntiles);
+    return cudaGetLastError();
+  }
   TrItem* d_items = nullptr;
   const size_t bytes = live.size() * sizeof(TrItem);
   cudaError_t e = cudaMallocAsync((void**)&d_items, bytes, st);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(d_items, live.data(), bytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
-    const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sm_count() * 8);
     transpose_blocks_kernel<<<grid, kTrThreads, 0, st>>>(d_items, (int)live.size(), ntiles);
     e = cudaGetLastError();
   }

@@ -135,3 +135,45 @@ def synthetic_heff(D: int = 2000, nspin1: int = 18, seed: int = 1234, max2j: int
         hl = (hs, hx[0], 1.0)
         hr = (hs, hx[1], 1.0)
     return HeffWorkload(psi, x, terms, hl, hr, D)
+
+
+@dataclass
+class SiteStepWorkload:
+    """The tensors around one two-site step at bond dimension D (same sector
+    counts as synthetic_heff): the MPS pair (ul, ur) whose product is the
+    step's initial vector, and an environment batch (uu = vv, operators,
+    block Hamiltonian) of the site update that follows."""
+    ul: tuple   # (Su2Struct, data): (bond +1, spin-1/2, centre bond -1)
+    ur: tuple   # (spin-1/2, bond +1, centre bond -1)
+    uu: tuple   # (bond -1, spin-1/2, new bond +1)
+    ops: list   # [(Su2Struct, data)]: (bond +1, spin 1 (-1), bond -1)
+    hh: tuple   # (bond +1, bond -1) block Hamiltonian
+    D: int
+
+
+def synthetic_site_step(D: int = 2000, nops: int = 18, seed: int = 4321, max2j: int = 12) -> SiteStepWorkload:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = gaussian_sector_counts(D, max2j)
+    angm = [k for k in range(max2j + 1) if counts[k] > 0]
+    dims = [counts[k] for k in angm]
+    b = lambda d: Su2Bond(d, list(angm), list(dims))
+    ph = _spin_half()
+
+    def fill(struct):
+        s = struct.with_legal_flags()
+        off, tot = s.offsets()
+        x = np.zeros(tot)
+        for i in range(s.nten):
+            if s.flag[i]:
+                shape = s.block_shape(i)
+                n = int(np.prod(shape))
+                x[off[i]: off[i] + n] = rng.standard_normal(n) / np.sqrt(max(1, shape[0]))
+        return s, x
+
+    ul = fill(Su2Struct([b(1), ph, b(-1)], 0))
+    ur = fill(Su2Struct([ph, b(1), b(-1)], 0))
+    uu = fill(Su2Struct([b(-1), ph, b(1)], 0))
+    spin = Su2Bond(-1, [2], [1])
+    ops = [fill(Su2Struct([b(1), spin, b(-1)], 0)) for _ in range(nops)]
+    hh = fill(Su2Struct([b(1), b(-1)], 0))
+    return SiteStepWorkload(ul, ur, uu, ops, hh, D)
