@@ -512,9 +512,16 @@ int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len
   if (scratch_bytes)
     *scratch_bytes = (p->work.scratch_len + p->oz.partial_len) * (int64_t)sizeof(double) + p->oz.packed_bytes +
                      p->oz.exp_len * (int64_t)sizeof(int);
-  if (ntiles)
-    *ntiles = p->S > 0 ? (int)(p->oz.tile1.size() + p->oz.tile2.size())
-                       : (int)(p->work.tile1.size() + p->work.tile2.size());
+  if (ntiles) {
+    if (p->S > 0) {  // without the empty tiles that pad the persistent schedule
+      int n = 0;
+      for (const auto* v : {&p->oz.tile1, &p->oz.tile2})
+        for (const su2g::oz::OzTile& t : *v) n += t.mlen > 0;
+      *ntiles = n;
+    } else {
+      *ntiles = (int)(p->work.tile1.size() + p->work.tile2.size());
+    }
+  }
   return SU2G_OK;
 }
 

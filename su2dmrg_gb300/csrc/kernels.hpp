@@ -40,6 +40,9 @@ cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaSt
 // one-time per-process setup of the GEMM kernel (function attributes, SM count),
 // done before any launch is captured into a graph
 cudaError_t prepare_ozaki_gemm(int S);
+// CTAs of the persistent GEMM grid on the current device (its SM count); 152
+// when no device answers (host-only planning and validation).
+int ozaki_persistent_grid();
 // row-exponent pass (when rows_pass) + digit pass: 1 or 2 kernels, none for nunits == 0
 cudaError_t launch_pack(int S, const PackJob* jobs, const int2* units, int nunits, int max_nkt, bool rows_pass,
                         const Bases& bases, uint8_t* packed, int* exps, cudaStream_t stream);

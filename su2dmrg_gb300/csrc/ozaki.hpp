@@ -14,10 +14,10 @@
 //     C_ij = 2^(e_i + f_j - 7(S+1)) sum_{g=2}^{S+1} 2^(7(S+1-g)) G_g(i,j),
 //     G_g  = sum_{p+q=g} sum_k dA_p(i,k) dB_q(j,k)
 // (pairs with p+q > S+1 are dropped: they weigh below 2^-7(S+2)).  With
-// |d| <= 65 and at most S <= 7 pairs per group, a group summed over 512
-// values of k stays below 7 * 512 * 65^2 = 15,142,400 < 2^24 in magnitude
+// |d| <= 65 and at most S <= 7 pairs per group, a group summed over 560
+// values of k stays below 7 * 560 * 65^2 = 16,562,000 < 2^24 in magnitude
 // (every partial sum too), so the FP32 tensor-core accumulation of one group
-// over one K chunk of 512 is exact, and the chunk sums are combined in 64-bit
+// over one K chunk of 560 is exact, and the chunk sums are combined in 64-bit
 // integers, C = 2^(e_i + f_j - 48) sum_g 2^(48 - 7g) G_g.  The only
 // rounding is in forming N (2^-48 relative to the row maximum for S = 7), in
 // the dropped pairs, and in aligning products of different exponents to the
@@ -48,7 +48,7 @@ constexpr int kTM = 128;            // tile rows (MMA M)
 constexpr int kTN = 64;             // tile columns (MMA N)
 constexpr int kKS = 16;             // K per packed unit and shared-memory stage (one MMA deep)
 constexpr int kSBO = 8 * kKS * 2;   // bytes between 8-row core groups of a unit
-constexpr int kChunkStages = 32;    // exact FP32 group sums over 32 stages = 512 k
+constexpr int kChunkStages = 35;    // exact FP32 group sums over 35 stages = 560 k
 constexpr int kStages = 4;          // shared-memory ring depth of the tile GEMM
 constexpr int kExpZero = -(1 << 20);  // exponent of an all-zero row
 constexpr int kFixedTop = 48;         // fixed point: group g weighs 2^(kFixedTop - 7g)

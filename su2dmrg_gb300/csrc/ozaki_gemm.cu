@@ -11,7 +11,7 @@
 //                   columns per group g; frees each stage with a commit;
 //   warps 0-15      epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile
 //                   rows) and columns 16 (w / 4) .. + 15; after every K chunk
-//                   of 512 (or segment end) it reads the S group sums of its
+//                   of 560 (or segment end) it reads the S group sums of its
 //                   16 columns (tcgen05.ld), converts them exactly to
 //                   integers, weights them by 2^(48 - 7g) and adds them,
 //                   aligned to the tile's largest product exponents, into 16
@@ -115,6 +115,26 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ int f32_to_int_exact(uint32_t bits) { return __float2int_rn(__uint_as_float(bits)); }
 
 __device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
+
+// Weighted sum of one column's S group sums, v = sum_g shl_signed(G_g, 34 - 7g)
+// (group g weighs 2^(kFixedTop - 7(g+2))), from their FP32 bit patterns, in
+// few instructions: |G_g| <= 7 * 560 * 65^2 = 16,562,000 (the exactness bound
+// of a chunk), so G_1 * 128 + G_2 and G_3 * 128 + G_4 are exact in int32
+// (below 129 * 16,562,000 < 2^31) and only three 64-bit shift-adds remain:
+//   v = G_0 2^34 + (G_1 2^7 + G_2) 2^20 + (G_3 2^7 + G_4) 2^6 + sum_{g>=5} G_g >> (7g - 34).
+template <int S>
+__device__ __forceinline__ long long combine_groups(const uint32_t (&r)[S][4], int x) {
+  static_assert(S >= 5 && kFixedTop == 48 && kBits == 7, "group weights 2^34, 2^27, ... assumed");
+  int G[S];
+#pragma unroll
+  for (int gg = 0; gg < S; ++gg) G[gg] = f32_to_int_exact(r[gg][x]);
+  const int Y = G[1] * 128 + G[2];
+  const int X = G[3] * 128 + G[4];
+  int small = 0;
+#pragma unroll
+  for (int gg = 5; gg < S; ++gg) small += G[gg] >> (kBits * (gg + 2) - kFixedTop);
+  return ((long long)G[0] << 34) + ((long long)Y << 20) + ((long long)X << 6) + (long long)small;
+}
 
 // ilogb of a nonzero finite double given as its bit pattern (sign ignored)
 __device__ __forceinline__ int ilogb_bits(unsigned long long b) {
@@ -364,16 +384,13 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
             tmem_wait_ld();
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
-              long long v = 0;
-#pragma unroll
-              for (int gg = 0; gg < S; ++gg)
-                v += shl_signed((long long)f32_to_int_exact(r[gg][x]), kFixedTop - kBits * (gg + 2));
+              const long long v = combine_groups<S>(r, x);
               const int j = cb * 4 + x;
               const int sh = sha + shb_sh[warp][j];
               if (sh == 0) {
                 acc[j] += v;
               } else if (sh < 63) {
-                acc[j] += (v + (1ll << (sh - 1))) >> sh;  // round to nearest
+                acc[j] += ((v >> (sh - 1)) + 1) >> 1;  // = (v + 2^(sh-1)) >> sh: round to nearest
               }
             }
           }
@@ -459,6 +476,20 @@ int g_sms = 0;            // one resident CTA per SM (shared memory and TMEM): a
 bool g_prepared[9] = {};  // per S
 std::mutex g_prep_mu;
 }  // namespace
+
+int ozaki_persistent_grid() {
+  static std::once_flag once;
+  static int grid = 152;
+  std::call_once(once, [] {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        n > 0)
+      grid = n;
+    else
+      cudaGetLastError();  // no device here: clear the error it left
+  });
+  return grid;
+}
 
 cudaError_t prepare_ozaki_gemm(int S) {
   if (S != 6 && S != 7) return cudaErrorInvalidValue;

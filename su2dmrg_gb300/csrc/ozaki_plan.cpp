@@ -3,9 +3,12 @@
 // segments, derived from the block-level products of the H_eff work list.
 #include "ozaki_plan.hpp"
 
+#include "kernels.hpp"
+
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <queue>
 #include <tuple>
 
 namespace su2g {
@@ -183,6 +186,54 @@ void split_phase2(OzWork& w) {
   w.tile2.swap(out);
 }
 
+// Static schedule of the persistent GEMM, whose CTA b walks the tiles b, b +
+// G, b + 2G, ... (G = grid).  Each tile's cost in stage units counts its
+// stages, one drain of the TMEM group sums per chunk (about five stages of
+// MMA time) and its store (about four); tiles are dealt longest first to the
+// least-loaded CTA, then laid out so that the walk of CTA b visits exactly
+// its own tiles, heaviest first.  CTAs with fewer tiles meet empty tiles (no
+// segments, no rows) at the end of their walk.
+void schedule_tiles(std::vector<OzTile>* tiles, const std::vector<OzSeg>& segs, int grid) {
+  const int n = (int)tiles->size();
+  auto heavier = [](const OzTile& x, const OzTile& y) { return x.work > y.work; };
+  if (n <= grid || grid <= 0) {
+    std::stable_sort(tiles->begin(), tiles->end(), heavier);
+    return;
+  }
+  std::vector<int64_t> cost(n);
+  for (int i = 0; i < n; ++i) {
+    const OzTile& t = (*tiles)[i];
+    int64_t c = 4;
+    for (int s = t.seg0; s < t.seg0 + t.nseg; ++s)
+      c += segs[s].nks + 5 * ((segs[s].nks + kChunkStages - 1) / kChunkStages);
+    cost[i] = c;
+  }
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  using Load = std::pair<int64_t, int>;  // (load, cta)
+  std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+  for (int b = 0; b < grid; ++b) heap.push({0, b});
+  std::vector<std::vector<int>> lists(grid);
+  for (int i : order) {
+    const Load l = heap.top();
+    heap.pop();
+    lists[l.second].push_back(i);
+    heap.push({l.first + cost[i], l.second});
+  }
+  size_t kmax = 0;
+  for (const auto& l : lists) kmax = std::max(kmax, l.size());
+  OzTile pad{};
+  pad.c_buf = kBufAbs;
+  pad.ldc = 1;
+  pad.rowmax = -1;
+  pad.rms = 1;
+  std::vector<OzTile> out((size_t)grid * kmax, pad);
+  for (int b = 0; b < grid; ++b)
+    for (size_t k = 0; k < lists[b].size(); ++k) out[b + k * grid] = (*tiles)[lists[b][k]];
+  tiles->swap(out);
+}
+
 }  // namespace
 
 int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
@@ -230,9 +281,9 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
     }
   }
   split_phase2(w);
-  auto heavier = [](const OzTile& x, const OzTile& y) { return x.work > y.work; };
-  std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
-  std::stable_sort(w.tile2.begin(), w.tile2.end(), heavier);
+  const int grid = ozaki_persistent_grid();
+  schedule_tiles(&w.tile1, w.seg1, grid);
+  schedule_tiles(&w.tile2, w.seg2, grid);
   for (int c = 0; c < 3; ++c) {
     w.units[c].clear();
     w.max_nkt[c] = 0;
@@ -260,6 +311,7 @@ int validate_ozaki_work(const OzWork& w, std::string* err) {
     }
   auto check = [&](const std::vector<OzTile>& tiles, const std::vector<OzSeg>& segs) -> bool {
     for (const OzTile& t : tiles) {
+      if (t.nseg == 0 && t.mlen == 0 && t.nlen == 0 && t.rowmax < 0) continue;  // schedule padding
       if (t.seg0 < 0 || t.nseg < 0 || t.seg0 + t.nseg > (int)segs.size() || t.mlen <= 0 || t.mlen > kTM ||
           t.nlen <= 0 || t.nlen > kTN || t.ldc < t.m0 + t.mlen)
         return false;
