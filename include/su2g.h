@@ -38,6 +38,7 @@ extern "C" {
 #define SU2G_ECUDA 3       /* a CUDA runtime call failed */
 #define SU2G_ETIMEOUT 4    /* a bounded device wait gave up */
 #define SU2G_EUNSUPPORTED 5
+#define SU2G_EIO 6          /* a checkpoint file is missing, unreadable or malformed */
 
 #define SU2G_MODE_F64 0             /* plain FP64 contractions (FP64 tensor-core MMA) */
 #define SU2G_MODE_SPLIT_BF16 1      /* FP64 emulated with 7 BF16 digit slices on the tcgen05 tensor cores */
@@ -301,6 +302,42 @@ int su2g_vectran(su2g_tensor u, int flag, double* out, void* stream);
 int su2g_input_vector_layout(su2g_tensor ul, su2g_tensor ur, int* out_desc, int out_desc_cap, int* out_flag,
                              int out_flag_cap, int64_t* out_len);
 int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double* out, int mode, void* stream);
+
+/* -------------------------------------------------------- checkpoints -- */
+/* The engine's checkpoint files (dmrg_su2::save_mps2 / read_mps,
+ * save_enr / read_enr, save_ww / read_ww; dmrg_su2_omp.cpp:864-1242), for
+ * resuming a run and for serving checkpoints.  Host files, device tensors.
+ * File names as the engine builds them, in the current directory:
+ *   SU2G_CKPT_MPS_DAT  uu-<ns>-<dcut>-<totspin>-<ky>-<exc>-<pos>.dat
+ *   SU2G_CKPT_MPS_BIN  uu-<ns>-<dcut>-<totspin>-<ky>-<exc>-<pos>.bin
+ *   SU2G_CKPT_ENR      enr-<ns>-<dcut>-<totspin>-<ky>-<exc>.dat   (pos unused)
+ *   SU2G_CKPT_WW       ww-<ns>-<dcut>-<totspin>-<ky>-<exc>-<pos>.bin (the engine uses pos = ns/2) */
+#define SU2G_CKPT_MPS_DAT 0
+#define SU2G_CKPT_MPS_BIN 1
+#define SU2G_CKPT_ENR 2
+#define SU2G_CKPT_WW 3
+int su2g_checkpoint_name(int kind, int ns, int dcut, int totspin, int ky, int exc, int pos, char* buf, int cap);
+/* One site's MPS tensor (device data) to its .dat (structure as text) and
+ * .bin (block flags, reduced blocks, then the canonical CG part of each stored
+ * block) files, byte for byte as save_mps2 writes them. */
+int su2g_mps_save(const char* dat_path, const char* bin_path, su2g_tensor t, void* stream);
+/* read_mps for one site: the structure and flags (host only), then the
+ * reduced blocks into out (device, at most out_cap doubles).  Each block's CG
+ * part must be proportional to the canonical one (the engine writes it
+ * exactly); the block is rescaled by the ratio.  Missing or malformed files
+ * give SU2G_EIO. */
+int su2g_mps_load_layout(const char* dat_path, const char* bin_path, int* out_desc, int out_desc_cap, int* out_flag,
+                         int out_flag_cap, int64_t* out_len);
+int su2g_mps_load(const char* dat_path, const char* bin_path, double* out, int64_t out_cap, void* stream);
+/* save_enr: appends one value with 16 significant digits (the engine writes
+ * gs_enr, its eigenvalue with the -1000 shift where it applies); enr_read
+ * returns every value of the file in order (read_enr keeps the last one and
+ * adds 1000).  *count = values in the file. */
+int su2g_enr_append(const char* path, double value);
+int su2g_enr_read(const char* path, double* values, int cap, int* count);
+/* save_ww / read_ww: raw doubles (host); *nread = doubles actually read. */
+int su2g_ww_save(const char* path, const double* ww, int64_t n);
+int su2g_ww_load(const char* path, double* ww, int64_t n, int64_t* nread);
 
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme

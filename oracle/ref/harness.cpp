@@ -21,6 +21,7 @@
 #include <cstring>
 #include <algorithm>
 #include <vector>
+#include <unistd.h>
 #define private public
 #include "dmrg_su2_omp.hpp"
 #undef private
@@ -444,6 +445,70 @@ int ref_legal(const int* desc, int* legal) {
 // scratch-directory creation) and returns the per-sweep energies E0-1000.
 // Must be called from a scratch working directory: the engine writes its
 // checkpoint files (uu-*, ww-*, enr-*) into the current directory.
+// Checkpoint files written by the engine itself in directory `dir`: do_idmrg
+// and niter sweeps (as ref_run_dmrg), then save_mps2 (every site, memory_flag
+// 0; dmrg_su2_omp.cpp:864-941), save_enr (:1070-1097) and save_ww
+// (:1154-1186).  uu[0..ns) are exported for ref_idmrg_select; *enr gets
+// gs_enr[0] as written.  Returns ns, or -1 if `dir` cannot be entered.
+int ref_checkpoint_write(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
+                         int nthreads, const char* dir, double* enr) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return -1;
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  omp_set_nested(1);
+  omp_set_max_active_levels(2);
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  c->do_idmrg();
+  for (int i = 0; i < niter; ++i) c->sweep();
+  c->save_mps2();
+  c->save_enr();
+  c->save_ww();
+  *enr = c->gs_enr[0];
+  g_export.clear();
+  for (int i = 0; i < c->ns; ++i) g_export.push_back(&c->uu[i]);
+  const int ns = c->ns;
+  if (chdir(cwd) != 0) return -1;
+  return ns;
+}
+
+// The same files read back by the engine (read_mps, read_enr, read_ww with
+// read1 = d, read2 = 0: dmrg_su2_omp.cpp:944-1151, 1188-1242) into a fresh
+// engine of the same lattice.  uu[0..ns) are exported; *enr = gs_enr[0] after
+// read_enr; ww[0][0..d) copied to ww_out (cap >= d).  Returns ns, -1 if `dir`
+// cannot be entered, -2 if read_mps reports a missing file.
+int ref_checkpoint_read(int lx, int ly, int sec, int d, const char* dir, double* enr, double* ww_out, int ww_cap) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return -1;
+  max_dcut = d;
+  memory_flag = 0;
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  const bool ok = c->read_mps(d, 0);
+  c->read_enr(d, 0);
+  c->read_ww(d, 0);
+  *enr = c->gs_enr[0];
+  for (int i = 0; i < d && i < ww_cap; ++i) ww_out[i] = c->ww[0][i];
+  g_export.clear();
+  for (int i = 0; i < c->ns; ++i) g_export.push_back(&c->uu[i]);
+  const int ns = c->ns;
+  if (chdir(cwd) != 0) return -1;
+  return ok ? ns : -2;
+}
+
 int ref_run_dmrg(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
                  int nthreads, double* energies) {
   max_dcut = d;

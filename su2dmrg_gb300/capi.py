@@ -20,6 +20,7 @@ SU2G_ENOMEM = 2
 SU2G_ECUDA = 3
 SU2G_ETIMEOUT = 4
 SU2G_EUNSUPPORTED = 5
+SU2G_EIO = 6
 
 MODE_F64 = 0
 MODE_SPLIT_BF16 = 1
@@ -95,6 +96,14 @@ _PROTOS = {
     "su2g_vectran": (_i, [Tensor, _i, _vp, _vp]),
     "su2g_input_vector_layout": (_i, [Tensor, Tensor, _vp, _i, _vp, _i, _vp]),
     "su2g_prepare_input_vector": (_i, [Tensor, Tensor, _vp, _i, _vp]),
+    "su2g_checkpoint_name": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp, _i]),
+    "su2g_mps_save": (_i, [_vp, _vp, Tensor, _vp]),
+    "su2g_mps_load_layout": (_i, [_vp, _vp, _vp, _i, _vp, _i, _vp]),
+    "su2g_mps_load": (_i, [_vp, _vp, _vp, _i64, _vp]),
+    "su2g_enr_append": (_i, [_vp, _d]),
+    "su2g_enr_read": (_i, [_vp, _vp, _i, _vp]),
+    "su2g_ww_save": (_i, [_vp, _vp, _i64]),
+    "su2g_ww_load": (_i, [_vp, _vp, _i64, _vp]),
     "su2g_vec_dot": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "su2g_vec_axpy": (_i, [_d, _vp, _vp, _i64, _vp]),
     "su2g_vec_scale": (_i, [_d, _vp, _i64, _vp]),

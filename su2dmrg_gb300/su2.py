@@ -14,6 +14,7 @@ entry points; all arithmetic runs on the GPU through the C ABI.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -533,3 +534,67 @@ def prepare_input_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, mode: int = capi.
                                           stream_handle(stream)))
     return s, y
 
+
+
+# ---------------------------------------------------------------- checkpoints
+CKPT_MPS_DAT, CKPT_MPS_BIN, CKPT_ENR, CKPT_WW = 0, 1, 2, 3
+
+
+def checkpoint_name(kind: int, ns: int, dcut: int, totspin: int = 0, ky: int = 0, exc: int = 0, pos: int = 0) -> str:
+    """A checkpoint file name as the engine builds it (kind CKPT_*)."""
+    buf = ctypes.create_string_buffer(256)
+    check(lib().su2g_checkpoint_name(int(kind), int(ns), int(dcut), int(totspin), int(ky), int(exc), int(pos),
+                                     buf, len(buf)))
+    return buf.value.decode()
+
+
+def _path(p) -> bytes:
+    return os.fsencode(p)
+
+
+def mps_save(dat_path, bin_path, s: Su2Struct, data, stream=None) -> None:
+    """One site's MPS tensor (device data) to its .dat / .bin files."""
+    keep = []
+    check(lib().su2g_mps_save(_path(dat_path), _path(bin_path), _tensor(s, data, keep), stream_handle(stream)))
+
+
+def mps_load_layout(dat_path, bin_path) -> Su2Struct:
+    return _layout_out(lib().su2g_mps_load_layout, _path(dat_path), _path(bin_path))
+
+
+def mps_load(dat_path, bin_path, device="cuda", stream=None):
+    """read_mps for one site: returns (Su2Struct, device tensor)."""
+    import torch
+
+    s = mps_load_layout(dat_path, bin_path)
+    y = torch.empty(max(1, s.size()), dtype=torch.float64, device=device)
+    check(lib().su2g_mps_load(_path(dat_path), _path(bin_path), ptr(y), y.numel(), stream_handle(stream)))
+    return s, y
+
+
+def enr_append(path, value: float) -> None:
+    check(lib().su2g_enr_append(_path(path), float(value)))
+
+
+def enr_read(path) -> np.ndarray:
+    """Every value of an energy file, in order."""
+    n = ctypes.c_int()
+    out = np.zeros(4096)
+    rc = lib().su2g_enr_read(_path(path), ptr(out), len(out), ctypes.addressof(n))
+    if rc == capi.SU2G_EINVAL and n.value > len(out):
+        out = np.zeros(n.value)
+        rc = lib().su2g_enr_read(_path(path), ptr(out), len(out), ctypes.addressof(n))
+    check(rc)
+    return out[: n.value].copy()
+
+
+def ww_save(path, ww) -> None:
+    a = np.ascontiguousarray(ww, np.float64)
+    check(lib().su2g_ww_save(_path(path), ptr(a), a.size))
+
+
+def ww_load(path, n: int) -> np.ndarray:
+    out = np.zeros(max(1, n))
+    got = ctypes.c_int64()
+    check(lib().su2g_ww_load(_path(path), ptr(out), int(n), ctypes.addressof(got)))
+    return out[: got.value].copy()

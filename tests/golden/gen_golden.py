@@ -490,8 +490,51 @@ def idmrg_cases(L):
     return cases
 
 
+def checkpoint_cases(L):
+    """Checkpoint files written by the engine itself (save_mps2, save_enr,
+    save_ww after do_idmrg and one sweep of a 4x2 J1 lattice at D=16), copied
+    into tests/golden/ckpt/, with the engine's in-memory MPS tensors (reduced
+    blocks and CG parts) and what its own readers return for the same files
+    (read_mps, read_enr, read_ww)."""
+    import shutil
+
+    out = os.path.join(HERE, "ckpt")
+    os.makedirs(out, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    L.ref_checkpoint_write.restype = ctypes.c_int
+    L.ref_checkpoint_read.restype = ctypes.c_int
+    e = ctypes.c_double()
+    ns = L.ref_checkpoint_write(4, 2, 0, 16, 1, ctypes.c_double(1.0), ctypes.c_double(0.0), 2, 1,
+                                tmp.encode(), ctypes.byref(e))
+    assert ns > 0
+    for f in sorted(os.listdir(tmp)):
+        shutil.copy(os.path.join(tmp, f), out)
+    case = dict(ns=np.int32(ns), enr_written=np.float64(e.value), files=np.array(sorted(os.listdir(tmp))))
+    for i in range(ns):
+        L.ref_idmrg_select(i)
+        d = np.zeros(1024, np.int32)
+        nd = L.ref_result_desc(p(d))
+        flag, x1, x2 = read_result(L)
+        case.update({f"desc{i}": d[:nd].copy(), f"flag{i}": flag, f"x{i}": x1, f"cg{i}": x2})
+    e2 = ctypes.c_double()
+    ww = np.zeros(64)
+    r = L.ref_checkpoint_read(4, 2, 0, 16, tmp.encode(), ctypes.byref(e2), p(ww), 64)
+    assert r == ns
+    for i in range(ns):  # the engine reads back what it wrote
+        L.ref_idmrg_select(i)
+        flag, x1, x2 = read_result(L)
+        assert np.array_equal(flag, case[f"flag{i}"]) and np.array_equal(x1, case[f"x{i}"])
+    case.update(enr_read=np.float64(e2.value), ww_read=ww[:16].copy())
+    shutil.rmtree(tmp)
+    return case
+
+
 def main():
     L = ctypes.CDLL(REFLIB)
+    if "--only-ckpt" in sys.argv:
+        L.ref_setup(1, 25)
+        np.savez(os.path.join(HERE, "ckpt_engine.npz"), **checkpoint_cases(L))
+        return
     L.ref_setup(1, 25)
     rng = np.random.Generator(np.random.PCG64(20241203))
     fac = np.zeros(25**3)
@@ -517,6 +560,7 @@ def main():
         for c in idmrg_cases(L):
             name = c.pop("name")
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **c)
+    np.savez(os.path.join(HERE, "ckpt_engine.npz"), **checkpoint_cases(L))
     if "--no-dmrg" not in sys.argv:
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)
