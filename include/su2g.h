@@ -303,6 +303,33 @@ int su2g_input_vector_layout(su2g_tensor ul, su2g_tensor ur, int* out_desc, int 
                              int out_flag_cap, int64_t* out_len);
 int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double* out, int mode, void* stream);
 
+/* ------------------------------------------------------- measurement -- */
+/* tensor_su2::take_trace (tensor_su2.cpp:720-742): the sum of the traces of
+ * the blocks of equal spins of a 2-leg tensor (device data; no (2j+1)
+ * weight). */
+int su2g_take_trace(su2g_tensor t, double* out, void* stream);
+/* tensor_su2::ss_inner_prod (tensor_su2.cpp:687-715): sum over the blocks
+ * stored in a of their element overlap with b's, weighted by
+ * sqrt(2j_2+1)/sqrt(2j_0+1) for 3-leg operators; a and b of one structure,
+ * every block of a stored in b.  Both desc NULL (operators never built): 0. */
+int su2g_ss_inner_prod(su2g_tensor a, su2g_tensor b, double* out, void* stream);
+/* tensor_su2::multiply_singular_value(leg, w) (tensor_su2.cpp:359-384), in
+ * place on device data: each multiplet of leg `leg` scaled by its weight,
+ * w (host) laid out sector by sector in the leg's order, nw >= the leg's
+ * multiplets. */
+int su2g_multiply_singular_value(const int* desc, const int* flag, double* data, int leg, const double* w, int64_t nw,
+                                 void* stream);
+/* dmrg_su2::mea_enr (dmrg_su2_omp_mea_enr.cpp:194-242): the energy at the
+ * centre bond from the environments the measurement run builds,
+ *   [tr hl + tr(W hr W) + sum_k coef[k] ss_inner_prod(left[k], right[k])] / sum_i ww[i]^2,
+ * hl = hh[ns/2-1], hr = hh[ns/2] (not scaled; W = the weights ww on both of
+ * its legs, nww >= their multiplets; the denominator sums all nww), the pairs
+ * in mea_enr's loop order (couplings with coup, plaquettes with -qdelta).
+ * parts (optional, 4 doubles): tr hl, tr(W hr W), the pair sum, sum ww^2.
+ * hr is left unchanged (mea_enr scales it in place). */
+int su2g_mea_enr(su2g_tensor hl, su2g_tensor hr, const double* ww, int64_t nww, int npairs, const su2g_tensor* left,
+                 const su2g_tensor* right, const double* coef, double* energy, double* parts, void* stream);
+
 /* -------------------------------------------------------- checkpoints -- */
 /* The engine's checkpoint files (dmrg_su2::save_mps2 / read_mps,
  * save_enr / read_enr, save_ww / read_ww; dmrg_su2_omp.cpp:864-1242), for

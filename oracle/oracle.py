@@ -922,3 +922,55 @@ def vectran(s: Struct, x, direction: int):
     for b, blk in dst.items():
         y[off[b]: off[b] + blk.size] = blk.ravel(order="F")
     return out, y
+
+
+# --------------------------------------------------------------------------
+# Centre-bond energy (dmrg_su2::mea_enr, dmrg_su2_omp_mea_enr.cpp:194-242)
+# and its reductions (tensor_su2.cpp:359-384, 687-742)
+# --------------------------------------------------------------------------
+def take_trace(s: Struct, x) -> float:
+    """Sum of the traces of the blocks of equal spins (no (2j+1) weight)."""
+    t = 0.0
+    for b, blk in _blocks(s, x).items():
+        a = s.block_angm(b)
+        if a[0] == a[1]:
+            t += float(np.trace(blk))
+    return t
+
+
+def ss_inner_prod(sa: Struct, xa, sb: Struct, xb) -> float:
+    """Block overlaps weighted by sqrt(2j_2+1)/sqrt(2j_0+1) (3 legs)."""
+    B = _blocks(sb, xb)
+    t = 0.0
+    for b, blk in _blocks(sa, xa).items():
+        a = sa.block_angm(b)
+        w = np.sqrt(a[2] + 1) / np.sqrt(a[0] + 1) if len(sa.bonds) == 3 else 1.0
+        t += float(np.sum(blk * B[b])) * w
+    return t
+
+
+def multiply_singular_value(s: Struct, x, leg: int, w):
+    """Each multiplet of `leg` scaled by its weight (sector by sector)."""
+    off = np.concatenate([[0], np.cumsum(s.bonds[leg].dim)])
+    y = np.array(x, np.float64, copy=True)
+    o, _ = s.offsets()
+    for b, blk in _blocks(s, x).items():
+        sec = (b // int(np.prod([len(q.angm) for q in s.bonds[:leg]], dtype=np.int64))) % len(s.bonds[leg].angm)
+        shape = [1] * len(s.bonds)
+        shape[leg] = blk.shape[leg]
+        scaled = blk * np.asarray(w[off[sec]: off[sec] + blk.shape[leg]]).reshape(shape)
+        y[o[b]: o[b] + blk.size] = scaled.ravel(order="F")
+    return y
+
+
+def mea_enr(hl, hr, ww, pairs):
+    """[tr hl + tr(W hr W) + sum coef ss(L, R)] / sum ww^2, hl/hr = (Struct, x),
+    pairs = [((Struct, x) | None, (Struct, x) | None, coef)]."""
+    num = take_trace(*hl)
+    s, x = hr
+    y = multiply_singular_value(s, multiply_singular_value(s, x, 0, ww), 1, ww)
+    num += take_trace(s, y)
+    for l, r, c in pairs:
+        if l is not None:
+            num += c * ss_inner_prod(l[0], l[1], r[0], r[1])
+    return num / float(np.sum(np.asarray(ww) ** 2))

@@ -7,6 +7,9 @@
 #                              missing-return patch (patch_ref.py)
 #   oracle/_ref/libsu2ref.so   the reference objects + harness.cpp, a C entry
 #                              layer used to generate golden fixtures
+#   oracle/_ref/libsu2ref_mea.so  the same with the engine's measurement
+#                              variant (dmrg_su2_omp_mea_enr.cpp) in place of
+#                              dmrg_su2_omp.cpp
 # Sources are copied to a scratch directory under /tmp and patched there; the
 # reference tree is never written and no reference source enters the repo.
 # BLAS/LAPACK come from SciPy's bundled OpenBLAS (blas_shim.c), the Fortran
@@ -36,10 +39,19 @@ for f in tensor tensor_dmrg_src tensor_su2 tensor_su2_dmrg_src tensor_su2_hamilt
 done
 g++ $CXXFLAGS -c "$WORK/main_omp.cpp" -o "$WORK/main_omp.o" &
 g++ $CXXFLAGS -c "$HERE/harness.cpp" -o "$WORK/harness.o" &
+g++ $CXXFLAGS -c "$WORK/dmrg_su2_omp_mea_enr.cpp" -o "$WORK/dmrg_su2_omp_mea_enr.o" &
+g++ $CXXFLAGS -DSU2REF_MEA -c "$HERE/harness.cpp" -o "$WORK/harness_mea.o" &
 gcc -O2 -fPIC -c "$REPO/oracle/fhelpers.c" -o "$WORK/fhelpers.o" &
 gcc -O2 -fPIC -c "$HERE/blas_shim.c" -o "$WORK/blas_shim.o" &
 for job in $(jobs -p); do wait "$job"; done
 LIBS=("$WORK/fhelpers.o" "$WORK/blas_shim.o" "$OPENBLAS" -Wl,-rpath,"$OBDIR" -fopenmp)
 g++ -o "$OUT/main_omp" "$WORK/main_omp.o" "${OBJS[@]}" "${LIBS[@]}"
 g++ -shared -o "$OUT/libsu2ref.so" "$WORK/harness.o" "${OBJS[@]}" "${LIBS[@]}"
-echo "built $OUT/main_omp and $OUT/libsu2ref.so"
+# the measurement variant of the engine (dmrg_su2_omp_mea_enr.cpp in place of
+# dmrg_su2_omp.cpp), for the centre-bond energy mea_enr
+MEA_OBJS=()
+for o in "${OBJS[@]}"; do
+  if [ "$o" = "$WORK/dmrg_su2_omp.o" ]; then MEA_OBJS+=("$WORK/dmrg_su2_omp_mea_enr.o"); else MEA_OBJS+=("$o"); fi
+done
+g++ -shared -o "$OUT/libsu2ref_mea.so" "$WORK/harness_mea.o" "${MEA_OBJS[@]}" "${LIBS[@]}"
+echo "built $OUT/main_omp, $OUT/libsu2ref.so and $OUT/libsu2ref_mea.so"

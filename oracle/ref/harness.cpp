@@ -509,6 +509,141 @@ int ref_checkpoint_read(int lx, int ly, int sec, int d, const char* dir, double*
   return ok ? ns : -2;
 }
 
+#ifdef SU2REF_MEA
+// Built only into libsu2ref_mea.so, where the measurement variant of the
+// engine (dmrg_su2_omp_mea_enr.cpp) replaces dmrg_su2_omp.cpp.
+//
+// The centre-bond energy of that variant on the checkpoint files in `dir`:
+//   engine 1 runs what its driver runs (main_omp.cpp:164-170: read_mps,
+//   read_enr, read_ww, then prepare_sweep, which ends in mea_enr,
+//   dmrg_su2_omp_mea_enr.cpp:160-242); parts[4] = its gs_enr[0];
+//   engine 2 builds the same environments (prepare_sweep's end tensors and
+//   site-operator loop, :165-186) without calling mea_enr, so that hh[ns/2]
+//   is not yet scaled, and exports hh[ns/2-1], hh[ns/2] and the operators of
+//   mea_enr's pair list (ref_idmrg_select), the pairs as ints = [npairs,
+//   left_idx, right_idx, ...], dbls = [coef, ...] in mea_enr's loop order
+//   (where none of its plaquette cases applies, mea_enr reuses the previous
+//   product, and so does the list).  parts[0..3] = tr hh[ns/2-1], tr of
+//   hh[ns/2] scaled by ww on both legs, the pair sum, sum ww^2, from the
+//   engine's own tensor_su2 members on engine 2's tensors; ww[0..d) to
+//   ww_out.  Returns the number of exported tensors, < 0 on failure.
+int ref_mea_enr(int lx, int ly, int sec, int d, double jcoup, double qcoup, int boundary, int nthreads,
+                const char* dir, double* parts, double* ww_out, int ww_cap) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return -1;
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  omp_set_nested(1);
+  omp_set_max_active_levels(2);
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* e1 = new dmrg_su2(lx, ly, sec, d, 0, 0);
+  chain_ptr = e1;
+  e1->set_ky(0);
+  bool ok = e1->read_mps(d, 0);
+  e1->read_enr(d, 0);
+  e1->read_ww(d, 0);
+  if (ok) e1->prepare_sweep();
+  parts[4] = e1->gs_enr[0];
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, d, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  ok = ok && c->read_mps(d, 0);
+  c->read_ww(d, 0);
+  if (chdir(cwd) != 0 || !ok) return -2;
+  const int ns = c->ns;
+  su2bond bb[4];
+  int a = 0, one = 1;
+  bb[0].set_su2bond(1, 1, &a, &one);
+  a = c->physpn;
+  bb[1].set_su2bond(1, 1, &a, &one);
+  c->uu[0].fuse(bb[0], bb[1]);
+  a = c->physpn;
+  bb[2].set_su2bond(1, 1, &a, &one);
+  a = c->totspin;
+  bb[3].set_su2bond(1, 1, &a, &one);
+  c->uu[ns - 1].fuse(bb[2], bb[3]);
+  for (int i = 0; i < ns / 2; ++i) {
+    c->prepare_site_operator_from_left(i, 0);
+    c->prepare_site_operator_from_right(ns - 1 - i, 0);
+  }
+  const int il = ns / 2 - 1, ir = ns / 2;
+  double* w = c->ww[0];
+  g_export = {&c->hh[il], &c->hh[ir]};
+  g_term_i.assign(1, 0);
+  g_term_d.clear();
+  auto idx = [&](tensor_su2* t) {
+    for (size_t q = 0; q < g_export.size(); ++q)
+      if (g_export[q] == t) return (int)q;
+    g_export.push_back(t);
+    return (int)g_export.size() - 1;
+  };
+  double pair_sum = 0;
+  tensor_su2 *pl = nullptr, *pr = nullptr;
+  auto pair = [&](tensor_su2* l, tensor_su2* r, double coef) {
+    g_term_i[0]++;
+    g_term_i.push_back(idx(l));
+    g_term_i.push_back(idx(r));
+    g_term_d.push_back(coef);
+    pair_sum += coef * l->ss_inner_prod(*r);
+    pl = l;
+    pr = r;
+  };
+  for (int i = 0; i < ns / 2; ++i)
+    for (int j = ns / 2; j < ns; ++j)
+      if (c->hmap[i][j] != 0) pair(&c->opr[il][i], &c->opr[ir][j], c->coup[c->hmap[i][j]]);
+  for (int m = 0; m < ns * 2; ++m) {
+    const int j = m % ns;
+    if (!(c->plqflg[il][j] && c->plqflg[ir][j])) continue;
+    const int* q = c->plqpos[j];
+    if (il >= q[0] && ir <= q[1]) pair(&c->opr[il][q[0]], &c->plqopr[ir][m], -qdelta);
+    else if (il >= q[1] && ir <= q[2]) pair(&c->plqopr[il][m], &c->plqopr[ir][m], -qdelta);
+    else if (il >= q[2] && ir <= q[3]) pair(&c->plqopr[il][m], &c->opr[ir][q[3]], -qdelta);
+    else if (pl) pair(pl, pr, -qdelta);
+  }
+  parts[0] = c->hh[il].take_trace();
+  g_result = c->hh[ir];
+  g_result.multiply_singular_value(0, w);
+  g_result.multiply_singular_value(1, w);
+  parts[1] = g_result.take_trace();
+  parts[2] = pair_sum;
+  double den = 0;
+  for (int i = 0; i < max_dcut; ++i) den += w[i] * w[i];
+  parts[3] = den;
+  for (int i = 0; i < d && i < ww_cap; ++i) ww_out[i] = w[i];
+  return (int)g_export.size();
+}
+#endif
+
+// tensor_su2::take_trace, ss_inner_prod and multiply_singular_value on given
+// block tensors (tensor_su2.cpp:359-384, 687-742); the scaled tensor becomes
+// the result (ref_result_*).
+double ref_take_trace(const int* d, const int* f, const double* x) {
+  build_tensor(g_result, d, f, x);
+  return g_result.take_trace();
+}
+double ref_ss_inner_prod(const int* da, const int* fa, const double* xa, const int* db, const int* fb,
+                         const double* xb) {
+  tensor_su2 b;
+  build_tensor(g_result, da, fa, xa);
+  build_tensor(b, db, fb, xb);
+  return g_result.ss_inner_prod(b);
+}
+int ref_multiply_singular_value(const int* d, const int* f, const double* x, int leg, const double* w) {
+  build_tensor(g_result, d, f, x);
+  g_result.multiply_singular_value(leg, const_cast<double*>(w));
+  g_sel = &g_result;
+  return 0;
+}
+
 int ref_run_dmrg(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
                  int nthreads, double* energies) {
   max_dcut = d;

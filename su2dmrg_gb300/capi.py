@@ -96,6 +96,10 @@ _PROTOS = {
     "su2g_vectran": (_i, [Tensor, _i, _vp, _vp]),
     "su2g_input_vector_layout": (_i, [Tensor, Tensor, _vp, _i, _vp, _i, _vp]),
     "su2g_prepare_input_vector": (_i, [Tensor, Tensor, _vp, _i, _vp]),
+    "su2g_take_trace": (_i, [Tensor, _vp, _vp]),
+    "su2g_ss_inner_prod": (_i, [Tensor, Tensor, _vp, _vp]),
+    "su2g_multiply_singular_value": (_i, [_vp, _vp, _vp, _i, _vp, _i64, _vp]),
+    "su2g_mea_enr": (_i, [Tensor, Tensor, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "su2g_checkpoint_name": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp, _i]),
     "su2g_mps_save": (_i, [_vp, _vp, Tensor, _vp]),
     "su2g_mps_load_layout": (_i, [_vp, _vp, _vp, _i, _vp, _i, _vp]),

@@ -536,6 +536,61 @@ def prepare_input_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, mode: int = capi.
 
 
 
+# ---------------------------------------------------------------- measurement
+def _opt_tensor(t, keep):
+    """(Su2Struct, data) or None (an operator never built) as a C tensor."""
+    if t is None:
+        return capi.Tensor(None, None, None)
+    return _tensor(t[0], t[1], keep)
+
+
+def take_trace(s: Su2Struct, x, stream=None) -> float:
+    keep = []
+    out = ctypes.c_double()
+    check(lib().su2g_take_trace(_tensor(s, x, keep), ctypes.addressof(out), stream_handle(stream)))
+    return out.value
+
+
+def ss_inner_prod(a, b, stream=None) -> float:
+    """a, b = (Su2Struct, device data) or None."""
+    keep = []
+    out = ctypes.c_double()
+    check(lib().su2g_ss_inner_prod(_opt_tensor(a, keep), _opt_tensor(b, keep), ctypes.addressof(out),
+                                   stream_handle(stream)))
+    return out.value
+
+
+def multiply_singular_value(s: Su2Struct, x, leg: int, w, stream=None) -> None:
+    """In place on the device data x."""
+    d = np.ascontiguousarray(s.desc(), np.int32)
+    f = np.ascontiguousarray(s.flag, np.int32)
+    wa = np.ascontiguousarray(w, np.float64)
+    check(lib().su2g_multiply_singular_value(ptr(d), ptr(f), ptr(x), int(leg), ptr(wa), wa.size,
+                                             stream_handle(stream)))
+
+
+def mea_enr(hl, hr, ww, pairs, stream=None):
+    """dmrg_su2::mea_enr: hl, hr = (Su2Struct, device data); pairs =
+    [(left, right, coef)] with left/right (Su2Struct, device data) or None.
+    Returns (energy, [tr hl, tr W hr W, pair sum, sum ww^2])."""
+    keep = []
+    n = len(pairs)
+    L = (capi.Tensor * max(1, n))()
+    R = (capi.Tensor * max(1, n))()
+    c = np.zeros(max(1, n))
+    for k, (l, r, cf) in enumerate(pairs):
+        L[k] = _opt_tensor(l, keep)
+        R[k] = _opt_tensor(r, keep)
+        c[k] = cf
+    wa = np.ascontiguousarray(ww, np.float64)
+    e = ctypes.c_double()
+    parts = np.zeros(4)
+    check(lib().su2g_mea_enr(_tensor(hl[0], hl[1], keep), _tensor(hr[0], hr[1], keep), ptr(wa), wa.size, n,
+                             ctypes.addressof(L), ctypes.addressof(R), ptr(c), ctypes.addressof(e), ptr(parts),
+                             stream_handle(stream)))
+    return e.value, parts
+
+
 # ---------------------------------------------------------------- checkpoints
 CKPT_MPS_DAT, CKPT_MPS_BIN, CKPT_ENR, CKPT_WW = 0, 1, 2, 3
 

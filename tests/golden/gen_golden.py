@@ -529,8 +529,87 @@ def checkpoint_cases(L):
     return case
 
 
+def measure_op_cases(L, rng):
+    """take_trace, ss_inner_prod and multiply_singular_value of the engine
+    (tensor_su2.cpp:359-384, 687-742) on random block tensors."""
+    L.ref_take_trace.restype = ctypes.c_double
+    L.ref_ss_inner_prod.restype = ctypes.c_double
+    cases = []
+    specs = [([0, 2, 4], [5, 9, 3], [2], [1]), ([1, 3, 5, 7], [4, 6, 2, 7], [2], [1]), ([0, 1, 2, 3], [3, 4, 5, 2], [0, 2], [1, 2])]
+    for ci, (sa, da, ss, ds) in enumerate(specs):
+        h = [(1, sa, da), (-1, sa, da)]
+        dh = desc_of(h)
+        fh = legal_flags(L, dh)
+        xh = random_data(h, fh, rng)
+        tr = L.ref_take_trace(p(dh), p(fh), p(xh))
+        w = rng.random(sum(da))
+        out = {}
+        for leg in (0, 1):
+            L.ref_multiply_singular_value(p(dh), p(fh), p(xh), leg, p(w))
+            _, y, _ = read_result(L)
+            out[f"msv{leg}"] = y
+        o = [(1, sa, da), (-1, ss, ds), (-1, sa, da)]
+        do = desc_of(o)
+        fb = legal_flags(L, do)
+        fa = (fb * (rng.random(len(fb)) >= 0.3)).astype(np.int32)
+        xa, xb = random_data(o, fa, rng), random_data(o, fb, rng)
+        ip = L.ref_ss_inner_prod(p(do), p(fa), p(xa), p(do), p(fb), p(xb))
+        cases.append(dict(name=f"meaop_{ci}", dh=dh, fh=fh, xh=xh, trace=np.float64(tr), w=w, do=do, fa=fa, xa=xa,
+                          fb=fb, xb=xb, inner=np.float64(ip), **out))
+    return cases
+
+
+def mea_cases(L):
+    """The centre-bond energy of the engine's measurement variant
+    (prepare_sweep + mea_enr, dmrg_su2_omp_mea_enr.cpp:160-242, built into
+    libsu2ref_mea.so) on checkpoint files the engine wrote after do_idmrg and
+    one sweep: the centre tensors, the pair list, the weights, the parts and
+    the energy mea_enr returned, next to the sweep's Lanczos energy."""
+    M = ctypes.CDLL(REFLIB.replace("libsu2ref.so", "libsu2ref_mea.so"))
+    M.ref_setup(1, 25)
+    L.ref_checkpoint_write.restype = ctypes.c_int
+    cases = []
+    for ci, (lx, ly, d, jc, qc) in enumerate([(4, 2, 16, 1.0, 0.0), (4, 4, 24, 1.0, 1.0)]):
+        tmp = tempfile.mkdtemp()
+        e = ctypes.c_double()
+        ns = L.ref_checkpoint_write(lx, ly, 0, d, 1, ctypes.c_double(jc), ctypes.c_double(qc), 2, 1, tmp.encode(),
+                                    ctypes.byref(e))
+        assert ns > 0
+        parts = np.zeros(5)
+        ww = np.zeros(4096)
+        n = M.ref_mea_enr(lx, ly, 0, d, ctypes.c_double(jc), ctypes.c_double(qc), 2, 1, tmp.encode(), p(parts), p(ww),
+                          len(ww))
+        assert n > 0, n
+        case = dict(name=f"mea_{ci}", lx=np.int32(lx), ly=np.int32(ly), d=np.int32(d), parts=parts, ww=ww[:d].copy(),
+                    lanczos=np.float64(e.value + 1000.0), nexp=np.int32(n))
+        for i in range(n):
+            M.ref_idmrg_select(i)
+            dd = np.zeros(1024, np.int32)
+            nd = M.ref_result_desc(p(dd))
+            if nd <= 2:  # an operator never built
+                case[f"d{i}"] = dd[:0]
+                continue
+            flag, x1, _ = read_result(M)
+            case.update({f"d{i}": dd[:nd].copy(), f"f{i}": flag, f"x{i}": x1})
+        ints = np.zeros(1 << 16, np.int32)
+        dbls = np.zeros(1 << 16)
+        ni = M.ref_idmrg_terms(p(ints), len(ints), p(dbls), len(dbls))
+        case.update(pairs=ints[:ni].copy(), coefs=dbls[: int(ints[0])].copy())
+        cases.append(case)
+        import shutil
+        shutil.rmtree(tmp)
+    return cases
+
+
 def main():
     L = ctypes.CDLL(REFLIB)
+    if "--only-mea" in sys.argv:
+        L.ref_setup(1, 25)
+        rng = np.random.Generator(np.random.PCG64(777))
+        for c in measure_op_cases(L, rng) + mea_cases(L):
+            name = c.pop("name")
+            np.savez(os.path.join(HERE, name + ".npz"), **c)
+        return
     if "--only-ckpt" in sys.argv:
         L.ref_setup(1, 25)
         np.savez(os.path.join(HERE, "ckpt_engine.npz"), **checkpoint_cases(L))
@@ -561,6 +640,9 @@ def main():
             name = c.pop("name")
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **c)
     np.savez(os.path.join(HERE, "ckpt_engine.npz"), **checkpoint_cases(L))
+    for c in measure_op_cases(L, np.random.Generator(np.random.PCG64(777))) + mea_cases(L):
+        name = c.pop("name")
+        np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)

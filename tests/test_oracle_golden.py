@@ -251,3 +251,38 @@ def test_vectran_matches_reference(oracle, path):
     assert out.desc().tolist() == g["rdesc"].tolist()
     assert out.flag.tolist() == g["rflag"].tolist()
     assert np.array_equal(y, g["rx"])
+
+
+def _mea_tensor(oracle, g, i):
+    d = g[f"d{i}"]
+    if len(d) == 0:
+        return None
+    return oracle.struct_from_desc(d, g[f"f{i}"]), g[f"x{i}"]
+
+
+def mea_case(oracle, g):
+    """(hl, hr, ww, [(left, right, coef)]) of a mea_*.npz fixture (oracle structs, host data)."""
+    ints, coefs = g["pairs"], g["coefs"]
+    pairs = [(_mea_tensor(oracle, g, int(ints[1 + 2 * k])), _mea_tensor(oracle, g, int(ints[2 + 2 * k])), float(coefs[k]))
+             for k in range(int(ints[0]))]
+    return _mea_tensor(oracle, g, 0), _mea_tensor(oracle, g, 1), g["ww"], pairs
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "meaop_*.npz"))))
+def test_measure_reductions_match_reference(oracle, path):
+    g = np.load(path)
+    sh = oracle.struct_from_desc(g["dh"], g["fh"])
+    assert abs(oracle.take_trace(sh, g["xh"]) - g["trace"]) <= 1e-13 * max(1.0, abs(g["trace"]))
+    for leg in (0, 1):
+        assert np.allclose(oracle.multiply_singular_value(sh, g["xh"], leg, g["w"]), g[f"msv{leg}"], rtol=0, atol=1e-15)
+    sa, sb = oracle.struct_from_desc(g["do"], g["fa"]), oracle.struct_from_desc(g["do"], g["fb"])
+    assert abs(oracle.ss_inner_prod(sa, g["xa"], sb, g["xb"]) - g["inner"]) <= 1e-13 * max(1.0, abs(g["inner"]))
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "mea_*.npz"))))
+def test_mea_enr_matches_reference(oracle, path):
+    """The measurement variant's own mea_enr value, from its centre tensors."""
+    g = np.load(path)
+    hl, hr, ww, pairs = mea_case(oracle, g)
+    e = oracle.mea_enr(hl, hr, ww, pairs)
+    assert abs(e - g["parts"][4]) <= 1e-12 * abs(g["parts"][4])
