@@ -287,6 +287,21 @@ int su2g_vectran_layout(su2g_tensor u, int flag, int* out_desc, int out_desc_cap
                         int64_t* out_len);
 int su2g_vectran(su2g_tensor u, int flag, double* out, void* stream);
 
+/* tensor_su2::fuse(b1, b2) (tensor_su2.cpp:839-909), the MPS tensor the
+ * warm-up starts each new site with (do_idmrg, dmrg_su2_omp.cpp:30-66): legs
+ * (b1, b2, fuse(b1, b2) of direction -b1), every legal block present, each
+ * block the rows of an identity placed where tensor_su2::fuse places them.
+ * bonds_desc = a 2-leg desc holding b1 and b2 (locspin ignored); out (device)
+ * has the layout su2g_fuse_tensor_layout reports. */
+int su2g_fuse_tensor_layout(const int* bonds_desc, int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap,
+                            int64_t* out_len);
+int su2g_fuse_tensor(const int* bonds_desc, double* out, void* stream);
+/* The warm-up's two-site start vector (prepare_input_vector_initial +
+ * initialize_input_vector + normalize_vector, dmrg_su2_omp.cpp:196-216,
+ * 79-80): the structure of su2g_prepare_input_vector's vector with every
+ * element 1/sqrt(N), N its length. */
+int su2g_initial_vector(su2g_tensor ul, su2g_tensor ur, double* out, void* stream);
+
 /* dmrg_su2::prepare_input_vector(il, ir, vec) (dmrg_su2_omp.cpp:229-254):
  * the initial two-site vector of a step from ul = uu[il] and ur = uu[ir]
  * (device data; legs 0 and 1 of each of one direction, leg 2 the same bond

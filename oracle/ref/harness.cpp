@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <iostream>
 #include <algorithm>
 #include <vector>
 #include <unistd.h>
@@ -270,7 +271,10 @@ int ref_idmrg_capture(int lx, int ly, int sec, int d, int niter, double jcoup, d
   dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
   chain_ptr = c;
   c->set_ky(0);
+  // the step eigenvalues the engine prints (dmrg_su2.cpp:539), in full
+  std::streamsize prec = std::cout.precision(17);
   c->do_idmrg();
+  std::cout.precision(prec);
   energies[0] = c->get_enr();
   for (int i = 0; i < niter; ++i) {
     c->sweep();
@@ -363,6 +367,51 @@ int ref_prepare_input_vector(const int* dl, const int* fl, const double* xl, con
 
 // uu.right2left_vectran() (dir 0) / uu.left2right_vectran() (dir 1), the
 // step of dmrg_su2::wavefunc_transformation (dmrg_su2_omp.cpp:1864-1877)
+// The warm-up's initial two-site vector (dmrg_su2_omp.cpp:196-216 and
+// do_idmrg :79-80): prepare_input_vector_initial's fuse / overlap_initial /
+// fuse_to_singlet / contract sequence on ul = uu[il], ur = uu[ir], then
+// initialize_input_vector and normalize_vector; the result is g_result.
+int ref_input_vector_initial(const int* dl, const int* fl, const double* xl, const int* dr, const int* fr,
+                             const double* xr) {
+  tensor_su2 ul, ur, tmp1, tmp2, left, rght, tmp, tmp3;
+  build_tensor(ul, dl, fl, xl);
+  build_tensor(ur, dr, fr, xr);
+  su2bond bb[4];
+  ul.get_su2bond(0, bb[0]);
+  ul.get_su2bond(1, bb[1]);
+  ur.get_su2bond(0, bb[2]);
+  ur.get_su2bond(1, bb[3]);
+  tmp1.fuse(bb[0], bb[1]);
+  tmp2.fuse(bb[2], bb[3]);
+  left.overlap_initial(ul, tmp1, 0);
+  rght.overlap_initial(ur, tmp2, 1);
+  left.get_su2bond(0, bb[0]);
+  rght.get_su2bond(0, bb[1]);
+  bb[0].invert_bonddir();
+  bb[1].invert_bonddir();
+  tmp.fuse_to_singlet(bb[0], bb[1]);
+  tmp3.contract(left, 0, tmp, 0);
+  g_result.contract(tmp3, 1, rght, 0);
+  g_result.makeup_input_vector();
+  g_result.initialize_input_vector();
+  g_result.normalize_vector();
+  g_sel = &g_result;
+  return 0;
+}
+
+// tensor_su2::fuse(b1, b2) (tensor_su2.cpp:839-909) of the two legs of a
+// 2-leg desc; the result is g_result.
+int ref_fuse_tensor(const int* bonds_desc) {
+  su2struct s;
+  desc_to_struct(bonds_desc, s);
+  su2bond b1, b2;
+  s.get_su2bond(0, b1);
+  s.get_su2bond(1, b2);
+  g_result.fuse(b1, b2);
+  g_sel = &g_result;
+  return 0;
+}
+
 int ref_vectran(const int* du, const int* fu, const double* xu, int dir) {
   build_tensor(g_result, du, fu, xu);
   if (dir == 0) g_result.right2left_vectran();
@@ -471,7 +520,10 @@ int ref_checkpoint_write(int lx, int ly, int sec, int d, int niter, double jcoup
   dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
   chain_ptr = c;
   c->set_ky(0);
+  // the step eigenvalues the engine prints (dmrg_su2.cpp:539), in full
+  std::streamsize prec = std::cout.precision(17);
   c->do_idmrg();
+  std::cout.precision(prec);
   for (int i = 0; i < niter; ++i) c->sweep();
   c->save_mps2();
   c->save_enr();
@@ -642,6 +694,75 @@ int ref_multiply_singular_value(const int* d, const int* f, const double* x, int
   g_result.multiply_singular_value(leg, const_cast<double*>(w));
   g_sel = &g_result;
   return 0;
+}
+
+// The engine's lattice tables and site operators (dmrg_su2.cpp:31-300,
+// initialize_local_operators) for a device-side warm-up:
+//   ints = [ns, physpn, totspin, hmap (ns x ns), fll (ns x ns), frr (ns x ns),
+//           plqflg (ns x ns), plqpos (ns x 4)]   (row-major)
+//   dbls = [coup[0..ns)]
+// and exports sigma[0], sigma[1], qterm[0..8) (ref_idmrg_select 0..9).
+// Returns the int count, -1 if a capacity is too small.
+int ref_engine_tables(int lx, int ly, int sec, int d, double jcoup, double qcoup, int boundary, int* ints, int icap,
+                      double* dbls, int dcap) {
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  const int ns = c->ns;
+  if (icap < 3 + 4 * ns * ns + 4 * ns || dcap < ns) return -1;
+  int p = 0;
+  ints[p++] = ns;
+  ints[p++] = c->physpn;
+  ints[p++] = c->totspin;
+  for (int** t : {c->hmap, c->fll, c->frr, c->plqflg})
+    for (int i = 0; i < ns; ++i)
+      for (int j = 0; j < ns; ++j) ints[p++] = t[i][j];
+  for (int i = 0; i < ns; ++i)
+    for (int k = 0; k < 4; ++k) ints[p++] = c->plqpos[i][k];
+  for (int i = 0; i < ns; ++i) dbls[i] = c->coup[i];
+  g_export = {&c->sigma[0], &c->sigma[1]};
+  for (int k = 0; k < 8; ++k) g_export.push_back(&c->qterm[k]);
+  return p;
+}
+
+// The reference warm-up alone (do_idmrg, dmrg_su2_omp.cpp:20-95): *enr =
+// gs_enr + 1000 after it (the eigenvalue of the last step), ww[0..d) its
+// last truncation's singular values.
+int ref_warmup(int lx, int ly, int sec, int d, double jcoup, double qcoup, int boundary, int nthreads, double* enr,
+               double* ww_out, int ww_cap) {
+  max_dcut = d;
+  bdry = boundary;
+  delta = jcoup;
+  qdelta = qcoup;
+  memory_flag = 0;
+  psize = nthreads;
+  omp_set_num_threads(nthreads);
+  mkl_set_num_threads(1);
+  omp_set_nested(1);
+  omp_set_max_active_levels(2);
+  if (ly > 1) {
+    cosk = cos(0.0);
+    coskminus = cosk;
+  }
+  dmrg_su2* c = new dmrg_su2(lx, ly, sec, 0, 0, 0);
+  chain_ptr = c;
+  c->set_ky(0);
+  // the step eigenvalues the engine prints (dmrg_su2.cpp:539), in full
+  std::streamsize prec = std::cout.precision(17);
+  c->do_idmrg();
+  std::cout.precision(prec);
+  *enr = c->gs_enr[0] + 1000.0;
+  for (int i = 0; i < d && i < ww_cap; ++i) ww_out[i] = c->ww[0][i];
+  return c->ns;
 }
 
 int ref_run_dmrg(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,

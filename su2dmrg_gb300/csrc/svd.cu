@@ -44,6 +44,37 @@ __global__ void scale_columns(double* a, int rows, int c0, int ncol, int ld, con
   }
 }
 
+// The eigenvector sign rule of su2g::canonical_column_signs (tridiag.hpp)
+// on the device: one CTA per column of the rows x cols matrix z (ld rows).
+// The largest magnitude and the first index above 1e-4 of it are exact
+// reductions (max, min), so the choice does not depend on the order.
+__global__ void __launch_bounds__(256) canonical_signs_kernel(double* z, int rows) {
+  __shared__ double smax[8];
+  __shared__ int sfirst[8];
+  double* col = z + (int64_t)blockIdx.x * rows;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double mx = 0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) mx = fmax(mx, fabs(col[i]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) smax[wid] = mx;
+  __syncthreads();
+  mx = smax[0];
+  for (int w = 1; w < 8; ++w) mx = fmax(mx, smax[w]);
+  int first = rows;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x)
+    if (fabs(col[i]) > 1e-4 * mx) {
+      first = i;
+      break;
+    }
+  for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+  if (lane == 0) sfirst[wid] = first;
+  __syncthreads();
+  first = sfirst[0];
+  for (int w = 1; w < 8; ++w) first = min(first, sfirst[w]);
+  if (first < rows && col[first] < 0)
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) col[i] = -col[i];
+}
+
 // Per-device resources kept across calls: one stream and one pair of
 // cuBLAS / cuSOLVER handles per concurrently processed sector (creating
 // handles costs milliseconds), and a library-private memory pool whose freed
@@ -145,7 +176,8 @@ struct Ctx {
     cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
   }
-  // symmetric eigendecomposition in place (a: n x n, ld n); w: host eigenvalues
+  // symmetric eigendecomposition in place (a: n x n, ld n), eigenvector signs
+  // by the canonical rule; w: host eigenvalues
   void eigh(double* a, int n, std::vector<double>* w) {
     if (!ok()) return;
     int lwork = 0;
@@ -167,6 +199,10 @@ struct Ctx {
     w->assign(n, 0.0);
     int info = 0;
     cudaError_t e = cudaMemcpyAsync(w->data(), dw, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && n > 0) {
+      canonical_signs_kernel<<<n, 256, 0, st>>>(a, n);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));

@@ -4,7 +4,8 @@
 // on the dense matrix (Golub & Van Loan, "Matrix Computations", sec. 8.5):
 // unconditionally convergent and accurate to a few ulps of the matrix norm for
 // these sizes.  Eigenvalues ascending; eigenvectors column-major in z
-// (column j belongs to eigenvalue j), each of unit length.
+// (column j belongs to eigenvalue j), each of unit length.  Column signs,
+// which dstev leaves to the LAPACK build, follow canonical_column_signs.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -12,6 +13,25 @@
 #include <vector>
 
 namespace su2g {
+
+// Sign rule for eigenvectors: in each column of the rows x cols matrix z
+// (column-major, leading dimension ld) the first entry whose magnitude exceeds
+// 1e-4 of the column's largest is made positive.  The reference takes the
+// signs LAPACK happens to return; fixing them makes results independent of
+// the eigen-solver (the svd's device eigenvectors follow the same rule).
+inline void canonical_column_signs(int rows, int cols, double* z, int ld) {
+  for (int c = 0; c < cols; ++c) {
+    double* col = z + (size_t)c * ld;
+    double mx = 0;
+    for (int i = 0; i < rows; ++i) mx = std::max(mx, std::fabs(col[i]));
+    for (int i = 0; i < rows; ++i)
+      if (std::fabs(col[i]) > 1e-4 * mx) {
+        if (col[i] < 0)
+          for (int k = 0; k < rows; ++k) col[k] = -col[k];
+        break;
+      }
+  }
+}
 
 inline void tridiag_eigh(const std::vector<double>& d, const std::vector<double>& e, std::vector<double>* w,
                          std::vector<double>* z) {
@@ -64,6 +84,7 @@ inline void tridiag_eigh(const std::vector<double>& d, const std::vector<double>
     (*w)[j] = a[order[j] + order[j] * n];
     for (int i = 0; i < n; ++i) (*z)[i + j * n] = v[i + order[j] * n];
   }
+  canonical_column_signs(n, n, z->data(), n);
 }
 
 }  // namespace su2g

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -137,6 +138,47 @@ cudaError_t launch_transposes(std::vector<TrItem>& items, cudaStream_t st) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFreeAsync(d_items, st);
   return e;
+}
+
+// One identity placement of a fuse tensor: block rows r (< rows) carry a 1 in
+// column r + shift (tensor::shift_set_identity, tensor.cpp:1411-1432).
+struct OneItem {
+  double* blk;
+  int rows, shift;
+};
+
+__global__ void place_ones_kernel(const OneItem* __restrict__ items, int n) {
+  const OneItem it = items[blockIdx.y];
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < it.rows; r += gridDim.x * blockDim.x)
+    it.blk[r + (int64_t)(r + it.shift) * it.rows] = 1.0;
+}
+
+__global__ void fill_kernel(double* x, int64_t n, double v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = v;
+}
+
+// fuse tensor of the two legs of a 2-leg desc: legs (b1, b2, fuse(b1, b2)),
+// every legal block present (tensor_su2::fuse, tensor_su2.cpp:839-909)
+int fuse_struct(const int* bonds_desc, su2g::Struct* out, std::string* err) {
+  su2g::Struct b;
+  if (!bonds_desc || !b.parse(bonds_desc, err)) return SU2G_EINVAL;
+  if (b.nbond != 2) {
+    *err = "two bonds expected";
+    return SU2G_EINVAL;
+  }
+  if (b.legs[0].dir != b.legs[1].dir) {  // su2bond::fuse refuses them (su2bond.cpp:159-162)
+    *err = "bonds of different directions";
+    return SU2G_EINVAL;
+  }
+  *out = su2g::Struct();
+  out->nbond = 3;
+  out->locspin = 0;
+  out->legs[0] = b.legs[0];
+  out->legs[1] = b.legs[1];
+  out->legs[2] = su2g::fuse(b.legs[0], b.legs[1]);
+  out->nten = out->legs[0].n() * out->legs[1].n() * out->legs[2].n();
+  out->set_layout(nullptr);
+  return SU2G_OK;
 }
 
 int write_layout(const su2g::Struct& s, int* out_desc, int out_desc_cap, int* out_flag, int out_flag_cap,
@@ -303,3 +345,64 @@ extern "C" int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double*
   if (e != cudaSuccess) return cuda_fail(e, "prepare_input_vector");
   return rc;
 }
+
+extern "C" int su2g_fuse_tensor_layout(const int* bonds_desc, int* out_desc, int out_desc_cap, int* out_flag,
+                                       int out_flag_cap, int64_t* out_len) {
+  su2g::Struct f;
+  std::string err;
+  if (fuse_struct(bonds_desc, &f, &err)) return fail(SU2G_EINVAL, "fuse_tensor: " + err);
+  return write_layout(f, out_desc, out_desc_cap, out_flag, out_flag_cap, out_len, "fuse_tensor_layout");
+}
+
+extern "C" int su2g_fuse_tensor(const int* bonds_desc, double* out, void* stream) {
+  su2g::Struct f;
+  std::string err;
+  if (fuse_struct(bonds_desc, &f, &err)) return fail(SU2G_EINVAL, "fuse_tensor: " + err);
+  if (f.total == 0) return SU2G_OK;
+  if (!out) return fail(SU2G_EINVAL, "fuse_tensor: null output");
+  std::vector<OneItem> items;
+  for (int b = 0; b < f.nten; ++b) {
+    if (!f.flag[b]) continue;
+    int sec[3];
+    f.sectors(b, sec);
+    const int c = f.legs[2].angm[sec[2]];
+    const int r0 = su2g::fused_row(f.legs[0], f.legs[1], c, sec[0], sec[1]);
+    if (r0 < 0) return fail(SU2G_EINVAL, "fuse_tensor: internal placement error");
+    items.push_back(OneItem{out + f.offset[b], f.legs[0].dim[sec[0]] * f.legs[1].dim[sec[1]], r0});
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  OneItem* d_items = nullptr;
+  cudaError_t e = cudaMemsetAsync(out, 0, f.total * sizeof(double), st);
+  if (e == cudaSuccess && items.size() > 65535) e = cudaErrorInvalidValue;
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_items, items.size() * sizeof(OneItem), st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(OneItem), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    int maxr = 1;
+    for (const OneItem& it : items) maxr = std::max(maxr, it.rows);
+    place_ones_kernel<<<dim3((maxr + 255) / 256, (unsigned)items.size()), 256, 0, st>>>(d_items, (int)items.size());
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host list must outlive the copy
+  if (d_items) cudaFreeAsync(d_items, st);
+  if (e != cudaSuccess) return cuda_fail(e, "fuse_tensor");
+  return SU2G_OK;
+}
+
+extern "C" int su2g_initial_vector(su2g_tensor ul, su2g_tensor ur, double* out, void* stream) {
+  su2g::Struct v;
+  su2g::HeffWork w;
+  std::string err;
+  int rc = su2g::build_input_vector(ul, ur, nullptr, nullptr, &v, &w, &err);
+  if (rc) return fail(rc, "initial_vector: " + err);
+  if (v.total == 0) return SU2G_OK;
+  if (!out) return fail(SU2G_EINVAL, "initial_vector: null output");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int grid = (int)std::min<int64_t>((v.total + 255) / 256, (int64_t)sm_count() * 4);
+  fill_kernel<<<grid, 256, 0, st>>>(out, v.total, 1.0 / std::sqrt((double)v.total));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "initial_vector");
+  return SU2G_OK;
+}
+

@@ -536,6 +536,33 @@ def prepare_input_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, mode: int = capi.
 
 
 
+def fuse_tensor(b1: Su2Bond, b2: Su2Bond, device="cuda", stream=None):
+    """tensor_su2::fuse(b1, b2): returns (Su2Struct, device tensor)."""
+    import torch
+
+    bd = Su2Struct([b1, b2], 0).desc()
+    s = _layout_out(lib().su2g_fuse_tensor_layout, ptr(bd))
+    y = torch.empty(max(1, s.size()), dtype=torch.float64, device=device)
+    check(lib().su2g_fuse_tensor(ptr(bd), ptr(y), stream_handle(stream)))
+    return s, y
+
+
+def fuse_tensor_layout(b1: Su2Bond, b2: Su2Bond) -> Su2Struct:
+    bd = Su2Struct([b1, b2], 0).desc()
+    return _layout_out(lib().su2g_fuse_tensor_layout, ptr(bd))
+
+
+def initial_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, stream=None):
+    """The warm-up's start vector on prepare_input_vector's structure."""
+    import torch
+
+    keep = []
+    s = input_vector_layout(ul, ur)
+    y = torch.empty(max(1, s.size()), dtype=torch.float64, device=xl.device)
+    check(lib().su2g_initial_vector(_tensor(ul, xl, keep), _tensor(ur, xr, keep), ptr(y), stream_handle(stream)))
+    return s, y
+
+
 # ---------------------------------------------------------------- measurement
 def _opt_tensor(t, keep):
     """(Su2Struct, data) or None (an operator never built) as a C tensor."""

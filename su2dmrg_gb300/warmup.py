@@ -1,0 +1,306 @@
+"""Warm-up of a DMRG run with every tensor on the device.
+
+dmrg_su2::do_idmrg (dmrg_su2_omp.cpp:20-95) grows the MPS from both ends to
+the centre: at each step the site operators of the two new sites are built
+(prepare_site_operator_from_left / _right, :319-603 and :604-827), the two
+new sites start as fuse tensors (tensor_su2::fuse), and once the block is
+large enough the two-site ground state is found (Lanczos from the uniform
+start vector, lanczos_solve_eigenvector_idmrg dmrg_su2.cpp:527-540) and
+truncated (tensor_su2::svd).  This module drives that sequence over the C ABI
+of libsu2g: MPS tensors, block Hamiltonians, site operators, plaquette
+operators and the two-site vector stay in device memory from the first step
+to the last; only structures, the engine's lattice tables and its one-site
+operators (a few doubles) live on the host.
+
+The lattice (hmap, coup, fll, frr, plqflg, plqpos) and the one-site
+operators (sigma, qterm) are the engine's own tables (built by its
+constructor and initialize_local_operators, dmrg_su2.cpp:31-300); they are
+inputs here.  Only the ground state (exci = 0) is covered: the excited-state
+overlaps (ovlp, orth) are not built.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from . import su2 as S
+
+
+@dataclass
+class Lattice:
+    """The engine tables the warm-up reads (dmrg_su2.cpp:31-300)."""
+    ns: int
+    physpn: int
+    totspin: int
+    hmap: np.ndarray    # (ns, ns): index into coup of the coupling of sites (i, k), 0 = none
+    coup: np.ndarray    # (ns,)
+    fll: np.ndarray     # (ns, ns): opr[i][k] is carried to the left block at site i
+    frr: np.ndarray     # (ns, ns): ... to the right block
+    plqflg: np.ndarray  # (ns, ns): plaquette j passes site i
+    plqpos: np.ndarray  # (ns, 4): the four sites of plaquette j
+    qdelta: float
+    sigma: list         # [(Su2Struct, host data)] x 2: the one-site spin operators
+    qterm: list         # [(Su2Struct, host data)] x 8: the plaquette permutation operators
+    max_dcut: int
+
+    @classmethod
+    def from_tables(cls, ints, coup, sites, qdelta: float, max_dcut: int) -> "Lattice":
+        """From the flat layout [ns, physpn, totspin, hmap, fll, frr, plqflg
+        (each ns x ns, row-major), plqpos (ns x 4)], coup[0..ns) and the ten
+        one-site operators [sigma[0], sigma[1], qterm[0..8)] as (desc, flag,
+        host data) (desc of length <= 2: never built)."""
+        ints = np.asarray(ints)
+        ns, q = int(ints[0]), 3
+        mats = []
+        for _ in range(4):
+            mats.append(ints[q: q + ns * ns].reshape(ns, ns).copy())
+            q += ns * ns
+        plqpos = ints[q: q + 4 * ns].reshape(ns, 4).copy()
+        ops = []
+        for desc, flag, x in sites:
+            if len(desc) <= 2:
+                ops.append(None)
+                continue
+            st = S._parse_desc(desc)
+            st.flag = np.ascontiguousarray(flag, np.int32)
+            ops.append((st, np.ascontiguousarray(x, np.float64)))
+        return cls(ns, int(ints[1]), int(ints[2]), mats[0], np.asarray(coup, np.float64), mats[1], mats[2], mats[3],
+                   plqpos, float(qdelta), ops[:2], ops[2:10], int(max_dcut))
+
+
+@dataclass
+class _Jobs:
+    """One environment batch: jobs and their named output slots."""
+    jobs: list = field(default_factory=list)
+    names: list = field(default_factory=list)
+
+    def add(self, name, kind, x=None, site1=None, site2=None, coef=1.0):
+        if name not in self.names:
+            self.names.append(name)
+        j = {"kind": kind, "slot": self.names.index(name), "coef": coef, "x": x}
+        if site1 is not None:
+            j["site1"] = site1
+        if site2 is not None:
+            j["site2"] = site2
+        self.jobs.append(j)
+
+
+class Warmup:
+    """do_idmrg on the device.  mode: capi.MODE_* for every contraction."""
+
+    def __init__(self, lat: Lattice, mode: int = capi.MODE_F64, mlanc: int = 5):
+        self.lat, self.mode, self.mlanc = lat, mode, mlanc
+        ns = lat.ns
+        self.uu = [None] * ns
+        self.hh = [None] * ns
+        self.opr = [[None] * ns for _ in range(ns)]
+        self.plq = [[None] * (2 * ns) for _ in range(ns)]
+        self.energies = []   # (il, ir, eigenvalue) per Lanczos step
+        self.ww = None       # singular values of the last truncation
+        self._keep = []
+
+    # ---------------------------------------------------------- helpers
+    def _run(self, u, flag, b: _Jobs):
+        if not b.jobs:
+            return {}
+        res = S.env_batch(u[0], u[1], u[0], u[1], flag, b.jobs, mode=self.mode)
+        return {name: (st, x[: st.size()]) for name, (st, x) in zip(b.names, res)}
+
+    def _combine(self, lst):
+        """sum c * op over [(op, c)], None when empty (tensor_su2 += of scaled copies)."""
+        lst = [(t, c) for t, c in lst if t is not None]
+        if not lst:
+            return None
+        if len(lst) == 1 and lst[0][1] == 1.0:
+            return lst[0][0]
+        r = S.operator_combine([t for t, _ in lst], [c for _, c in lst])
+        return r[0], r[1][: r[0].size()]
+
+    @staticmethod
+    def _legs01(u):
+        return u[0].bonds[0], u[0].bonds[1]
+
+    # ---------------------------------------------------- site updates
+    def site_left(self, i: int, u):
+        """prepare_site_operator_from_left(i[, flag]) with MPS tensor u at site i."""
+        L, p = self.lat, self.lat.plqpos
+        if i == 0:
+            b = _Jobs()
+            b.add(("opr", 0), "init", site1=L.sigma[0])
+            self.opr[0][0] = self._run(u, 0, b)[("opr", 0)]
+            self.hh[0] = None
+            return
+        b = _Jobs()
+        if self.hh[i - 1] is not None:
+            b.add("hh", "overlap", x=self.hh[i - 1])
+        for k in range(i):
+            if L.fll[i][k] == 1:
+                b.add(("opr", k), "transform", x=self.opr[i - 1][k])
+        op = self._combine([(self.opr[i - 1][k], float(L.coup[L.hmap[i][k]])) for k in range(i) if L.hmap[i][k] > 0])
+        if op is not None:
+            b.add("hh", "pair", x=op, site1=L.sigma[1])
+        b.add(("opr", i), "init", site1=L.sigma[0])
+        for m in range(2 * L.ns):
+            j, k = m % L.ns, m // L.ns
+            if L.plqflg[i][j] == 0 or i < p[j][1]:
+                continue
+            prev = self.plq[i - 1][m]
+            if k == 0:
+                if i == p[j][1]:
+                    b.add(("plq", m), "pair", x=self.opr[i - 1][p[j][0]], site1=L.sigma[1])
+                elif i == p[j][2]:
+                    b.add(("plq", m), "init", x=prev, site1=L.sigma[0])
+                elif i == p[j][3]:
+                    b.add(("plq", m), "pair", x=prev, site1=L.sigma[1], coef=-L.qdelta)
+                    b.add("hh", "pair", x=prev, site1=L.sigma[1], coef=-L.qdelta)
+                elif p[j][1] < i < p[j][2]:
+                    b.add(("plq", m), "overlap", x=prev)
+                elif p[j][2] < i < p[j][3]:
+                    b.add(("plq", m), "transform", x=prev)
+            else:
+                if i == p[j][1]:
+                    b.add(("plq", m), "perm", x=self.opr[i - 1][p[j][0]], site1=L.qterm[0], site2=L.qterm[1])
+                elif i == p[j][2]:
+                    b.add(("plq", m), "perm", x=prev, site1=L.qterm[2], site2=L.qterm[3])
+                elif i == p[j][3]:
+                    b.add(("plq", m), "pair", x=prev, site1=L.sigma[1], coef=-L.qdelta)
+                    b.add("hh", "pair", x=prev, site1=L.sigma[1], coef=-L.qdelta)
+                elif p[j][1] < i < p[j][2] or p[j][2] < i < p[j][3]:
+                    b.add(("plq", m), "transform", x=prev)
+        out = self._run(u, 0, b)
+        self.hh[i] = out.get("hh")
+        for name, t in out.items():
+            if isinstance(name, tuple) and name[0] == "opr":
+                self.opr[i][name[1]] = t
+            elif isinstance(name, tuple):
+                self.plq[i][name[1]] = t
+
+    def site_right(self, i: int, u):
+        """prepare_site_operator_from_right(i[, flag]) with MPS tensor u at site i."""
+        L, p, ns = self.lat, self.lat.plqpos, self.lat.ns
+        if i == ns - 1:
+            b = _Jobs()
+            b.add(("opr", i), "init", site1=L.sigma[1])
+            self.opr[i][i] = self._run(u, 1, b)[("opr", i)]
+            self.hh[i] = None
+            return
+        b = _Jobs()
+        if self.hh[i + 1] is not None:
+            b.add("hh", "overlap", x=self.hh[i + 1])
+        for k in range(i + 1, ns):
+            if L.frr[i][k] == 1:
+                b.add(("opr", k), "transform", x=self.opr[i + 1][k])
+        op = self._combine([(self.opr[i + 1][k], float(L.coup[L.hmap[i][k]])) for k in range(i + 1, ns)
+                            if L.hmap[i][k] > 0])
+        if op is not None:
+            b.add("hh", "pair", x=op, site1=L.sigma[0])
+        b.add(("opr", i), "init", site1=L.sigma[1])
+        for m in range(2 * ns):
+            j, k = m % ns, m // ns
+            if L.plqflg[i][j] == 0 or i > p[j][2]:
+                continue
+            prev = self.plq[i + 1][m]
+            if k == 0:
+                if i == p[j][2]:
+                    b.add(("plq", m), "pair", x=self.opr[i + 1][p[j][3]], site1=L.sigma[0])
+                elif i == p[j][1]:
+                    b.add(("plq", m), "init", x=prev, site1=L.sigma[1])
+                elif i == p[j][0]:
+                    b.add(("plq", m), "pair", x=prev, site1=L.sigma[0], coef=-L.qdelta)
+                    b.add("hh", "pair", x=prev, site1=L.sigma[0], coef=-L.qdelta)
+                elif p[j][1] < i < p[j][2]:
+                    b.add(("plq", m), "overlap", x=prev)
+                elif p[j][0] < i < p[j][1]:
+                    b.add(("plq", m), "transform", x=prev)
+            else:
+                if i == p[j][2]:
+                    b.add(("plq", m), "perm", x=self.opr[i + 1][p[j][3]], site1=L.qterm[6], site2=L.qterm[7])
+                elif i == p[j][1]:
+                    b.add(("plq", m), "perm", x=prev, site1=L.qterm[4], site2=L.qterm[5])
+                elif i == p[j][0]:
+                    b.add(("plq", m), "pair", x=prev, site1=L.sigma[0], coef=-L.qdelta)
+                    b.add("hh", "pair", x=prev, site1=L.sigma[0], coef=-L.qdelta)
+                elif p[j][1] < i < p[j][2] or p[j][0] < i < p[j][1]:
+                    b.add(("plq", m), "transform", x=prev)
+        out = self._run(u, 1, b)
+        self.hh[i] = out.get("hh")
+        for name, t in out.items():
+            if isinstance(name, tuple) and name[0] == "opr":
+                self.opr[i][name[1]] = t
+            elif isinstance(name, tuple):
+                self.plq[i][name[1]] = t
+
+    # ------------------------------------------------------- two-site step
+    def heff_plan(self, il: int, ir: int, vs):
+        """The terms of hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664)."""
+        L, ns = self.lat, self.lat.ns
+        terms = []
+
+        def term(a, b, coef):
+            if a is not None and b is not None:
+                terms.append((a[0], a[1], b[0], b[1], coef))
+
+        if il < ns // 2:
+            for j in range(il + 1):
+                r = self._combine([(self.opr[ir][k], float(L.coup[L.hmap[j][k]])) for k in range(ir, ns)
+                                   if L.hmap[j][k] > 0])
+                if r is not None:
+                    self._keep.append(r)
+                    term(self.opr[il][j], r, 1.0)
+        else:
+            for k in range(ir, ns):
+                l = self._combine([(self.opr[il][j], float(L.coup[L.hmap[j][k]])) for j in range(il + 1)
+                                   if L.hmap[j][k] > 0])
+                if l is not None:
+                    self._keep.append(l)
+                    term(l, self.opr[ir][k], 1.0)
+        if il == ir - 1:
+            for m in range(2 * ns):
+                j = m % ns
+                if L.plqflg[il][j] != 1 or L.plqflg[ir][j] != 1:
+                    continue
+                q = L.plqpos[j]
+                if il >= q[0] and ir <= q[1]:
+                    term(self.opr[il][q[0]], self.plq[ir][m], -L.qdelta)
+                elif il >= q[1] and ir <= q[2]:
+                    term(self.plq[il][m], self.plq[ir][m], -L.qdelta)
+                elif il >= q[2] and ir <= q[3]:
+                    term(self.plq[il][m], self.opr[ir][q[3]], -L.qdelta)
+        hl = (self.hh[il][0], self.hh[il][1], 1.0) if self.hh[il] is not None else None
+        hr = (self.hh[ir][0], self.hh[ir][1], 1.0) if self.hh[ir] is not None else None
+        return S.HeffPlan(vs, terms, hl, hr, mode=self.mode)
+
+    def run(self):
+        """do_idmrg: returns the eigenvalue of the last two-site step."""
+        L, ns = self.lat, self.lat.ns
+        B = S.Su2Bond
+        self.uu[0] = S.fuse_tensor(B(1, [0], [1]), B(1, [L.physpn], [1]))
+        self.uu[ns - 1] = S.fuse_tensor(B(1, [L.physpn], [1]), B(1, [L.totspin], [1]))
+        phys = B(1, [L.physpn], [1])
+        for i in range(ns // 2 - 1):
+            self.site_left(i, self.uu[i])
+            self.site_right(ns - 1 - i, self.uu[ns - 1 - i])
+            bl = self.uu[i][0].bonds[2].inverted()
+            br = self.uu[ns - 1 - i][0].bonds[2].inverted()
+            self.uu[i + 1] = S.fuse_tensor(bl, phys)
+            self.uu[ns - 2 - i] = S.fuse_tensor(phys, br)
+            if (i + 2) * 2 * L.physpn >= L.totspin and i >= 1 or i == ns // 2 - 2:
+                il, ir = i + 1, ns - 2 - i
+                ul, ur = self.uu[il], self.uu[ir]
+                vs, vx = S.initial_vector(ul[0], ul[1], ur[0], ur[1])
+                vx = vx[: vs.size()]
+                self.site_left(il, S.fuse_tensor(*self._legs01(ul)))
+                self.site_right(ir, S.fuse_tensor(*self._legs01(ur)))
+                plan = self.heff_plan(il, ir, vs)
+                n = vs.size()
+                e, _ = plan.lanczos(vx, mlanc=self.mlanc if self.mlanc <= n else n + 1)
+                plan.close()
+                self._keep.clear()
+                self.energies.append((il, ir, e))
+                p1, p2 = (1.0, 0.0) if i == ns // 2 - 2 else (0.0, 0.0)
+                tu, xu, tv, xv, w = S.svd(vs, vx, ul[0], p1, ur[0], p2, L.max_dcut)
+                self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
+                self.ww = w
+        return self.energies[-1][2] if self.energies else None

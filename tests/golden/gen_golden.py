@@ -24,6 +24,7 @@ from __future__ import annotations
 import ctypes
 import json
 import os
+import subprocess
 import sys
 import tempfile
 
@@ -601,8 +602,69 @@ def mea_cases(L):
     return cases
 
 
+def warmup_cases(L):
+    """do_idmrg alone on small lattices: the engine's lattice tables and
+    one-site operators (inputs of the device warm-up), the eigenvalue of every
+    two-site step and the singular values of the last truncation.  The J1 4x2
+    warm-up runs as the engine has it (five Lanczos vectors per step); the
+    J1-J2 6x2 and J-Q 4x4 warm-ups with mlanc Lanczos vectors (the
+    su2ref_idmrg_mlanc hook of patch_ref.py): with five, their steps stop
+    near an invariant subspace of the uniform start vector and the result
+    follows rounding noise (the FP64 and split device engines already differ
+    there at the second step)."""
+    cases = []
+    L.ref_engine_tables.restype = ctypes.c_int
+    for ci, (lx, ly, d, jc, qc, mlanc) in enumerate([(4, 2, 16, 1.0, 0.0, 5), (6, 2, 24, 0.5, 0.0, 40),
+                                                      (4, 4, 24, 1.0, 1.0, 40)]):
+        ints = np.zeros(1 << 16, np.int32)
+        dbls = np.zeros(4096)
+        n = L.ref_engine_tables(lx, ly, 0, d, ctypes.c_double(jc), ctypes.c_double(qc), 2, p(ints), len(ints), p(dbls),
+                                len(dbls))
+        assert n > 0
+        ns = int(ints[0])
+        case = dict(name=f"warmup_{ci}", lx=np.int32(lx), ly=np.int32(ly), d=np.int32(d), jcoup=np.float64(jc),
+                    qcoup=np.float64(qc), mlanc=np.int32(mlanc), tables=ints[:n].copy(), coup=dbls[:ns].copy())
+        for i in range(10):  # sigma[0], sigma[1], qterm[0..8)
+            L.ref_idmrg_select(i)
+            dd = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(dd))
+            flag, x1, _ = read_result(L)
+            case.update({f"site{i}_desc": dd[:nd].copy(), f"site{i}_flag": flag, f"site{i}_x": x1})
+        # the warm-up in a child process: its per-step energies are only printed
+        # ("lanczos <il> gs_enr[0]=<eigenvalue - 1000>", dmrg_su2.cpp:539; ref_warmup
+        # prints them with 17 digits)
+        code = (f"import ctypes, numpy as np; L = ctypes.CDLL({REFLIB!r}); L.ref_setup(1, 25); "
+                f"L.su2ref_set_sign_convention(1); L.su2ref_set_idmrg_mlanc({mlanc}); "
+                f"e = ctypes.c_double(); ww = np.zeros(4096); "
+                f"L.ref_warmup({lx}, {ly}, 0, {d}, ctypes.c_double({jc}), ctypes.c_double({qc}), 2, 1, "
+                f"ctypes.byref(e), ww.ctypes.data_as(ctypes.c_void_p), 4096); "
+                f"print('RESULT', repr(float(e.value)), ' '.join(repr(float(v)) for v in ww[:{d}]))")
+        out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, check=True).stdout
+        steps = [float(ln.split("=")[-1]) + 1000.0 for ln in out.splitlines() if ln.startswith("lanczos")]
+        res = [ln for ln in out.splitlines() if ln.startswith("RESULT")][0].split()[1:]
+        case.update(energy=np.float64(float(res[0])), ww=np.array([float(v) for v in res[1:]]),
+                    step_energies=np.array(steps))
+        cases.append(case)
+    fuse = []
+    for bonds in ([(-1, [0, 2, 4], [3, 2, 1]), (-1, [1], [1])], [(1, [1], [1]), (1, [0, 1, 2, 3], [2, 4, 1, 3])]):
+        bd = desc_of(bonds)
+        L.ref_fuse_tensor(p(bd))
+        dd = np.zeros(1024, np.int32)
+        nd = L.ref_result_desc(p(dd))
+        flag, x1, _ = read_result(L)
+        fuse.append(dict(bonds=bd, desc=dd[:nd].copy(), flag=flag, x=x1))
+    cases.append(dict(name="fuse_tensor", **{f"{k}{i}": v for i, c in enumerate(fuse) for k, v in c.items()}))
+    return cases
+
+
 def main():
     L = ctypes.CDLL(REFLIB)
+    if "--only-warmup" in sys.argv:
+        L.ref_setup(1, 25)
+        for c in warmup_cases(L):
+            name = c.pop("name")
+            np.savez(os.path.join(HERE, name + ".npz"), **c)
+        return
     if "--only-mea" in sys.argv:
         L.ref_setup(1, 25)
         rng = np.random.Generator(np.random.PCG64(777))
@@ -640,7 +702,7 @@ def main():
             name = c.pop("name")
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **c)
     np.savez(os.path.join(HERE, "ckpt_engine.npz"), **checkpoint_cases(L))
-    for c in measure_op_cases(L, np.random.Generator(np.random.PCG64(777))) + mea_cases(L):
+    for c in measure_op_cases(L, np.random.Generator(np.random.PCG64(777))) + mea_cases(L) + warmup_cases(L):
         name = c.pop("name")
         np.savez(os.path.join(HERE, name + ".npz"), **c)
     if "--no-dmrg" not in sys.argv:

@@ -316,3 +316,16 @@ def test_wavefunc_argument_checks_without_gpu(su2lib):
     with pytest.raises(CheckError, match="flag"):
         vectran_layout(ul, 2)
     assert capi.SU2G_EINVAL == 1
+
+
+def test_fuse_tensor_layout_matches_reference(su2lib):
+    """tensor_su2::fuse(b1, b2): legs, every legal block present."""
+    from su2dmrg_gb300 import su2 as S
+
+    g = np.load(os.path.join(GOLDEN, "fuse_tensor.npz"))
+    for i in range(2):
+        b = S._parse_desc(g[f"bonds{i}"]).bonds
+        s = S.fuse_tensor_layout(b[0], b[1])
+        assert s.desc().tolist() == g[f"desc{i}"].tolist()
+        assert s.flag.tolist() == g[f"flag{i}"].tolist()
+        assert s.size() == len(g[f"x{i}"])
