@@ -13,7 +13,14 @@ Printed JSON (rank 0, one line):
          flush is needed between iterations);
   e2e    the same metric through the C ABI with host buffers: pinned-host psi
          copied in, applied, y copied back, every step;
-  roofline, cpu_baseline, clocks, gpu_launches as documented in DESIGN.md.
+  roofline  the two split GEMM launches against the measured BF16 burst peak
+         of MEASURED_PEAKS.json (28 BF16 products per FP64 product), with
+         their DRAM traffic per launch;
+  cpu_baseline  the oracle port on the host cores (a bounded sample);
+  clocks  nvidia-smi SM clocks and throttle reasons during the timed region;
+  gpu_launches  the library's kernel launches in the timed region.
+Default steps: 250 applications (about 1 s, so that the clock record holds
+several samples under load); 10 calls for the other rows.
 --impl reference times the CPU restatement of the reference's hot path (the
 reference itself is not built on the GPU host) on all host cores.
 
@@ -46,7 +53,7 @@ UNIT = "TFLOP/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="su2g", choices=["su2g", "reference"])
     ap.add_argument("--mode", default="split", choices=["f64", "split", "split-fast"])
@@ -56,7 +63,10 @@ def parse():
     ap.add_argument("--row", default="heff", choices=["heff", "input_vector", "vectran", "env", "svd"],
                     help="heff (the headline) or another operation of the site step, timed on the "
                          "D-multiplet site-step workload (workloads.synthetic_site_step)")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.steps is None:
+        a.steps = 250 if a.row == "heff" else 10
+    return a
 
 
 def dist_setup(args):
@@ -103,6 +113,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.mark = 0
 
     def __enter__(self):
         try:
@@ -111,6 +122,12 @@ class ClockSampler:
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes a moment to start: wait (at most 3 s) for its
+            # first line, and count only the samples taken after it
+            t_end = time.time() + 3.0
+            while not self.lines and time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.mark = len(self.lines)
         except OSError:
             self.proc = None
         return self
@@ -130,7 +147,8 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines[self.mark:] or self.lines[-1:]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 7:
                 continue
