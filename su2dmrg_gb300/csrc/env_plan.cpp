@@ -113,6 +113,38 @@ int64_t block_size(const Struct& s, int b) {
   return n;
 }
 
+// The stored blocks of a tensor grouped by the 2j of one leg (or of two legs),
+// each group in ascending block order: the contribution loops visit exactly
+// the blocks a full scan with the same tests would, in the same order,
+// without scanning every block of uu and vv for every operator block.
+struct Buckets {
+  int w2 = 1;
+  std::vector<std::vector<int>> b;
+  const std::vector<int>& at(int a1, int a2 = 0) const {
+    static const std::vector<int> none;
+    if (a1 < 0 || a2 < 0 || a2 >= w2) return none;
+    const size_t key = (size_t)a1 * w2 + a2;
+    return key < b.size() ? b[key] : none;
+  }
+};
+
+Buckets bucket(const Struct& s, int l1, int l2 = -1) {
+  auto width = [&](int l) {
+    int m = 0;
+    for (int a : s.legs[l].angm) m = std::max(m, a);
+    return m + 1;
+  };
+  Buckets r;
+  r.w2 = l2 >= 0 ? width(l2) : 1;
+  r.b.resize((size_t)width(l1) * r.w2);
+  for (int k = 0; k < s.nten; ++k) {
+    if (!s.flag[k]) continue;
+    const int a1 = s.block_angm(k, l1), a2 = l2 >= 0 ? s.block_angm(k, l2) : 0;
+    if (a1 >= 0 && a2 >= 0) r.b[(size_t)a1 * r.w2 + a2].push_back(k);
+  }
+  return r;
+}
+
 }  // namespace
 
 int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int njobs, const su2g_env_job* jobs,
@@ -145,6 +177,11 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
     *err = "job " + std::to_string(t) + ": " + m;
     return code;
   };
+  const Buckets u_bond = bucket(U, flag), u_phys = bucket(U, pl);
+  const Buckets v_bond = bucket(V, flag), v_bond_phys = bucket(V, flag, pl);
+  std::vector<int> u_all;
+  for (int k = 0; k < U.nten; ++k)
+    if (U.flag[k]) u_all.push_back(k);
 
   std::vector<Job> J(njobs);
   std::vector<Contrib> cs;
@@ -241,11 +278,9 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
         const int a = jb.X.block_angm(j, 0), ap = jb.X.block_angm(j, xr);
         const int s = kind == SU2G_ENV_TRANSFORM ? jb.X.block_angm(j, 1) : 0;
         const int ms = kind == SU2G_ENV_TRANSFORM ? jb.X.block_dim(j, 1) : 1;
-        for (int k = 0; k < U.nten; ++k) {
-          if (!U.flag[k] || U.block_angm(k, flag) != a) continue;
+        for (int k : u_bond.at(a)) {
           const int sig = U.block_angm(k, pl), c = U.block_angm(k, 2);
-          for (int l = 0; l < V.nten; ++l) {
-            if (!V.flag[l] || V.block_angm(l, flag) != ap || V.block_angm(l, pl) != sig) continue;
+          for (int l : v_bond_phys.at(ap, sig)) {
             const int cp = V.block_angm(l, 2);
             int m;
             if (!out_block(c, s, cp, &m)) continue;
@@ -267,22 +302,21 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
       if (!same_sectors(U.legs[pl], S.legs[0]) || U.legs[pl].dir != -S.legs[0].dir ||
           !same_sectors(V.legs[pl], S.legs[2]) || V.legs[pl].dir != S.legs[2].dir)
         return fail(SU2G_EINVAL, t, "site operator bonds do not match uu/vv");
+      const Buckets x_leg0 = jb.has_x ? bucket(jb.X, 0) : Buckets();
+      const std::vector<int> no_endt{-1};
       for (int j = 0; j < S.nten; ++j) {
         if (!S.flag[j]) continue;
         if (block_size(S, j) != 1)
           return fail(SU2G_EUNSUPPORTED, t, "operator_initial needs single-element site operator blocks");
         const int sig = S.block_angm(j, 0), s = S.block_angm(j, 1), sigp = S.block_angm(j, 2);
         const double op = jb.s1[S.offset[j]];
-        for (int k = 0; k < U.nten; ++k) {
-          if (!U.flag[k] || U.block_angm(k, pl) != sig) continue;
+        for (int k : u_phys.at(sig)) {
           const int a = U.block_angm(k, flag), c = U.block_angm(k, 2);
           // with endt, each U block meets the endt blocks (a, a'); a' is the
           // bond that meets vv (spin-0 endt: a' = a in 2j)
-          for (int e = 0; e < (jb.has_x ? jb.X.nten : 1); ++e) {
-            if (jb.has_x && (!jb.X.flag[e] || jb.X.block_angm(e, 0) != a)) continue;
+          for (int e : jb.has_x ? x_leg0.at(a) : no_endt) {
             const int ap = jb.has_x ? jb.X.block_angm(e, 1) : a;
-            for (int l = 0; l < V.nten; ++l) {
-              if (!V.flag[l] || V.block_angm(l, pl) != sigp || V.block_angm(l, flag) != ap) continue;
+            for (int l : v_bond_phys.at(ap, sigp)) {
               const int cp = V.block_angm(l, 2);
               int m;
               if (!out_block(c, s, cp, &m)) continue;
@@ -305,11 +339,9 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
         if (!jb.X.flag[j]) continue;
         const int a = jb.X.block_angm(j, 0), s = jb.X.block_angm(j, 1), ap = jb.X.block_angm(j, 2);
         const int ms = jb.X.block_dim(j, 1);
-        for (int k = 0; k < U.nten; ++k) {
-          if (!U.flag[k] || U.block_angm(k, flag) != a) continue;
+        for (int k : u_bond.at(a)) {
           const int sig = U.block_angm(k, pl), c = U.block_angm(k, 2);
-          for (int l = 0; l < V.nten; ++l) {
-            if (!V.flag[l] || V.block_angm(l, flag) != ap) continue;
+          for (int l : v_bond.at(ap)) {
             const int sigp = V.block_angm(l, pl), cp = V.block_angm(l, 2);
             for (int n = 0; n < S.nten; ++n) {
               if (!S.flag[n] || S.block_angm(n, 0) != sig || S.block_angm(n, 2) != sigp || S.block_angm(n, 1) != s)
@@ -336,16 +368,14 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
       if (!same_sectors(b1, b2) || b1.dir != -b2.dir)
         return fail(SU2G_EINVAL, t, "site operators do not share a bond");
       // reference loop order: U block, vec block, V block, op1 block, op2 block
-      for (int j = 0; j < U.nten; ++j) {
-        if (!U.flag[j]) continue;
+      const Buckets x_leg0 = bucket(jb.X, 0);
+      for (int j : u_all) {
         const int a = U.block_angm(j, flag), sig = U.block_angm(j, pl), c = U.block_angm(j, 2);
-        for (int k = 0; k < jb.X.nten; ++k) {
-          if (!jb.X.flag[k] || jb.X.block_angm(k, 0) != a) continue;
+        for (int k : x_leg0.at(a)) {
           const int s = jb.X.block_angm(k, 1), ap = jb.X.block_angm(k, 2);
           if (jb.X.block_dim(k, 1) != 1)
             return fail(SU2G_EUNSUPPORTED, t, "permutation needs an operator spin of multiplicity 1");
-          for (int l = 0; l < V.nten; ++l) {
-            if (!V.flag[l] || V.block_angm(l, flag) != ap) continue;
+          for (int l : v_bond.at(ap)) {
             const int sigp = V.block_angm(l, pl), cp = V.block_angm(l, 2);
             for (int mm = 0; mm < O1.nten; ++mm) {
               if (!O1.flag[mm]) continue;
