@@ -765,6 +765,13 @@ int ref_warmup(int lx, int ly, int sec, int d, double jcoup, double qcoup, int b
   return c->ns;
 }
 
+// after ref_run_dmrg: select the engine's MPS tensor uu[i] for ref_result_desc
+int ref_select_mps(int i) {
+  if (!chain_ptr || i < 0 || i >= chain_ptr->ns) return -1;
+  g_sel = &chain_ptr->uu[i];
+  return 0;
+}
+
 int ref_run_dmrg(int lx, int ly, int sec, int d, int niter, double jcoup, double qcoup, int boundary,
                  int nthreads, double* energies) {
   max_dcut = d;

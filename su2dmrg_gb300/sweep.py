@@ -1,0 +1,88 @@
+"""DMRG sweeps with every tensor on the device.
+
+dmrg_su2::sweep (dmrg_su2_omp.cpp:97-145) moves the two-site centre from the
+middle to the left end, across to the right end and back to the middle.  At
+each step the centre tensor is rotated to the side it moves to
+(wavefunc_transformation, :1864-1877), the site just left behind is
+updated (the two-argument prepare_site_operator_from_left / _right), the
+two-site vector is predicted from the MPS pair (prepare_input_vector,
+:229-254), the new centre's operators are built (the one-argument forms),
+the Lanczos ground state is found (lanczos_solve_eigenvector_idmrg,
+dmrg_su2.cpp:527-540, five vectors from the predicted state) and truncated
+(tensor_su2::svd, with the singular values on the side the centre moves to).
+main_omp.cpp:183-201 repeats sweeps after the warm-up until the energy
+changes by less than 1e-6.  This module drives that sequence over the C ABI
+of libsu2g, continuing from the device state the warm-up leaves
+(su2dmrg_gb300.warmup); nothing but structures and the engine's tables lives
+on the host.  Ground state only (exci = 0).
+"""
+from __future__ import annotations
+
+import time
+
+from . import su2 as S
+from .warmup import Warmup
+
+
+class Dmrg(Warmup):
+    """do_idmrg followed by sweeps.  nfree: the sites at each end the sweep
+    does not reach (dmrg_su2.cpp:54 sets 2)."""
+
+    nfree = 2
+
+    def _vectran(self, i: int, flag: int) -> None:
+        """wavefunc_transformation(i, flag): right2left_vectran (0) or
+        left2right_vectran (1) of uu[i]."""
+        s, y = S.vectran(*self.uu[i], flag)
+        self.uu[i] = (s, y[: s.size()])
+
+    def _step(self, il: int, ir: int, p1: float, p2: float) -> float:
+        L = self.lat
+        vs, vx = S.prepare_input_vector(*self.uu[il], *self.uu[ir], mode=self.mode)
+        vx = vx[: vs.size()]
+        self.site_left(il, S.fuse_tensor(*self._legs01(self.uu[il])))
+        self.site_right(ir, S.fuse_tensor(*self._legs01(self.uu[ir])))
+        plan = self.heff_plan(il, ir, vs)
+        n = vs.size()
+        e, _ = plan.lanczos(vx, mlanc=self.mlanc if self.mlanc <= n else n + 1)
+        plan.close()
+        self._keep.clear()
+        self.energies.append((il, ir, e))
+        tu, xu, tv, xv, w = S.svd(vs, vx, self.uu[il][0], p1, self.uu[ir][0], p2, L.max_dcut)
+        self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
+        self.ww = w
+        return e
+
+    def sweep(self) -> float:
+        """One sweep; returns the eigenvalue of its last step (the centre)."""
+        ns, nf = self.lat.ns, self.nfree
+        for i in range(ns // 2, nf + 1, -1):        # centre -> left end
+            self._vectran(i - 1, 1)
+            self.site_right(i, self.uu[i], release=True)
+            self._step(i - 2, i - 1, *((1.0, 0.0) if i > nf + 2 else (0.0, 1.0)))
+        for i in range(nf, ns - nf - 2):             # left end -> right end
+            self._vectran(i + 1, 0)
+            self.site_left(i, self.uu[i], release=True)
+            self._step(i + 1, i + 2, *((0.0, 1.0) if i < ns - nf - 3 else (1.0, 0.0)))
+        for i in range(ns - nf - 1, ns // 2, -1):   # right end -> centre
+            self._vectran(i - 1, 1)
+            self.site_right(i, self.uu[i], release=True)
+            self._step(i - 2, i - 1, 1.0, 0.0)
+        return self.energies[-1][2]
+
+    def run_dmrg(self, niter: int, tol: float = 1e-6):
+        """main_omp's loop: the warm-up, then up to niter sweeps, stopping when
+        a sweep changes the energy by less than tol.  Returns the energies
+        (eigenvalues) after the warm-up and after each sweep, and the seconds
+        each sweep took (device work included: every call blocks)."""
+        e1 = self.run()
+        energies, seconds = [e1], []
+        for _ in range(niter):
+            t0 = time.perf_counter()
+            e2 = self.sweep()
+            seconds.append(time.perf_counter() - t0)
+            energies.append(e2)
+            if abs(e1 - e2) < tol:
+                break
+            e1 = e2
+        return energies, seconds

@@ -122,9 +122,28 @@ class Warmup:
     def _legs01(u):
         return u[0].bonds[0], u[0].bonds[1]
 
+    def _release(self, p: int, lr: int) -> None:
+        """release_memory2(p, lr) (dmrg_su2_omp.cpp:1804-1824), which the
+        two-argument site updates call even without disk swap: the operators
+        carried at site p towards the left (lr 0) or right (lr 1) end, its block
+        Hamiltonian and its plaquette operators are emptied."""
+        L = self.lat
+        if p < 0 or p >= L.ns:
+            return
+        carry = L.fll if lr == 0 else L.frr
+        for k in range(L.ns):
+            if carry[p][k] == 1:
+                self.opr[p][k] = None
+        self.hh[p] = None
+        for j in range(L.ns):
+            if L.plqflg[p][j]:
+                self.plq[p][j] = self.plq[p][j + L.ns] = None
+
     # ---------------------------------------------------- site updates
-    def site_left(self, i: int, u):
-        """prepare_site_operator_from_left(i[, flag]) with MPS tensor u at site i."""
+    def site_left(self, i: int, u, release: bool = False):
+        """prepare_site_operator_from_left(i[, flag]) with MPS tensor u at site
+        i; release: the two-argument form, which first empties sites i+1 and
+        i+2 (dmrg_su2_omp.cpp:338-339)."""
         L, p = self.lat, self.lat.plqpos
         if i == 0:
             b = _Jobs()
@@ -132,6 +151,9 @@ class Warmup:
             self.opr[0][0] = self._run(u, 0, b)[("opr", 0)]
             self.hh[0] = None
             return
+        if release:
+            self._release(i + 1, 1)
+            self._release(i + 2, 1)
         b = _Jobs()
         if self.hh[i - 1] is not None:
             b.add("hh", "overlap", x=self.hh[i - 1])
@@ -177,8 +199,10 @@ class Warmup:
             elif isinstance(name, tuple):
                 self.plq[i][name[1]] = t
 
-    def site_right(self, i: int, u):
-        """prepare_site_operator_from_right(i[, flag]) with MPS tensor u at site i."""
+    def site_right(self, i: int, u, release: bool = False):
+        """prepare_site_operator_from_right(i[, flag]) with MPS tensor u at site
+        i; release: the two-argument form, which first empties sites i-1 and
+        i-2 (dmrg_su2_omp.cpp:480-481)."""
         L, p, ns = self.lat, self.lat.plqpos, self.lat.ns
         if i == ns - 1:
             b = _Jobs()
@@ -186,6 +210,9 @@ class Warmup:
             self.opr[i][i] = self._run(u, 1, b)[("opr", i)]
             self.hh[i] = None
             return
+        if release:
+            self._release(i - 1, 0)
+            self._release(i - 2, 0)
         b = _Jobs()
         if self.hh[i + 1] is not None:
             b.add("hh", "overlap", x=self.hh[i + 1])
@@ -280,8 +307,8 @@ class Warmup:
         self.uu[ns - 1] = S.fuse_tensor(B(1, [L.physpn], [1]), B(1, [L.totspin], [1]))
         phys = B(1, [L.physpn], [1])
         for i in range(ns // 2 - 1):
-            self.site_left(i, self.uu[i])
-            self.site_right(ns - 1 - i, self.uu[ns - 1 - i])
+            self.site_left(i, self.uu[i], release=True)
+            self.site_right(ns - 1 - i, self.uu[ns - 1 - i], release=True)
             bl = self.uu[i][0].bonds[2].inverted()
             br = self.uu[ns - 1 - i][0].bonds[2].inverted()
             self.uu[i + 1] = S.fuse_tensor(bl, phys)

@@ -409,8 +409,15 @@ def dmrg_runs(L):
             e = np.zeros(64)
             n = L.ref_run_dmrg(lx, ly, sec, d, niter, ctypes.c_double(jc), ctypes.c_double(qc), bd, 1, p(e))
             os.chdir(cwd)
+        # the structure of every MPS tensor at the end (kept multiplets per sector)
+        descs = []
+        for i in range(lx * ly):
+            assert L.ref_select_mps(i) == 0
+            dd = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(dd))
+            descs.append([int(v) for v in dd[:nd]])
         out.append(dict(lx=lx, ly=ly, sec=sec, d=d, niter=niter, jcoup=jc, qcoup=qc, boundary=bd,
-                        energies_minus_1000=[float(v) for v in e[:n]]))
+                        energies_minus_1000=[float(v) for v in e[:n]], mps_desc=descs))
         print("dmrg", lx, ly, d, jc, qc, out[-1]["energies_minus_1000"], file=sys.stderr)
     return out
 
@@ -602,6 +609,39 @@ def mea_cases(L):
     return cases
 
 
+def engine_tables(L, lx, ly, d, jc, qc, bd=2):
+    """The engine's lattice tables and one-site operators (sigma[0], sigma[1],
+    qterm[0..8)) for one lattice, as the device warm-up and sweep take them."""
+    L.ref_engine_tables.restype = ctypes.c_int
+    ints = np.zeros(1 << 16, np.int32)
+    dbls = np.zeros(4096)
+    n = L.ref_engine_tables(lx, ly, 0, d, ctypes.c_double(jc), ctypes.c_double(qc), bd, p(ints), len(ints), p(dbls),
+                            len(dbls))
+    assert n > 0
+    ns = int(ints[0])
+    case = dict(lx=np.int32(lx), ly=np.int32(ly), d=np.int32(d), jcoup=np.float64(jc), qcoup=np.float64(qc),
+                tables=ints[:n].copy(), coup=dbls[:ns].copy())
+    for i in range(10):
+        L.ref_idmrg_select(i)
+        dd = np.zeros(1024, np.int32)
+        nd = L.ref_result_desc(p(dd))
+        flag, x1, _ = read_result(L)
+        case.update({f"site{i}_desc": dd[:nd].copy(), f"site{i}_flag": flag, f"site{i}_x": x1})
+    return case
+
+
+def sweep_cases(L):
+    """Lattice tables of the whole runs in dmrg_energies.json (their energies
+    after the warm-up and after each sweep are the reference's, in that file)."""
+    cases = []
+    for ci, r in enumerate(json.load(open(os.path.join(HERE, "dmrg_energies.json")))):
+        assert r["boundary"] == 2 and r["sec"] == 0
+        case = engine_tables(L, r["lx"], r["ly"], r["d"], r["jcoup"], r["qcoup"])
+        case["name"] = f"sweep_{ci}"
+        cases.append(case)
+    return cases
+
+
 def warmup_cases(L):
     """do_idmrg alone on small lattices: the engine's lattice tables and
     one-site operators (inputs of the device warm-up), the eigenvalue of every
@@ -659,6 +699,17 @@ def warmup_cases(L):
 
 def main():
     L = ctypes.CDLL(REFLIB)
+    if "--only-dmrg" in sys.argv:
+        L.ref_setup(1, 25)
+        with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
+            json.dump(dmrg_runs(L), f, indent=1)
+        return
+    if "--only-sweep" in sys.argv:
+        L.ref_setup(1, 25)
+        for c in sweep_cases(L):
+            name = c.pop("name")
+            np.savez(os.path.join(HERE, name + ".npz"), **c)
+        return
     if "--only-warmup" in sys.argv:
         L.ref_setup(1, 25)
         for c in warmup_cases(L):
