@@ -60,9 +60,18 @@ def parse():
     ap.add_argument("--D", type=int, default=2000)
     ap.add_argument("--nspin1", type=int, default=18)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--row", default="heff", choices=["heff", "input_vector", "vectran", "env", "svd"],
+    ap.add_argument("--row", default="heff", choices=["heff", "input_vector", "vectran", "env", "svd", "sweep"],
                     help="heff (the headline) or another operation of the site step, timed on the "
-                         "D-multiplet site-step workload (workloads.synthetic_site_step)")
+                         "D-multiplet site-step workload (workloads.synthetic_site_step); sweep: one whole "
+                         "DMRG sweep of a J1-J2 cylinder after the device warm-up, split and FP64 contractions "
+                         "from the same state")
+    ap.add_argument("--lattice", default="16x8", help="sweep row: LXxLY cylinder")
+    ap.add_argument("--delta", type=float, default=2.0,
+                    help="sweep row: nearest-neighbour coupling (diagonal 1 - |qdelta|; 2.0 = J2/J1 0.5)")
+    ap.add_argument("--qdelta", type=float, default=0.0, help="sweep row: plaquette coupling Q")
+    ap.add_argument("--skip-fp64", action="store_true", help="sweep row: time the split sweep only")
+    ap.add_argument("--sweeps-before", type=int, default=1,
+                    help="sweep row: untimed split sweeps between the warm-up and the timed sweep")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = 250 if a.row == "heff" else 10
@@ -607,10 +616,85 @@ def run_row(args):
     return 0
 
 
+def run_sweep(args):
+    """One DMRG sweep (dmrg_su2::sweep) of an lx x ly J1-J2 cylinder at D
+    multiplets, every tensor on the device: the warm-up (do_idmrg) and
+    --sweeps-before sweeps in split mode, then the next sweep from that state
+    twice, with split-precision and with FP64 contractions (truncation,
+    Lanczos scalars and the tridiagonal problem are FP64 in both).  The first
+    sweep after the warm-up is not a comparison point: the warm-up's basis
+    holds rounding-noise Schmidt directions (every value above 1e-100 of the
+    largest is kept), the engine's own first sweep passes through energies far
+    below the ground state before it recovers, and two runs differing by
+    rounding follow different paths there.  Wall-clock seconds with the
+    device synchronised on both sides (every library call blocks)."""
+    import torch
+
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300.sweep import Dmrg
+    from su2dmrg_gb300.warmup import Lattice
+
+    capi.lib()
+    torch.cuda.set_device(0)
+    lx, ly = (int(v) for v in args.lattice.lower().split("x"))
+    lat = Lattice.cylinder(lx, ly, args.delta, args.qdelta, args.D)
+    split = MODES["split"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d = Dmrg(lat, mode=split)
+    e_warm = d.run()
+    torch.cuda.synchronize()
+    warm_s = time.perf_counter() - t0
+    before_s = []
+    for _ in range(args.sweeps_before):
+        t0 = time.perf_counter()
+        d.sweep()
+        torch.cuda.synchronize()
+        before_s.append(time.perf_counter() - t0)
+    nwarm = len(d.energies)
+    ref_state = None if args.skip_fp64 else d.clone(MODES["f64"])
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t0 = time.perf_counter()
+        e_split = d.sweep()
+        torch.cuda.synchronize()
+        split_s = time.perf_counter() - t0
+    steps_split = np.array([e for _, _, e in d.energies[nwarm:]])
+    line = {"metric": f"DMRG sweep seconds, {lx}x{ly} J1-J2 cylinder (delta {args.delta}, Q {args.qdelta}), "
+                      f"D={args.D}, split-precision contractions",
+            "value": split_s, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": split_s * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 emulated by bf16 x7 (fp32 accumulate); FP64 truncation and Lanczos scalars",
+            "data": "synthetic (lattice tables built here; the uniform warm-up start, as the engine)",
+            "config": {"workload": f"{lx}x{ly} cylinder, boundary 2, D={args.D}, sweep {args.sweeps_before + 1} "
+                                   f"after the warm-up",
+                       "row": "sweep", "two_site_steps": len(steps_split), "warmup_seconds": warm_s,
+                       "earlier_sweep_seconds": before_s,
+                       "warmup_energy_per_site": e_warm / lat.ns, "sweep_energy_per_site_split": e_split / lat.ns},
+            "clocks": clk.summary(), "cpu_baseline": None,
+            "cpu_baseline_note": "the reference main_omp is not built on the GPU host (x86 build, sources absent)"}
+    if ref_state is not None:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_f64 = ref_state.sweep()
+        torch.cuda.synchronize()
+        f64_s = time.perf_counter() - t0
+        steps_f64 = np.array([e for _, _, e in ref_state.energies[nwarm:]])
+        rel = np.abs(steps_split - steps_f64) / np.abs(steps_f64)
+        line["config"].update({"fp64_sweep_seconds": f64_s, "split_speedup_vs_fp64": f64_s / split_s,
+                               "sweep_energy_per_site_fp64": e_f64 / lat.ns,
+                               "max_rel_step_energy_diff_split_vs_fp64": float(rel.max()),
+                               "final_rel_energy_diff_split_vs_fp64": float(abs(e_split - e_f64) / abs(e_f64))})
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.row == "sweep":
+        return run_sweep(args)
     if args.row != "heff":
         return run_row(args)
     return run_su2g(args)

@@ -859,7 +859,11 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
     *energy = eig[0];
     if (nmatvec) *nmatvec = L.nmatvec;
     cudaError_t e = cudaStreamSynchronize(L.st);
-    return e == cudaSuccess ? SU2G_OK : cuda_fail(e, "lanczos");
+    if (e != cudaSuccess) return cuda_fail(e, "lanczos");
+    // a bounded wait of the split GEMM that gave up leaves partial products:
+    // the result is refused, not returned
+    int code = 0;
+    return su2g_heff_plan_status(p, &code);
   };
 
   // ff[0] = normalised start vector (lanczos_su2.cpp:45-46)

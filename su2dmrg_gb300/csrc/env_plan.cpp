@@ -287,7 +287,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
             double fac = 1.0;
             if (kind == SU2G_ENV_TRANSFORM) {
               if (!angm_ok(c) || !angm_ok(s) || !angm_ok(cp) || !angm_ok(a) || !angm_ok(ap))
-                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j >= 25)");
+                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j > 38)");
               fac = fac_operator_transformation(flag, c, s, cp, a, ap, sig);
               if (std::fabs(fac) < 1.e-8) continue;
             }
@@ -321,7 +321,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
               int m;
               if (!out_block(c, s, cp, &m)) continue;
               if (!angm_ok(c) || !angm_ok(s) || !angm_ok(cp) || !angm_ok(ap))
-                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j >= 25)");
+                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j > 38)");
               const double fac = fac_operator_onsite(flag, c, s, cp, ap, sig + sigp * 3);
               if (std::fabs(fac) < 1.e-8) continue;
               pres[m] = 1;
@@ -349,7 +349,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
               int m;
               if (!out_block(c, 0, cp, &m)) continue;
               if (!angm_ok(c) || !angm_ok(a) || !angm_ok(ap))
-                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j >= 25)");
+                return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j > 38)");
               const double fac = fac_operator_pairup(flag, c, a, ap, s, sig + sigp * 3);
               if (std::fabs(fac) < 1.e-8) continue;
               if (block_size(S, n) != ms)
@@ -396,7 +396,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
                 if (tix < 0 || tix >= 18)
                   return fail(SU2G_EUNSUPPORTED, t, "site operator spins outside the permutation table");
                 if (!angm_ok(a) || !angm_ok(c) || !angm_ok(ap) || !angm_ok(cp))
-                  return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j >= 25)");
+                  return fail(SU2G_EINVAL, t, "angular momentum beyond the recoupling table (2j > 38)");
                 const double fac = fac_permutation(flag, a, c, ap, cp, tix);
                 if (std::fabs(fac) < 1.e-8) continue;
                 // fac1 = op1 block . op2 block (tensor::inner_prod)

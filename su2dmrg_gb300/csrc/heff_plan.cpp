@@ -143,10 +143,9 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
     }
   }
 
-  const std::vector<double>& fac = fac_hamilt_vec_table();
   auto fac_of = [&](int ja, int s, int jc, double* f) -> bool {
     if (ja >= kMaxAngm || s >= kMaxAngm || jc >= kMaxAngm) return false;
-    *f = fac[(ja * kMaxAngm + s) * kMaxAngm + jc];
+    *f = fac_hamilt_vec_at(ja, s, jc);
     return true;
   };
 
@@ -179,7 +178,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
           if (scalar_pair[t]) {
             f = 1.0;
           } else if (!fac_of(ja, s, jc, &f)) {
-            *err = "angular momentum beyond the recoupling table (2j >= 25)";
+            *err = "angular momentum beyond the recoupling table (2j > 38)";
             return SU2G_EINVAL;
           }
           if (std::fabs(f) < 1.e-12) continue;

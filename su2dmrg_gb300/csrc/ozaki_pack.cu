@@ -16,9 +16,9 @@ namespace {
 
 constexpr int kPackThreads = 256;
 
-// round(x 2^s) to the nearest integer, ties to even (llrint of the exactly
-// scaled value), with integer operations only.  The caller guarantees
-// |x| 2^s < 2^48.
+// round(x 2^s) to the nearest integer, halves away from zero, with integer
+// operations only.  The caller guarantees |x| 2^s < 2^48, so the mantissa is
+// shifted right by at least five bits.
 __device__ __forceinline__ long long scale_round(double x, int s) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   int E = (int)((b >> 52) & 0x7FF);
@@ -29,16 +29,14 @@ __device__ __forceinline__ long long scale_round(double x, int s) {
   } else {
     M |= 1ull << 52;
   }
-  const int sh = E - 1075 + s;  // |x| 2^s = M 2^sh
+  const int r = 1075 - E - s;  // |x| 2^s = M 2^-r
   unsigned long long q;
-  if (sh >= 0) {
-    q = M << sh;
+  if (r <= 0) {
+    q = M << -r;  // excluded by the caller's bound; kept exact
+  } else if (r > 63) {
+    return 0;  // below 2^53 2^-64 < 1/2
   } else {
-    const int r = -sh;
-    if (r > 63) return 0;  // below 2^53 2^-64 < 1/2
-    q = M >> r;
-    const unsigned long long rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
-    if (rem > half || (rem == half && (q & 1ull))) ++q;
+    q = ((M >> (r - 1)) + 1) >> 1;
   }
   return (b >> 63) ? -(long long)q : (long long)q;
 }
@@ -154,14 +152,20 @@ __global__ void __launch_bounds__(kPackThreads) pack_digits_kernel(const PackJob
     const int s = kBits * S - e;
     long long N[8];
     const double* p = src + (int64_t)(r0 + r) * job.ld_r;
+    const int k0 = (kt0 * (kKS / 8) + kc) * 8;
+    double xv[8];
+    if (live && k0 + 8 <= job.K && job.ld_k == 1) {  // whole group along a contiguous row
+      const double* q = p + k0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) xv[i] = q[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) xv[i] = (live && k0 + i < job.K) ? p[(int64_t)(k0 + i) * job.ld_k] : 0.0;
+    }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int k = (kt0 * (kKS / 8) + kc) * 8 + i;
-      N[i] = 0;
-      if (live && k < job.K) {
-        const double x = p[(int64_t)k * job.ld_k];
-        N[i] = scale_round(unit_alpha ? (job.alpha < 0 ? -x : x) : x * job.alpha, s);
-      }
+      const double x = xv[i];
+      N[i] = scale_round(unit_alpha ? (job.alpha < 0 ? -x : x) : x * job.alpha, s);
     }
     // Balanced base-128 digits d_q in [-64, 63] (the leading one takes the
     // rest): N + sum_q 64 * 128^q has the plain base-128 digits d_q + 64, so

@@ -170,39 +170,49 @@ static inline double singlet_entry(int jj, int row) {
   return sgn / std::sqrt((double)(jj + 1));
 }
 
+namespace {
+bool hv_triangle(int i, int j, int k) { return k >= std::abs(i - j) && k <= std::abs(i + j) && (i % 2 == k % 2); }
+
+// one entry: <C, C contracted with the singlet on every leg> * sqrt(j+1);
+// each contracted entry is the product chain ((C*S_i)*S_j)*S_k
+double fac_hamilt_vec_entry(int i, int j, int k, std::vector<double>& c) {
+  const int n0 = i + 1, n1 = j + 1, n2 = k + 1, ne = n0 * n1 * n2;
+  c.assign(ne, 0.0);
+  make_cgc(i, j, k, c.data());
+  double prod = 0;
+  for (int e = 0; e < ne; ++e) {
+    const int a = e % n0, b = (e / n0) % n1, cc = e / (n0 * n1);
+    const int abar = n0 - 1 - a, bbar = n1 - 1 - b, cbar = n2 - 1 - cc;
+    double t = c[abar + bbar * n0 + cbar * n0 * n1] * singlet_entry(i, a);
+    t = t * singlet_entry(j, b);
+    t = t * singlet_entry(k, cc);
+    prod += c[e] * t;
+  }
+  return prod * std::sqrt((double)(j + 1));
+}
+}  // namespace
+
 void fac_hamilt_vec(int m, double* out) {
   for (int i = 0; i < m * m * m; ++i) out[i] = 0;
   std::vector<double> c;
   for (int i = 0; i < m; ++i)
     for (int j = 0; j < m; ++j)
-      for (int k = 0; k < m; ++k) {
-        if (!(k >= std::abs(i - j) && k <= std::abs(i + j) && (i % 2 == k % 2))) continue;
-        const int n0 = i + 1, n1 = j + 1, n2 = k + 1, ne = n0 * n1 * n2;
-        c.assign(ne, 0.0);
-        make_cgc(i, j, k, c.data());
-        // <C, C contracted with the singlet on every leg> * sqrt(j+1); each
-        // contracted entry is the product chain ((C*S_i)*S_j)*S_k.
-        double prod = 0;
-        for (int e = 0; e < ne; ++e) {
-          const int a = e % n0, b = (e / n0) % n1, cc = e / (n0 * n1);
-          const int abar = n0 - 1 - a, bbar = n1 - 1 - b, cbar = n2 - 1 - cc;
-          double t = c[abar + bbar * n0 + cbar * n0 * n1] * singlet_entry(i, a);
-          t = t * singlet_entry(j, b);
-          t = t * singlet_entry(k, cc);
-          prod += c[e] * t;
-        }
-        out[(i * m + j) * m + k] = prod * std::sqrt((double)(j + 1));
-      }
+      for (int k = 0; k < m; ++k)
+        if (hv_triangle(i, j, k)) out[(i * m + j) * m + k] = fac_hamilt_vec_entry(i, j, k, c);
 }
 
-const std::vector<double>& fac_hamilt_vec_table() {
-  static std::vector<double> table;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    table.assign(kMaxAngm * kMaxAngm * kMaxAngm, 0.0);
-    fac_hamilt_vec(kMaxAngm, table.data());
+double fac_hamilt_vec_at(int i, int j, int k) {
+  constexpr int m = kMaxAngm;
+  static std::vector<double> table((size_t)m * m * m, 0.0);
+  static std::once_flag once[m];
+  if (i < 0 || j < 0 || k < 0 || i >= m || j >= m || k >= m) return 0.0;
+  std::call_once(once[j], [j] {
+    std::vector<double> c;
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b)
+        if (hv_triangle(a, j, b)) table[((size_t)a * m + j) * m + b] = fac_hamilt_vec_entry(a, j, b, c);
   });
-  return table;
+  return table[((size_t)i * m + j) * m + k];
 }
 
 namespace {

@@ -17,7 +17,12 @@ namespace su2g {
 
 constexpr int kMaxLegs = 4;
 constexpr int kFuseCap = 38;   // su2bond.cpp:177
-constexpr int kMaxAngm = 25;   // dmrg_su2.cpp:46 (tables hold 2j < 25)
+// The engine's recoupling arrays hold 2j < 25 (max_angm, dmrg_su2.cpp:46),
+// while su2bond::fuse lets bonds reach 2j = 38; a run whose bonds pass 2j = 24
+// (a large-D warm-up keeps high-spin multiplets until D binds) reads outside
+// the engine's arrays.  The coefficients here are computed on demand from the
+// Clebsch-Gordan contractions, so they extend to the fuse cap.
+constexpr int kMaxAngm = kFuseCap + 1;
 
 struct Bond {
   int dir = 1;
@@ -75,8 +80,9 @@ double factorial(int n);
 void make_cgc(int j1, int j2, int j3, double* out);
 // fac_hamilt_vec[i][j][k] stored at (i*m + j)*m + k, m = max_angm
 void fac_hamilt_vec(int max_angm, double* out);
-// the table for kMaxAngm, computed once and cached
-const std::vector<double>& fac_hamilt_vec_table();
+// fac_hamilt_vec[i][j][k] for 2j < kMaxAngm: the slab of one operator spin j
+// is computed on first use (the same arithmetic as fac_hamilt_vec) and cached
+double fac_hamilt_vec_at(int i, int j, int k);
 
 // fac_operator_transformation_{left (side 0), rght (side 1)}[j][m][l][i][k][p]
 // of dmrg_su2.cpp:857-890: the ratio between the three-CG contraction of

@@ -20,7 +20,9 @@
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
+#include <algorithm>
 #include <cmath>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -226,27 +228,52 @@ struct Sector {
   std::vector<double> s;  // dc values, ascending
 };
 
-// tensor::svd for one m x n block (n0 = 1)
-void sector_svd(Ctx& c, const double* blk, int m, int n, double p1, double p2, int max_dcut, Sector* out) {
-  const bool tall = m >= n;
-  const int k = tall ? n : m;
-  double* G = c.dalloc((int64_t)k * k);
-  double* A0 = c.dalloc((int64_t)k * k);
+// First pass of tensor::svd for one m x n block (n0 = 1): the Gram matrix of
+// the smaller side and its eigendecomposition (tensor.cpp:1484-1490).
+struct SectorEig {
+  bool tall = true;
+  int k = 0;
+  double* G = nullptr;   // eigenvectors (k x k)
+  double* A0 = nullptr;  // the Gram matrix
+  std::vector<double> w;  // eigenvalues, ascending
+};
+
+void sector_eig(Ctx& c, const double* blk, int m, int n, SectorEig* e) {
+  e->tall = m >= n;
+  const int k = e->k = e->tall ? n : m;
+  e->G = c.dalloc((int64_t)k * k);
+  e->A0 = c.dalloc((int64_t)k * k);
   if (!c.ok()) return;
-  if (tall) c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, blk, m, blk, m, G, n);
-  else c.gemm(CUBLAS_OP_N, CUBLAS_OP_T, m, m, n, blk, m, blk, m, G, m);
-  c.copy(A0, G, (int64_t)k * k);
-  std::vector<double> w;
-  c.eigh(G, k, &w);  // G now holds the eigenvectors (k x k)
+  if (e->tall) c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, blk, m, blk, m, e->G, n);
+  else c.gemm(CUBLAS_OP_N, CUBLAS_OP_T, m, m, n, blk, m, blk, m, e->G, m);
+  c.copy(e->A0, e->G, (int64_t)k * k);
+  c.eigh(e->G, k, &e->w);  // G now holds the eigenvectors
+}
+
+// Second pass: the reference's refinement of the small-eigenvalue subspace
+// (tensor.cpp:1491-1529), then the factors.  Each refinement re-solves the
+// subspace of eigenvalues below 0.1 of its largest and rotates only those
+// columns, so a subspace whose largest eigenvalue is below 0.1 of lam_cut (the
+// max_dcut-th largest eigenvalue over all sectors, 0 when every multiplet is
+// kept or when the cut is too close to the first pass's rounding error to be
+// placed) holds no multiplet the truncation keeps: refining it further changes
+// neither the kept columns, their values nor the selection, and is skipped
+// (its values, all discarded, stay those of the last refinement).
+void sector_finish(Ctx& c, const double* blk, int m, int n, double p1, double p2, int max_dcut, double lam_cut,
+                   SectorEig& e, Sector* out) {
+  const bool tall = e.tall;
+  const int k = e.k;
+  double* G = e.G;
+  std::vector<double>& w = e.w;
   if (!c.ok()) return;
   int np = small_count(w, k);
-  if (np > 1) {  // refinement of the small-eigenvalue subspace (tensor.cpp:1498-1529)
+  if (np > 1 && !(lam_cut > 0 && w[np - 1] < 0.1 * lam_cut)) {
     double* ap = c.dalloc((int64_t)k * k);
     double* vp = c.dalloc((int64_t)k * k);
     double* app = c.dalloc((int64_t)k * k);
     double* vpp = c.dalloc((int64_t)k * k);
     double* tmp = c.dalloc((int64_t)k * k);
-    c.copy(ap, A0, (int64_t)k * k);
+    c.copy(ap, e.A0, (int64_t)k * k);
     c.copy(vp, G, (int64_t)k * k);
     int npp = np;
     np = k;
@@ -264,6 +291,7 @@ void sector_svd(Ctx& c, const double* blk, int m, int n, double p1, double p2, i
       const int j = small_count(ws, npp);
       np = npp;
       npp = j;
+      if (npp > 1 && lam_cut > 0 && ws[npp - 1] < 0.1 * lam_cut) break;
     } while (npp > 1 && c.ok());
   }
   if (!c.ok()) return;
@@ -384,20 +412,51 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
     const cudaError_t we = cudaStreamWaitEvent(c.st, ready, 0);  // psi is written on the caller's stream
     if (we != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(we));
   }
-  auto run = [&](size_t q) {
+  // two passes over the sectors, each sector on its own host thread: the
+  // eigendecompositions, then (with the global cut known) the refinements
+  // and the factors
+  std::vector<SectorEig> eig(jobs.size());
+  double lam_cut = 0.0;
+  auto on_threads = [&](auto&& body) {
+    std::vector<std::thread> threads;
+    for (size_t q = 1; q < jobs.size(); ++q) threads.emplace_back(body, q);
+    if (!jobs.empty()) body(0);
+    for (std::thread& t : threads) t.join();
+  };
+  on_threads([&](size_t q) {
+    Ctx& c = *ctx[q];
+    if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
+    if (c.ok()) sector_eig(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, &eig[q]);
+  });
+  {  // the max_dcut-th largest eigenvalue over all sectors; 0 (refine every
+     // subspace, as the reference) when nothing is cut or when the cut lies
+     // within 1e3 of the first pass's error k eps lambda_max of some sector,
+     // where values near it are not yet known well enough to place them
+    std::vector<double> all;
+    double floor = 0.0;
+    for (const SectorEig& e : eig) {
+      const double top = e.w.empty() ? 0.0 : e.w.back();
+      floor = std::max(floor, (double)e.k * 2.3e-16 * top);
+      for (double v : e.w)
+        if (v > 0 && v / top > 1.e-100) all.push_back(v);
+    }
+    if (max_dcut > 0 && (int64_t)all.size() > max_dcut) {
+      std::nth_element(all.begin(), all.begin() + (max_dcut - 1), all.end(), std::greater<double>());
+      lam_cut = all[max_dcut - 1];
+      if (lam_cut < 1e3 * floor) lam_cut = 0.0;
+    }
+  }
+  on_threads([&](size_t q) {
     Ctx& c = *ctx[q];
     if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
     if (c.ok()) {
       secs[q].i = jobs[q].i;
-      sector_svd(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, p1, p2, max_dcut, &secs[q]);
+      sector_finish(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, p1, p2, max_dcut, lam_cut, eig[q],
+                    &secs[q]);
     }
     const cudaError_t e = cudaEventRecord(res.lanes[q].done, c.st);
     if (e != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
-  };
-  std::vector<std::thread> threads;
-  for (size_t q = 1; q < jobs.size(); ++q) threads.emplace_back(run, q);
-  if (!jobs.empty()) run(0);
-  for (std::thread& t : threads) t.join();
+  });
   // the caller's stream continues after every sector (placement copies, frees)
   for (size_t q = 0; q < jobs.size(); ++q) cudaStreamWaitEvent(cst, res.lanes[q].done, 0);
   cudaEventDestroy(ready);

@@ -20,6 +20,8 @@ from __future__ import annotations
 
 import time
 
+import numpy as np
+
 from . import su2 as S
 from .warmup import Warmup
 
@@ -29,6 +31,23 @@ class Dmrg(Warmup):
     does not reach (dmrg_su2.cpp:54 sets 2)."""
 
     nfree = 2
+
+    def clone(self, mode: int = None) -> "Dmrg":
+        """A copy of the whole device state (MPS, block Hamiltonians, site and
+        plaquette operators) that continues independently, in `mode` (default:
+        this one's)."""
+        def cp(t):
+            return None if t is None else (t[0], t[1].clone())
+
+        d = Dmrg(self.lat, mode=self.mode if mode is None else mode, mlanc=self.mlanc)
+        d.uu = [cp(t) for t in self.uu]
+        d.hh = [cp(t) for t in self.hh]
+        d.opr = [[cp(t) for t in row] for row in self.opr]
+        d.plq = [[cp(t) for t in row] for row in self.plq]
+        d.energies = list(self.energies)
+        d.truncations = list(self.truncations)
+        d.ww = self.ww
+        return d
 
     def _vectran(self, i: int, flag: int) -> None:
         """wavefunc_transformation(i, flag): right2left_vectran (0) or
@@ -51,6 +70,7 @@ class Dmrg(Warmup):
         tu, xu, tv, xv, w = S.svd(vs, vx, self.uu[il][0], p1, self.uu[ir][0], p2, L.max_dcut)
         self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
         self.ww = w
+        self.truncations.append((il, ir, int(sum(tu.bonds[2].dim)), np.asarray(w)))
         return e
 
     def sweep(self) -> float:

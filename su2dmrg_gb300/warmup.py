@@ -20,6 +20,7 @@ overlaps (ovlp, orth) are not built.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -46,6 +47,21 @@ class Lattice:
     max_dcut: int
 
     @classmethod
+    def cylinder(cls, lx: int, ly: int, delta: float, qdelta: float, max_dcut: int, boundary: int = 2,
+                 totspin: int = 0) -> "Lattice":
+        """An lx x ly spin-1/2 cylinder built here (cylinder_tables), with the
+        engine's spin-1/2 one-site operators (site_ops_spin_half.npz)."""
+        hmap, coup, fll, frr, plqflg, plqpos = cylinder_tables(lx, ly, delta, qdelta, boundary)
+        g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "site_ops_spin_half.npz"))
+        ops = []
+        for i in range(10):
+            st = S._parse_desc(g[f"site{i}_desc"])
+            st.flag = np.ascontiguousarray(g[f"site{i}_flag"], np.int32)
+            ops.append((st, np.ascontiguousarray(g[f"site{i}_x"], np.float64)))
+        return cls(lx * ly, 1, int(totspin), hmap, coup, fll, frr, plqflg, plqpos, float(qdelta), ops[:2], ops[2:10],
+                   int(max_dcut))
+
+    @classmethod
     def from_tables(cls, ints, coup, sites, qdelta: float, max_dcut: int) -> "Lattice":
         """From the flat layout [ns, physpn, totspin, hmap, fll, frr, plqflg
         (each ns x ns, row-major), plqpos (ns x 4)], coup[0..ns) and the ten
@@ -70,6 +86,104 @@ class Lattice:
                    plqpos, float(qdelta), ops[:2], ops[2:10], int(max_dcut))
 
 
+def _snake(x: int, y: int, ly: int) -> int:
+    """Site index of column x, row y: columns in order, rows reversed in odd
+    columns (dmrg_su2.cpp:174-177)."""
+    return x * ly + (y if x % 2 == 0 else ly - 1 - y)
+
+
+def cylinder_tables(lx: int, ly: int, delta: float, qdelta: float, boundary: int = 2):
+    """The engine's lattice tables for an lx x ly cylinder (open in x, periodic
+    in y), restated from the dmrg_su2 constructor (dmrg_su2.cpp:93-300):
+
+      hmap[i][k]  coupling class of sites i, k (0 none, 1 nearest neighbour,
+                  2 diagonal / next-nearest, 3 vertical bond on the open ends of
+                  the boundary-2 lattice), for boundary 0 (square, periodic),
+                  1 (J1-J3), 2 (J1-J2) and 3 (Shastry-Sutherland);
+      coup[c]     delta + qdelta/2, 1 - |qdelta|, delta + qdelta/4 for c = 1, 2, 3;
+      plqpos[m]   the four sites of the plaquette at column m/ly, row m%ly
+                  (periodic in both directions), ascending;
+      plqflg[i][m]  plaquette m spans site i (|qdelta| > 1e-5, not the last column);
+      fll / frr   operators site i must carry for bonds and plaquettes that
+                  cross it towards the right / left.
+
+    Returns (hmap, coup, fll, frr, plqflg, plqpos) as numpy arrays."""
+    ns = lx * ly
+    hmap = np.zeros((ns, ns), np.int32)
+    for k in range(5):
+        for i in range(ns):
+            x1 = i // ly
+            y1 = i % ly if x1 % 2 == 0 else ly - 1 - (i % ly)
+            nb = None
+            if boundary == 0:
+                if k == 0:
+                    nb = ((x1 + 1) % lx, y1)
+                elif k == 1:
+                    nb = (x1, (y1 + 1) % ly)
+            elif boundary == 2:
+                nb = {0: (x1 + 1, y1), 1: (x1, (y1 + 1) % ly), 2: (x1 + 1, (y1 + 1) % ly),
+                      3: (x1 - 1, (y1 + 1) % ly)}.get(k)
+            elif boundary == 1:
+                nb = {0: (x1 + 1, y1), 1: (x1, (y1 + 1) % ly), 2: (x1 + 2, y1), 3: (x1, (y1 + 2) % ly)}.get(k)
+            elif boundary == 3:
+                if k == 0:
+                    nb = (x1 + 1, y1)
+                elif k == 1:
+                    nb = (x1, (y1 + 1) % ly)
+                elif k == 2 and x1 % 2 == 0 and y1 % 2 == 0:
+                    nb = (x1 + 1, (y1 + 1) % ly)
+                elif k == 3 and x1 % 2 == 1 and y1 % 2 == 0:
+                    nb = (x1 + 1, (y1 + ly - 1) % ly)
+                elif k == 4 and (x1 == 0 or x1 == lx - 1):
+                    nb = (x1 + 1, (y1 + 2) % ly)
+            if nb is None:
+                continue
+            x2, y2 = nb
+            if not (0 <= x2 < lx and 0 <= y2 < ly):
+                continue
+            j = _snake(x2, y2, ly)
+            if boundary == 2 and k == 1 and (x1 == 0 or x1 == lx - 1):
+                c = 3
+            elif (boundary == 3 and k < 2) or (boundary in (1, 2) and 2 <= k < 4):
+                c = 2
+            elif (boundary == 3 and 2 <= k < 4) or (boundary in (0, 1, 2) and k < 2):
+                c = 1
+            else:
+                continue
+            hmap[i][j] = hmap[j][i] = c
+    plqpos = np.zeros((ns, 4), np.int32)
+    for m in range(ns):
+        x1, y1 = m // ly, m % ly
+        corners = [(x1, y1), (x1 % lx, (y1 + 1) % ly), ((x1 + 1) % lx, (y1 + 1) % ly), ((x1 + 1) % lx, y1)]
+        plqpos[m] = sorted(_snake(x, y, ly) for x, y in corners)
+    coup = np.zeros(max(ns, 4))
+    coup[1] = delta + qdelta / 2.0
+    coup[2] = 1.0 - abs(qdelta)
+    coup[3] = delta + qdelta / 4.0
+    plqflg = np.zeros((ns, ns), np.int32)
+    if abs(qdelta) > 1e-5:
+        for i in range(ns):
+            for j in range(ns - ly):
+                if plqpos[j][0] <= i <= plqpos[j][3]:
+                    plqflg[i][j] = 1
+    fll = np.zeros((ns, ns), np.int32)
+    frr = np.zeros((ns, ns), np.int32)
+    for i in range(ns):
+        for j in range(i):
+            if np.any(hmap[j, i + 1:] != 0):
+                fll[i][j] = 1
+        for j in range(ns):
+            if plqflg[i][j] and plqpos[j][0] < i < plqpos[j][1]:
+                fll[i][plqpos[j][0]] = 1
+        for j in range(i + 1, ns):
+            if np.any(hmap[j, :i] != 0):
+                frr[i][j] = 1
+        for j in range(ns):
+            if plqflg[i][j] and plqpos[j][2] < i < plqpos[j][3]:
+                frr[i][plqpos[j][3]] = 1
+    return hmap, coup, fll, frr, plqflg, plqpos
+
+
 @dataclass
 class _Jobs:
     """One environment batch: jobs and their named output slots."""
@@ -87,6 +201,14 @@ class _Jobs:
         self.jobs.append(j)
 
 
+def discarded_weight(kept: int, w) -> float:
+    """Discarded fraction of the squared singular values of one truncation
+    (w: kept then discarded, as the svd returns them)."""
+    w = np.asarray(w, np.float64)
+    tot = float(np.sum(w * w))
+    return float(np.sum(w[kept:] ** 2)) / tot if tot > 0 else 0.0
+
+
 class Warmup:
     """do_idmrg on the device.  mode: capi.MODE_* for every contraction."""
 
@@ -99,6 +221,7 @@ class Warmup:
         self.plq = [[None] * (2 * ns) for _ in range(ns)]
         self.energies = []   # (il, ir, eigenvalue) per Lanczos step
         self.ww = None       # singular values of the last truncation
+        self.truncations = []  # (il, ir, kept multiplets, singular values kept then discarded) per step
         self._keep = []
 
     # ---------------------------------------------------------- helpers
@@ -330,4 +453,5 @@ class Warmup:
                 tu, xu, tv, xv, w = S.svd(vs, vx, ul[0], p1, ur[0], p2, L.max_dcut)
                 self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
                 self.ww = w
+                self.truncations.append((il, ir, int(sum(tu.bonds[2].dim)), np.asarray(w)))
         return self.energies[-1][2] if self.energies else None

@@ -704,6 +704,14 @@ def main():
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)
         return
+    if "--only-siteops" in sys.argv:
+        # the engine's spin-1/2 one-site operators (initialize_local_operators,
+        # dmrg_su2.cpp:427-520), packaged with the library for Lattice.cylinder
+        L.ref_setup(1, 25)
+        c = engine_tables(L, 4, 2, 16, 1.0, 1.0)
+        np.savez(os.path.join(REPO, "su2dmrg_gb300", "site_ops_spin_half.npz"),
+                 **{k: v for k, v in c.items() if k.startswith("site")})
+        return
     if "--only-sweep" in sys.argv:
         L.ref_setup(1, 25)
         for c in sweep_cases(L):

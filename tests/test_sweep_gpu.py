@@ -2,12 +2,12 @@
 warm-up, then dmrg_su2::sweep until a sweep changes the energy by less than
 1e-6, as main_omp does) against whole runs of the reference engine
 (tests/golden/dmrg_energies.json: J1-J2 4x2 and 3x4 and J-Q 3x4 at D=64, J1-J2
-6x4 with J2/J1 = 2 at D=200; lattice tables in tests/golden/sweep_*.npz).
+6x4 with nearest-neighbour coupling 2 and diagonal 1 at D=200; lattice tables in tests/golden/sweep_*.npz).
 
 The warm-up's path follows rounding noise (tests/test_warmup_gpu.py), but
 the sweeps converge to the same state: the converged energy in FP64 and in
-split precision is the reference's to 1e-10 relative, and the final MPS has
-the reference's retained multiplets, sector by sector, at every bond."""
+split precision is the reference's to 1e-10 relative, and the final FP64 MPS
+has the reference's retained multiplets, sector by sector, at every bond."""
 import json
 import os
 
@@ -41,25 +41,38 @@ _CACHE = {}
 
 def _run(c, mode):
     from su2dmrg_gb300.sweep import Dmrg
+    from su2dmrg_gb300.warmup import discarded_weight
 
     if (c, mode) not in _CACHE:
         d = Dmrg(_lattice(c), mode=mode)
         e, _ = d.run_dmrg(RUNS[c]["niter"])
-        _CACHE[(c, mode)] = (e, [d.uu[i][0].desc().tolist() for i in range(d.lat.ns)])
+        dw = {}  # site -> discarded weight of the last truncation that set its bond
+        for il, ir, kept, w in d.truncations:
+            dw[il] = dw[ir] = discarded_weight(kept, w)
+        _CACHE[(c, mode)] = (e, [d.uu[i][0].desc().tolist() for i in range(d.lat.ns)], dw)
     return _CACHE[(c, mode)]
 
+
+def _legs(desc):
+    """[(dir, spins, dims)] per leg of a structure descriptor."""
+    out, p = [], 2
+    for _ in range(desc[0]):
+        n = desc[p + 1]
+        out.append((desc[p], desc[p + 2: p + 2 + n], desc[p + 2 + n: p + 2 + 2 * n]))
+        p += 2 + 2 * n
+    return out
 
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("c", range(len(RUNS)))
 def test_sweep_energy_matches_reference(torch_cuda, c, mode):
-    e, _ = _run(c, mode)
+    e, _, _ = _run(c, mode)
     ref = RUNS[c]["energies_minus_1000"][-1] + 1000.0
     assert abs(e[-1] - ref) <= 1e-10 * abs(ref), (e, ref)
 
 
 @pytest.mark.parametrize("c", range(len(RUNS)))
 def test_sweep_retained_multiplets_match_reference(torch_cuda, c):
-    _, descs = _run(c, 0)
+    _, descs, _ = _run(c, 0)
     ref = RUNS[c]["mps_desc"]
     assert len(descs) == len(ref)
     for i, (a, b) in enumerate(zip(descs, ref)):
@@ -69,8 +82,21 @@ def test_sweep_retained_multiplets_match_reference(torch_cuda, c):
 @pytest.mark.parametrize("c", range(len(RUNS)))
 def test_split_sweep_matches_fp64(torch_cuda, c):
     """Split-precision contractions against the FP64 path: converged energies
-    to 1e-10 relative and the same retained multiplets."""
-    e0, d0 = _run(c, 0)
-    e1, d1 = _run(c, 1)
+    to 1e-10 relative, and per bond the same retained multiplets, sector by
+    sector, or, where the two runs settled on different truncations of the
+    same quality, the same total with discarded weights within 1e-10 (at
+    D = 200 on 6x4 a 1e-16 change of the arithmetic moves one multiplet
+    between sectors at one bond)."""
+    e0, d0, w0 = _run(c, 0)
+    e1, d1, w1 = _run(c, 1)
     assert abs(e1[-1] - e0[-1]) <= 1e-10 * abs(e0[-1])
-    assert d1 == d0
+    assert len(d0) == len(d1)
+    for i, (a, b) in enumerate(zip(d0, d1)):
+        if a == b:
+            continue
+        la, lb = _legs(a), _legs(b)
+        assert [x[:2] for x in la] == [x[:2] for x in lb], i  # directions and sector spins
+        for x, y in zip(la, lb):  # a bond whose multiplets differ (it is a leg of both its sites)
+            if x[2] != y[2]:
+                assert sum(x[2]) == sum(y[2]), i
+                assert abs(w0[i] - w1[i]) <= 1e-10, (i, w0[i], w1[i])
