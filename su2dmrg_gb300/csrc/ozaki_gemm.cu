@@ -288,12 +288,16 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm(const OzTile* __restri
 #pragma unroll
             for (int p = 1; p <= S; ++p) {
               const uint64_t ad = smem_desc(sa + (p - 1) * (kTM * kKS * 2));
-#pragma unroll
-              for (int q = 1; q <= S + 1 - p; q += 4) {
-                const int n = (S + 2 - p - q) < 4 ? (S + 2 - p - q) : 4;
-                const uint64_t bd = smem_desc(sb + (q - 1) * (kTN * kKS * 2));
-                mma(tmem + (uint32_t)((p + q - 2) * kTN), ad, bd, idesc(kTN * n), (first && p == 1) ? 0u : 1u);
-              }
+              // partners of p split into MMAs of at most four slices; five
+              // go as 3 + 2, not 4 + 1 (an N = 64 MMA costs more than its
+              // width: 3.81 instead of 3.85 ms per D = 2000 application;
+              // 6 = 3 + 3 measured no better than 4 + 2)
+              const int np = S + 1 - p;
+              const int n1 = np <= 4 ? np : (np == 5 ? 3 : 4);
+              mma(tmem + (uint32_t)((p - 1) * kTN), ad, smem_desc(sb), idesc(kTN * n1), (first && p == 1) ? 0u : 1u);
+              if (np > n1)
+                mma(tmem + (uint32_t)((p - 1 + n1) * kTN), ad, smem_desc(sb + n1 * (kTN * kKS * 2)),
+                    idesc(kTN * (np - n1)), (first && p == 1) ? 0u : 1u);
             }
             mma_commit(smem_u32(&bar_empty[st]));
             if ((ks % kChunkStages) == kChunkStages - 1 || ks == nks - 1) {
