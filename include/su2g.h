@@ -381,6 +381,12 @@ int su2g_enr_read(const char* path, double* values, int cap, int* count);
 int su2g_ww_save(const char* path, const double* ww, int64_t n);
 int su2g_ww_load(const char* path, double* ww, int64_t n, int64_t* nread);
 
+/* Failure detection of the device waits, without a fault: runs the split
+ * GEMM's bounded mbarrier wait on a barrier nothing arrives at, giving up
+ * after `iterations` polls (> 0).  Returns SU2G_ETIMEOUT when the wait gave
+ * up, as it must (the context stays usable), SU2G_OK if it completed. */
+int su2g_selftest_bounded_wait(long long iterations, void* stream);
+
 /* ------------------------------------------------------------ Lanczos -- */
 /* Ground state of the plan's H_eff by the reference's Lanczos scheme
  * (lanczos_su2::lanczos1, lanczos_su2.cpp:125-195, driven as in

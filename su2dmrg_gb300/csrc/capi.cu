@@ -494,6 +494,14 @@ int su2g_heff_plan_launches(const su2g_heff_plan* p, int* n) {
   return SU2G_OK;
 }
 
+int su2g_selftest_bounded_wait(long long iterations, void* stream) {
+  if (iterations <= 0) return fail(SU2G_EINVAL, "selftest_bounded_wait: iterations must be positive");
+  int timed_out = 0;
+  SU2G_CUDA(su2g::oz::bounded_wait_selftest(iterations, &timed_out, (cudaStream_t)stream));
+  if (timed_out) return fail(SU2G_ETIMEOUT, "bounded wait gave up after " + std::to_string(iterations) + " polls");
+  return SU2G_OK;
+}
+
 int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
   if (!p || !code) return fail(SU2G_EINVAL, "plan_status: bad arguments");
   *code = 0;

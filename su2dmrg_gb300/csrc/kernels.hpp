@@ -40,6 +40,9 @@ cudaError_t launch_reduce(const RedTile* reds, int n, const Bases& bases, cudaSt
 // one-time per-process setup of the GEMM kernel (function attributes, SM count),
 // done before any launch is captured into a graph
 cudaError_t prepare_ozaki_gemm(int S);
+// runs the GEMM's bounded mbarrier wait on a barrier nothing arrives at, with
+// `limit` polls; *timed_out_host = 1 when it gave up (the expected outcome)
+cudaError_t bounded_wait_selftest(long long limit, int* timed_out_host, cudaStream_t stream);
 // CTAs of the persistent GEMM grid on the current device (its SM count); 152
 // when no device answers (host-only planning and validation).
 int ozaki_persistent_grid();

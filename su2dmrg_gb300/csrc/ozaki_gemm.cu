@@ -47,8 +47,8 @@ __device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
-  for (long long i = 0; i < kWaitIters; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, long long limit = kWaitIters) {
+  for (long long i = 0; i < limit; ++i) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -473,6 +473,31 @@ int gemm_smem_bytes(int S) {
     case 8: return Smem<8>::kBytes;
   }
   return 0;
+}
+
+namespace {
+// The GEMM's bounded wait on an mbarrier that nothing arrives at: it must give
+// up after `limit` polls and report it, leaving the context usable.
+__global__ void bounded_wait_selftest_kernel(long long limit, int* timed_out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *timed_out = mbar_wait(smem_u32(&bar), 0, limit) ? 0 : 1;
+  }
+}
+}  // namespace
+
+cudaError_t bounded_wait_selftest(long long limit, int* timed_out_host, cudaStream_t stream) {
+  int* d = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&d, sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  bounded_wait_selftest_kernel<<<1, 32, 0, stream>>>(limit, d);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(timed_out_host, d, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaFreeAsync(d, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return e;
 }
 
 namespace {
