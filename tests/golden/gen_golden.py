@@ -704,6 +704,19 @@ def main():
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)
         return
+    if "--only-lattices" in sys.argv:
+        # lattice tables of the other boundary conditions (0 square, 1 J1-J3,
+        # 3 Shastry-Sutherland), with and without plaquettes
+        L.ref_setup(1, 25)
+        out = {}
+        for ci, (lx, ly, bd, jc, qc) in enumerate([(4, 4, 0, 1.0, 0.0), (6, 4, 1, 0.5, 0.0), (4, 4, 3, 0.7, 0.0),
+                                                  (6, 4, 0, 1.0, 0.5), (4, 6, 3, 1.0, 1.0), (5, 4, 1, 2.0, 0.3)]):
+            c = engine_tables(L, lx, ly, 16, jc, qc, bd)
+            for k in ("lx", "ly", "jcoup", "qcoup", "tables", "coup"):
+                out[f"c{ci}_{k}"] = c[k]
+            out[f"c{ci}_boundary"] = np.int32(bd)
+        np.savez(os.path.join(HERE, "lattice_tables.npz"), **out)
+        return
     if "--only-siteops" in sys.argv:
         # the engine's spin-1/2 one-site operators (initialize_local_operators,
         # dmrg_su2.cpp:427-520), packaged with the library for Lattice.cylinder
