@@ -101,14 +101,23 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The largest x over the ranks (replicas: each rank times its own copy of
+    the workload; the job takes as long as the slowest)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_throughput(units_per_step, world, steps, seconds):
+    """Whole-job rate: every rank processes units_per_step per step (weak
+    scaling, replicas), over the max-over-ranks time."""
+    return units_per_step * world * steps / seconds
 
 
 class ClockSampler:
@@ -312,7 +321,7 @@ def run_su2g(args):
     total = t0.elapsed_time(t1) / 1e3
     total = max_over_ranks(total, world)
     ms_per_step = total / args.steps * 1e3
-    value = flops * world * args.steps / total / 1e12
+    value = job_throughput(flops, world, args.steps, total) / 1e12
 
     # ---- end to end through the C ABI with host buffers ----
     h_psi = torch.from_numpy(w.psi_data.copy()).pin_memory()
@@ -334,7 +343,7 @@ def run_su2g(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_total = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
-    e2e_value = flops * world * args.steps / e2e_total / 1e12
+    e2e_value = job_throughput(flops, world, args.steps, e2e_total) / 1e12
     nbytes = psi.numel() * 8
 
     if rank != 0:
