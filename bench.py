@@ -293,6 +293,7 @@ def run_su2g(args):
     capi.lib()
     w = synthetic_heff(D=args.D, nspin1=args.nspin1, seed=1234)
     psi, terms, hl, hr = w.to_device()
+    op_bytes = 8.0 * (sum(t[1].numel() + t[3].numel() for t in terms) + sum(h[1].numel() for h in (hl, hr) if h))
     plan = HeffPlan(w.psi, terms, hl, hr, mode=MODES[args.mode])
     info = plan.info()
     flops = info["flops"]
@@ -407,7 +408,7 @@ def run_su2g(args):
         "config": {"workload": f"synthetic SU(2) two-site H_eff, D={args.D}, width {args.nspin1 + 2}",
                    "mode": args.mode, "psi_doubles": int(psi.numel()), "flops_per_step": flops,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs (operators ~1.3 GB) larger than L2; no flush"},
+                   "l2": f"inputs (operators {op_bytes / 1e9:.1f} GB) larger than L2; no flush"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "path": "su2g_heff_apply via ctypes, pinned host psi -> device -> host y; operators resident"},
         "gpu_launches": plan.launches() * args.steps,
