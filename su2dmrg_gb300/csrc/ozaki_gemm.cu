@@ -114,9 +114,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // an FP32 group sum is an integer below 2^24 in magnitude: the conversion is exact
 __device__ __forceinline__ int f32_to_int_exact(uint32_t bits) { return __float2int_rn(__uint_as_float(bits)); }
 
-__device__ __forceinline__ long long shl_signed(long long v, int s) { return s >= 0 ? (v << s) : (v >> (-s)); }
-
-// Weighted sum of one column's S group sums, v = sum_g shl_signed(G_g, 34 - 7g)
+// Weighted sum of one column's S group sums, v = sum_g G_g 2^(34 - 7g)
 // (group g weighs 2^(kFixedTop - 7(g+2))), from their FP32 bit patterns, in
 // few instructions: |G_g| <= 7 * 560 * 65^2 = 16,562,000 (the exactness bound
 // of a chunk), so G_1 * 128 + G_2 and G_3 * 128 + G_4 are exact in int32
