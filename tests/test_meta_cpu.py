@@ -329,3 +329,27 @@ def test_fuse_tensor_layout_matches_reference(su2lib):
         assert s.desc().tolist() == g[f"desc{i}"].tolist()
         assert s.flag.tolist() == g[f"flag{i}"].tolist()
         assert s.size() == len(g[f"x{i}"])
+
+
+def test_cgc_orthonormal_up_to_the_fuse_cap(su2lib):
+    """The recoupling coefficients extend past the engine's 2j < 25 tables to
+    the fuse cap 2j = 38 (a large-D warm-up reaches such bonds): the
+    Clebsch-Gordan tensors they are built from stay orthonormal there."""
+    import ctypes
+
+    def cgc(j1, j2, j3):
+        out = np.zeros((j1 + 1) * (j2 + 1) * (j3 + 1))
+        assert su2lib.su2g_make_cgc(j1, j2, j3, out.ctypes.data_as(ctypes.c_void_p)) == 0
+        return out.reshape(j3 + 1, j2 + 1, j1 + 1)
+
+    worst = 0.0
+    for j1, j2 in [(24, 2), (31, 2), (38, 2), (37, 1), (34, 6), (20, 20)]:
+        rows = {j3: cgc(j1, j2, j3) for j3 in range(abs(j1 - j2), min(j1 + j2, 38) + 1, 2)}
+        for j3, C in rows.items():
+            for m3 in range(-j3, j3 + 1, 2):
+                a = C[(m3 + j3) // 2]
+                worst = max(worst, abs(float(np.sum(a * a)) - 1.0))
+                for j3b, Cb in rows.items():
+                    if j3b > j3:
+                        worst = max(worst, abs(float(np.sum(a * Cb[(m3 + j3b) // 2]))))
+    assert worst < 1e-14
