@@ -353,3 +353,14 @@ def test_cgc_orthonormal_up_to_the_fuse_cap(su2lib):
                     if j3b > j3:
                         worst = max(worst, abs(float(np.sum(a * Cb[(m3 + j3b) // 2]))))
     assert worst < 1e-14
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built CUDA library every entry point
+    raises instead of computing anything."""
+    from su2dmrg_gb300 import capi
+
+    monkeypatch.setattr(capi, "_lib", None)
+    monkeypatch.setattr(capi, "LIB_PATH", str(tmp_path / "libsu2g.so"))
+    with pytest.raises(RuntimeError, match="is not built"):
+        capi.lib()
