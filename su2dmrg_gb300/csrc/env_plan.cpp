@@ -530,8 +530,12 @@ int build_input_vector(const su2g_tensor& ul, const su2g_tensor& ur, const doubl
     *err = "input vector: legs 0 and 1 of an MPS tensor have different directions";
     return SU2G_EINVAL;
   }
-  // vec.contract(left, 0, rght, 0) joins the two centre bonds
-  if (!same_bond(L.legs[2], R.legs[2])) {
+  // vec.contract(left, 0, rght, 0) joins the two centre bonds.  The structure
+  // alone (every block of equal spins of the fused legs, makeup_input_vector)
+  // does not depend on them: the warm-up's start vector joins blocks whose
+  // outer bonds differ when the total spin is not 0 (fuse_to_singlet,
+  // tensor_su2.cpp:1202-1247), and only its structure is used.
+  if (out && !same_bond(L.legs[2], R.legs[2])) {
     *err = "input vector: ul and ur do not share their leg 2";
     return SU2G_EINVAL;
   }

@@ -400,6 +400,9 @@ def dmrg_runs(L):
         (3, 4, 0, 64, 4, 0.5, 0.0, 2),
         (3, 4, 0, 64, 4, 0.5, 1.0, 2),
         (6, 4, 0, 200, 4, 2.0, 0.0, 2),
+        # total spin 1 (the engine's sector 2j = 2)
+        (4, 2, 2, 64, 4, 0.5, 0.0, 2),
+        (3, 4, 2, 64, 4, 0.5, 1.0, 2),
     ]
     out = []
     cwd = os.getcwd()
@@ -609,14 +612,14 @@ def mea_cases(L):
     return cases
 
 
-def engine_tables(L, lx, ly, d, jc, qc, bd=2):
+def engine_tables(L, lx, ly, d, jc, qc, bd=2, sec=0):
     """The engine's lattice tables and one-site operators (sigma[0], sigma[1],
     qterm[0..8)) for one lattice, as the device warm-up and sweep take them."""
     L.ref_engine_tables.restype = ctypes.c_int
     ints = np.zeros(1 << 16, np.int32)
     dbls = np.zeros(4096)
-    n = L.ref_engine_tables(lx, ly, 0, d, ctypes.c_double(jc), ctypes.c_double(qc), bd, p(ints), len(ints), p(dbls),
-                            len(dbls))
+    n = L.ref_engine_tables(lx, ly, sec, d, ctypes.c_double(jc), ctypes.c_double(qc), bd, p(ints), len(ints),
+                            p(dbls), len(dbls))
     assert n > 0
     ns = int(ints[0])
     case = dict(lx=np.int32(lx), ly=np.int32(ly), d=np.int32(d), jcoup=np.float64(jc), qcoup=np.float64(qc),
@@ -635,8 +638,8 @@ def sweep_cases(L):
     after the warm-up and after each sweep are the reference's, in that file)."""
     cases = []
     for ci, r in enumerate(json.load(open(os.path.join(HERE, "dmrg_energies.json")))):
-        assert r["boundary"] == 2 and r["sec"] == 0
-        case = engine_tables(L, r["lx"], r["ly"], r["d"], r["jcoup"], r["qcoup"])
+        assert r["boundary"] == 2
+        case = engine_tables(L, r["lx"], r["ly"], r["d"], r["jcoup"], r["qcoup"], sec=r["sec"])
         case["name"] = f"sweep_{ci}"
         cases.append(case)
     return cases

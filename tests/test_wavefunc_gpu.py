@@ -142,3 +142,19 @@ def test_step_move_chain(oracle, torch_cuda):
     s, y = prepare_input_vector(_lib_struct(sl), _dev(torch_cuda, xl), s_rot, x_rot)
     got = y[: s.size()].cpu().numpy()
     assert np.linalg.norm(got - want) <= 1e-12 * np.linalg.norm(want)
+
+
+def test_input_vector_product_refuses_different_centre_bonds(torch_cuda):
+    """U_L U_R^T contracts the two tensors' leg 2: bonds that differ are
+    refused before any device work (the structure alone accepts them)."""
+    from su2dmrg_gb300.capi import Su2gError
+    from su2dmrg_gb300.su2 import prepare_input_vector
+
+    g = np.load(os.path.join(GOLDEN, "inputvec_0.npz"))
+    ur = _from_desc(g["dr"], g["fr"])
+    b2 = ur.bonds[2]
+    ur.bonds[2] = type(b2)(b2.dir, list(b2.angm), [d + 1 for d in b2.dim])
+    ur.flag = np.asarray(ur.flag, np.int32)
+    xr = _dev(torch_cuda, np.zeros(ur.size() + 1))
+    with pytest.raises(Su2gError, match="leg 2"):
+        prepare_input_vector(_from_desc(g["dl"], g["fl"]), _dev(torch_cuda, g["xl"]), ur, xr)
