@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--D", type=int, default=2000)
     ap.add_argument("--nspin1", type=int, default=18)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--row", default="heff", choices=["heff", "input_vector", "vectran", "env", "svd", "sweep"],
+    ap.add_argument("--row", default="heff",
+                    choices=["heff", "input_vector", "vectran", "env", "svd", "sweep", "serve"],
                     help="heff (the headline) or another operation of the site step, timed on the "
                          "D-multiplet site-step workload (workloads.synthetic_site_step); sweep: one whole "
                          "DMRG sweep of a J1-J2 cylinder after the device warm-up, split and FP64 contractions "
@@ -70,6 +71,8 @@ def parse():
                     help="sweep row: nearest-neighbour coupling (diagonal 1 - |qdelta|; 2.0 = J2/J1 0.5)")
     ap.add_argument("--qdelta", type=float, default=0.0, help="sweep row: plaquette coupling Q")
     ap.add_argument("--skip-fp64", action="store_true", help="sweep row: time the split sweep only")
+    ap.add_argument("--requests", type=int, default=6, help="serve row: requests in the sample")
+    ap.add_argument("--rate", type=float, default=0.1, help="serve row: Poisson arrival rate (solves per second)")
     ap.add_argument("--sweeps-before", type=int, default=1,
                     help="sweep row: untimed split sweeps between the warm-up and the timed sweep")
     a = ap.parse_args()
@@ -699,12 +702,78 @@ def run_sweep(args):
     return 0
 
 
+def couplings(j2_over_j1, q_over_j1):
+    """The engine's (delta, qdelta) for a J1-J2-Q cylinder given as ratios: its
+    nearest-neighbour bond is delta + qdelta/2, its diagonal bond 1 - |qdelta|
+    and its plaquette term qdelta (up to the overall scale, which the ratios
+    do not fix)."""
+    r, q = float(j2_over_j1), float(q_over_j1)
+    qd = q / (r + q)
+    delta = (1.0 - qd) / r - qd / 2.0 if r > 0 else 1.0 / q - 0.5
+    return delta, qd
+
+
+def run_serve(args):
+    """Independent DMRG solves as requests (the survey's serving stream): seeded
+    Poisson arrivals at --rate; per request lx in {6, 8, 10, 12}, ly in {4, 6},
+    J2/J1 in U[0, 1], Q/J1 in U[0, 2], total spin 0 or 1, D in {128, 256, 512},
+    a warm-up and up to 4 sweeps in split mode.  The solves run one after
+    another on one GPU (no batching of concurrent solves): each request's
+    latency is its queueing on the arrival timeline plus its measured service
+    time.  A bounded sample of --requests solves; p99 of so few is their
+    maximum."""
+    import torch
+
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300.sweep import Dmrg
+    from su2dmrg_gb300.warmup import Lattice
+
+    capi.lib()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(42)
+    t_arrive = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
+    free_at, lat, reqs = 0.0, [], []
+    for k in range(args.requests):
+        lx, ly = int(rng.choice([6, 8, 10, 12])), int(rng.choice([4, 6]))
+        r, q = rng.uniform(0.0, 1.0), rng.uniform(0.0, 2.0)
+        spin, d = int(rng.integers(0, 2)), int(rng.choice([128, 256, 512]))
+        delta, qd = couplings(r, q)
+        lattice = Lattice.cylinder(lx, ly, delta, qd, d, totspin=2 * spin)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e, _ = Dmrg(lattice, mode=MODES["split"]).run_dmrg(4)
+        torch.cuda.synchronize()
+        service = time.perf_counter() - t0
+        start = max(free_at, t_arrive[k])
+        free_at = start + service
+        lat.append(free_at - t_arrive[k])
+        reqs.append({"lattice": f"{lx}x{ly}", "j2_over_j1": round(r, 4), "q_over_j1": round(q, 4), "spin": spin,
+                     "D": d, "sweeps": len(e) - 1, "energy_per_site": e[-1] / lattice.ns, "service_s": service})
+    span = free_at - t_arrive[0]
+    line = {"metric": "DMRG solves per second (serving stream, one GPU, solves in sequence)",
+            "value": args.requests / span, "unit": "solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 0,
+            "ms_per_step": 1e3 * float(np.mean([q["service_s"] for q in reqs])), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 emulated by bf16 x7 (fp32 accumulate); FP64 truncation and Lanczos scalars",
+            "data": "synthetic (seeded request stream, lattice tables built here)",
+            "config": {"workload": "serving stream: random J1-J2-Q cylinders, D in {128, 256, 512}, 4 sweeps",
+                       "row": "serve", "requests": reqs, "arrival_rate_per_s": args.rate, "seed": 42,
+                       "batching": "none (solves run in sequence)"},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(np.max(lat)), "sample": args.requests},
+            "cpu_baseline": None}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.row == "sweep":
         return run_sweep(args)
+    if args.row == "serve":
+        return run_serve(args)
     if args.row != "heff":
         return run_row(args)
     return run_su2g(args)
