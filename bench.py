@@ -374,16 +374,18 @@ def run_su2g(args):
         t_kernel = (prof[1] + prof[3]) / 1e3
         achieved = pairs * flops / t_kernel / 1e12
         # DRAM bytes of the two GEMM launches, measured with ncu (dram__bytes_read.sum +
-        # dram__bytes_write.sum) on the D=1000 case: 4.09 bytes per algorithmic byte of an
-        # application (FP64 operators + psi in/out); algorithmic bytes are computed here.
+        # dram__bytes_write.sum) on this D=2000 width-20 workload: 1.828e9 (phase 1) +
+        # 2.970e9 (phase 2) = 3.74 bytes per algorithmic byte of an application (FP64
+        # operators + psi in/out); other sizes are scaled by their algorithmic bytes.
         alg_bytes = 8.0 * (sum(x.numel() for (_s1, x1, _s2, x2, _c) in terms for x in (x1, x2))
                            + sum(h[1].numel() for h in (hl, hr) if h is not None) + 2 * w.psi.size())
-        traffic = 4.09 * alg_bytes / 2 if S == 7 else None
+        traffic = 3.737 * alg_bytes / 2 if S == 7 else None
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic,
-                "traffic_definition": "DRAM bytes per GEMM launch: ncu-measured 4.09 x algorithmic bytes per "
-                                      "application (D=1000 capture), scaled by this workload's algorithmic bytes "
-                                      f"({alg_bytes:.4g} B), halved over the two launches",
+                "traffic_definition": "DRAM bytes per GEMM launch: ncu-measured 3.737 x algorithmic bytes per "
+                                      "application (D=2000 width-20 capture: 1.828e9 + 2.970e9 B over the two "
+                                      f"launches), this workload's algorithmic bytes {alg_bytes:.4g} B, halved "
+                                      "over the two launches",
                 "kernel": f"ozaki_gemm<{S}> (tcgen05 BF16, {pairs} digit-pair products per FP64 product), "
                           "2 launches per step",
                 "achieved_definition": f"{pairs} x algorithmic FP64 FLOPs of the two GEMM launches / their time",
