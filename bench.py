@@ -223,32 +223,31 @@ def fp64_peak_tflops(torch):
 
 
 class CpuSample:
-    """Oracle (CPU restatement of the reference hot path, BLAS dgemm) on a
-    bounded sample of the workload: `nspin1_sample` of the spin-1 terms plus
-    the spin-0 terms at full D, all host cores."""
+    """The oracle (CPU restatement of the reference hot path: C loops over
+    the blocks, OpenBLAS dgemm, all host cores) applying the same synthetic
+    H_eff as the GPU arm, full width.  The workload is built by the oracle
+    itself (oracle.synthetic_heff draws the same numbers as the library's
+    generator), so nothing of the GPU library is loaded on this path."""
 
-    def __init__(self, D, nspin1_sample):
+    def __init__(self, D, nspin1):
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle as o
 
-        from su2dmrg_gb300.workloads import synthetic_heff
-
         self.o = o
+        o.build()
         self.cores = os.cpu_count() or 1
         o.set_blas_threads(self.cores)
-        w = synthetic_heff(D=D, nspin1=nspin1_sample, seed=1234)
-        self.w = w
-        self.prob = o.HeffProblem(w.psi, w.terms, w.hl, w.hr)
+        self.prob, self.psi = o.synthetic_heff(D=D, nspin1=nspin1, seed=1234)
         self.flops = o.heff_flops(self.prob)
-        self.desc = (f"{nspin1_sample} of 18 spin-1 terms + both spin-0 terms at D={D} "
-                     f"(oracle C restatement of the reference, OpenBLAS dgemm, {self.cores} threads)")
+        self.desc = (f"the full width-{nspin1 + 2} application ({nspin1} spin-1 terms + both spin-0 terms) "
+                     f"at D={D} (oracle C restatement of the reference, OpenBLAS dgemm, {self.cores} threads)")
 
     def step(self):
         t0 = time.perf_counter()
-        self.o.heff_apply(self.prob, self.w.psi_data)
+        self.o.heff_apply(self.prob, self.psi)
         return time.perf_counter() - t0
 
-    def measure(self, seconds=10.0, max_steps=20):
+    def measure(self, seconds=10.0, max_steps=30):
         self.step()  # warm
         ts = []
         t0 = time.perf_counter()
@@ -260,24 +259,25 @@ class CpuSample:
 
 
 def run_reference(args):
-    rank, world = 0, 1
-    if args.gpus > 1 and "RANK" in os.environ:
-        rank = int(os.environ["RANK"])
+    """The reference arm: the CPU restatement of the reference's hot path
+    (oracle/), on the GPU arm's workload and metric.  Only the oracle and
+    numpy/SciPy are loaded; rank 0 alone runs under torchrun."""
+    rank = int(os.environ.get("RANK", "0")) if args.gpus > 1 else 0
     if rank != 0:
         return 0
-    cs = CpuSample(args.D, 2)
+    cs = CpuSample(args.D, args.nspin1)
     for _ in range(args.warmup):
         cs.step()
     ts = [cs.step() for _ in range(args.steps)]
-    dt = float(np.median(ts))
-    v = cs.flops / dt / 1e12
+    total = float(np.sum(ts))
+    v = cs.flops * args.steps / total / 1e12
     cb = {"value": v, "unit": UNIT, "cores": cs.cores, "kind": "port",
-          "sample": f"each step = one application of {cs.desc}; median of {args.steps}"}
+          "sample": f"each step = one application of {cs.desc}; {args.steps} steps"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"synthetic SU(2) two-site H_eff, D={args.D}, width {args.nspin1 + 2}",
-                       "sample": cb["sample"]},
+                       "flops_per_step": cs.flops, "same_config": True},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -368,6 +368,8 @@ def run_su2g(args):
                 "launch_ms": prof,
                 "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 is not in MEASURED_PEAKS.json)"}
         accuracy = {"mode": "FP64", "rel_err_vs_fp64_path": 0.0}
+        fp64 = {"value": value, "unit": UNIT, "ms_per_step": ms_per_step, "steps": args.steps,
+                "path": "this line (mode f64)"}
     else:
         peak, src = bf16_peak()
         pairs = S * (S + 1) // 2
@@ -379,13 +381,15 @@ def run_su2g(args):
         # operators + psi in/out); other sizes are scaled by their algorithmic bytes.
         alg_bytes = 8.0 * (sum(x.numel() for (_s1, x1, _s2, x2, _c) in terms for x in (x1, x2))
                            + sum(h[1].numel() for h in (hl, hr) if h is not None) + 2 * w.psi.size())
-        traffic = 3.737 * alg_bytes / 2 if S == 7 else None
+        captured = args.D == 2000 and args.nspin1 == 18 and S == 7
+        traffic = 3.737 * alg_bytes / 2 if captured else None
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic,
                 "traffic_definition": "DRAM bytes per GEMM launch: ncu-measured 3.737 x algorithmic bytes per "
                                       "application (D=2000 width-20 capture: 1.828e9 + 2.970e9 B over the two "
                                       f"launches), this workload's algorithmic bytes {alg_bytes:.4g} B, halved "
-                                      "over the two launches",
+                                      "over the two launches; the digit-pack launches are not included; "
+                                      "null when the workload is not the captured one",
                 "kernel": f"ozaki_gemm<{S}> (tcgen05 BF16, {pairs} digit-pair products per FP64 product), "
                           "2 launches per step",
                 "achieved_definition": f"{pairs} x algorithmic FP64 FLOPs of the two GEMM launches / their time",
@@ -398,13 +402,29 @@ def run_su2g(args):
         plan.apply(psi, y, stream)
         torch.cuda.synchronize()
         rel = float((y - y64).norm() / y64.norm())
+        # the plain FP64 GPU path on the same workload (the other half of the
+        # split-vs-FP64 metric): a few applications, device time
+        for _ in range(2):
+            ref_plan.apply(psi, y64, stream)
+        torch.cuda.synchronize()
+        nf = max(3, min(args.steps, 10))
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(nf):
+            ref_plan.apply(psi, y64, stream)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        f64_ms = f0.elapsed_time(f1) / nf
+        fp64 = {"value": flops / (f64_ms / 1e3) / 1e12, "unit": UNIT, "ms_per_step": f64_ms, "steps": nf,
+                "path": "gemm_f64_tiles (FP64 DMMA), same plan inputs, device-resident",
+                "split_speedup": f64_ms / ms_per_step}
         ref_plan.close()
         accuracy = {"mode": f"BF16 x {S} slices", "rel_err_vs_fp64_path": rel,
                     "tolerance": 1e-12 if S == 7 else 1e-10}
         assert plan.status() == 0
     cb = None
     if not args.no_cpu_baseline:
-        cb = CpuSample(args.D, 2).measure(seconds=10.0)
+        cb = CpuSample(args.D, args.nspin1).measure(seconds=10.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -419,6 +439,7 @@ def run_su2g(args):
         "gpu_launches": plan.launches() * args.steps,
         "roofline": roof,
         "accuracy": accuracy,
+        "fp64": fp64,
         "cpu_baseline": cb,
         "clocks": clk.summary(),
     }
@@ -687,7 +708,7 @@ def run_sweep(args):
                        "earlier_sweep_seconds": before_s,
                        "warmup_energy_per_site": e_warm / lat.ns, "sweep_energy_per_site_split": e_split / lat.ns},
             "clocks": clk.summary(), "cpu_baseline": None,
-            "cpu_baseline_note": "the reference main_omp is not built on the GPU host (x86 build, sources absent)"}
+            "cpu_baseline_note": "the reference main_omp cannot run on the GPU host: its sources are not there"}
     if ref_state is not None:
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -112,6 +112,12 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
 /* Reads and clears the plan's device error word (the split-precision kernels
  * record a bounded wait that gave up there).  SU2G_ETIMEOUT if one did. */
 int su2g_heff_plan_status(su2g_heff_plan* plan, int* code);
+/* Test hook, no counterpart in the reference: stores a nonzero `code` in the
+ * plan's error word from the host, as a device wait that gave up would, so a
+ * test can check on the CPU side, without any device fault, that every later
+ * result of the plan (su2g_lanczos on each of its exits) is refused with
+ * SU2G_ETIMEOUT. */
+int su2g_heff_plan_mark_failed(su2g_heff_plan* plan, int code);
 /* flops: algorithmic FLOPs of one application; psi_len: packed length of psi
  * and y (doubles); scratch_bytes: device scratch held by the plan; ntiles:
  * output tiles of the two launch phases. */
@@ -165,9 +171,12 @@ int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_f
  * GPU that loads libsu2g.so until the process exits; terms that need more are
  * refused with SU2G_EINVAL.  The first call on a device looks up the arrays'
  * device addresses (cudaGetSymbolAddress), so make it before any stream
- * capture.  Calls share the arrays: calls that overlap on the GPU race and
- * must be serialised by the caller.  Same arguments and result as
- * su2g_hamiltonian_vector_multiplication, asynchronous on `stream`. */
+ * capture.  Calls share the arrays.  Calls from several host threads on the
+ * same stream are safe: each call queues its copies and launches under a
+ * per-device lock, so stream order keeps them apart.  Calls on different
+ * streams race on the arrays and must be serialised by the caller.  Same
+ * arguments and result as su2g_hamiltonian_vector_multiplication,
+ * asynchronous on `stream`. */
 #define SU2G_NOALLOC_SCRATCH_DOUBLES 4194304 /* intermediate blocks: 32 MiB */
 #define SU2G_NOALLOC_MAX_TILES 65536
 #define SU2G_NOALLOC_MAX_SEGS 65536

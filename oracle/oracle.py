@@ -974,3 +974,84 @@ def mea_enr(hl, hr, ww, pairs):
         if l is not None:
             num += c * ss_inner_prod(l[0], l[1], r[0], r[1])
     return num / float(np.sum(np.asarray(ww) ** 2))
+
+
+# --------------------------------------------------------------------------
+# the synthetic H_eff workload, built from the oracle alone
+# --------------------------------------------------------------------------
+def gaussian_sector_counts(total: int, max2j: int = 12, mean_j: float = 2.0, sd_j: float = 1.5):
+    """Multiplet counts per 2j in 0..max2j from a discretised Gaussian in j,
+    largest-remainder rounding to exactly `total`."""
+    j = np.arange(max2j + 1) / 2.0
+    w = np.exp(-0.5 * ((j - mean_j) / sd_j) ** 2)
+    raw = w / w.sum() * total
+    base = np.floor(raw).astype(int)
+    order = np.argsort(-(raw - base), kind="stable")
+    base[order[: total - base.sum()]] += 1
+    return base.tolist()
+
+
+def _symmetric_operator(st: Struct, rng, fac, ratio_side: bool) -> np.ndarray:
+    """Operator blocks (ja, s, jc) drawn for ja <= jc (N(0,1)/sqrt(rows),
+    diagonal blocks symmetrised); the mirror block (jc, s, ja) is the
+    transpose, times fac[ja,s,jc]/fac[jc,s,ja] on the right-hand operator, so
+    that the effective Hamiltonian is symmetric."""
+    off, total = st.offsets()
+    data = np.zeros(total)
+    where = {st.block_angm(i): i for i in range(st.nten) if st.flag[i]}
+    for (ja, s, jc), i in where.items():
+        if ja > jc:
+            continue
+        a, _, c = st.block_shape(i)
+        blk = rng.standard_normal((a, c)) / np.sqrt(a)
+        if ja == jc:
+            blk = 0.5 * (blk + blk.T)
+        data[off[i]: off[i] + a * c] = blk.ravel(order="F")
+        mirror = where.get((jc, s, ja))
+        if ja != jc and mirror is not None:
+            t = blk.T * (fac[ja, s, jc] / fac[jc, s, ja]) if ratio_side else blk.T
+            data[off[mirror]: off[mirror] + a * c] = np.ascontiguousarray(t).ravel(order="F")
+    return data
+
+
+def synthetic_heff(D: int = 2000, nspin1: int = 18, seed: int = 1234, max2j: int = 12):
+    """The seeded synthetic two-site H_eff of the D-multiplet benchmark shape
+    (bond sectors 2j = 0..max2j with Gaussian counts, enlarged legs bond x
+    spin-1/2, psi a normalised N(0,1) singlet, `nspin1` spin-1 operator pairs
+    and the two spin-0 block Hamiltonians), drawn from numpy's PCG64 in the
+    same order as the library's own generator, so both hold the same numbers.
+    Built with the oracle's structures and recoupling table only.  Returns
+    (HeffProblem, psi data)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = gaussian_sector_counts(D, max2j)
+    angm = [k for k in range(max2j + 1) if counts[k] > 0]
+    bond = Bond(1, angm, [counts[k] for k in angm])
+    enl = fuse(bond, Bond(1, [1], [1]))
+    psi = Struct([enl, enl], 0).with_legal_flags()
+    off, total = psi.offsets()
+    x = np.zeros(total)
+    for i in range(psi.nten):
+        if psi.flag[i]:
+            a, b = psi.block_shape(i)
+            x[off[i]: off[i] + a * b] = rng.standard_normal(a * b)
+    x /= np.linalg.norm(x)
+    fac = fac_hamilt_vec(MAX_ANGM)
+    spin = Bond(1, [2], [1])
+    inb = enl.inverted()
+    terms = []
+    for _ in range(nspin1):
+        s1 = Struct([inb, spin, enl], 0).with_legal_flags()
+        s2 = Struct([inb, spin, enl], 0).with_legal_flags()
+        x1 = _symmetric_operator(s1, rng, fac, ratio_side=False)
+        x2 = _symmetric_operator(s2, rng, fac, ratio_side=True)
+        terms.append((s1, x1, s2, x2, 1.0))
+    hs = Struct([inb, enl], 0).with_legal_flags()
+    hoff, htot = hs.offsets()
+    hx = [np.zeros(htot), np.zeros(htot)]
+    for side in range(2):
+        for i in range(hs.nten):
+            if hs.flag[i]:
+                a, c = hs.block_shape(i)
+                blk = rng.standard_normal((a, c)) / np.sqrt(a)
+                hx[side][hoff[i]: hoff[i] + a * c] = (0.5 * (blk + blk.T)).ravel(order="F")
+    return HeffProblem(psi, terms, (hs, hx[0], 1.0), (hs, hx[1], 1.0)), x

@@ -10,6 +10,8 @@
 #   oracle/_ref/libsu2ref_mea.so  the same with the engine's measurement
 #                              variant (dmrg_su2_omp_mea_enr.cpp) in place of
 #                              dmrg_su2_omp.cpp
+# The sources are read from $SU2REF_SRC, by default the read-only reference
+# checkout this recipe was written against.
 # Sources are copied to a scratch directory under /tmp and patched there; the
 # reference tree is never written and no reference source enters the repo.
 # BLAS/LAPACK come from SciPy's bundled OpenBLAS (blas_shim.c), the Fortran
@@ -20,7 +22,10 @@ REPO="$(cd "$HERE/../.." && pwd)"
 SRC="${SU2REF_SRC:-/root/reference}"
 OUT="$REPO/oracle/_ref"
 if [ ! -f "$SRC/tensor_su2.cpp" ]; then
-  echo "build_ref.sh: reference sources not found at $SRC" >&2
+  # --if-present: a machine without the reference sources (the GPU hosts)
+  # uses the committed fixtures instead; nothing to build there
+  if [ "${1:-}" = "--if-present" ]; then exit 0; fi
+  echo "build_ref.sh: reference sources not found at $SRC (set SU2REF_SRC)" >&2
   exit 2
 fi
 WORK="$(mktemp -d /tmp/su2ref.XXXXXX)"

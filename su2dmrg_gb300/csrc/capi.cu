@@ -155,8 +155,6 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   su2g::oz::OzWork& w = p->oz;
   cudaError_t e = cudaMalloc((void**)&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
   if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
   for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
     e = upload(w.jobs[c], &p->d_jobs[c]);
     if (e == cudaSuccess) {
@@ -283,6 +281,10 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
   const int64_t scratch_doubles = p->work.scratch_len + p->oz.partial_len;
   if (e == cudaSuccess && scratch_doubles > 0)
     e = cudaMalloc((void**)&p->d_scratch, scratch_doubles * sizeof(double));
+  // the error word: set by a bounded device wait that gave up, read by
+  // su2g_heff_plan_status and every result-returning caller of the plan
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
   if (e == cudaSuccess && S > 0) e = setup_split(p);
   if (e != cudaSuccess) {
     p->release();
@@ -509,6 +511,12 @@ int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
   SU2G_CUDA(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   SU2G_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
   if (*code) return fail(SU2G_ETIMEOUT, "a bounded device wait gave up (code " + std::to_string(*code) + ")");
+  return SU2G_OK;
+}
+
+int su2g_heff_plan_mark_failed(su2g_heff_plan* p, int code) {
+  if (!p || !p->d_err || code == 0) return fail(SU2G_EINVAL, "plan_mark_failed: bad arguments");
+  SU2G_CUDA(cudaMemcpy(p->d_err, &code, sizeof(int), cudaMemcpyHostToDevice));
   return SU2G_OK;
 }
 
@@ -901,11 +909,12 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
       if ((rc = L.combine(z0, m, psi))) return rc;
       double ee, ov;
       if ((rc = L.check(psi, &ee, &ov))) return rc;
-      if (std::fabs(ov - 1.) < 1.e-8) {
+      if (std::fabs(ov - 1.) < 1.e-8) {  // lanczos_su2.cpp:178-188
         *energy = eig[0];
         if (nmatvec) *nmatvec = L.nmatvec;
         SU2G_CUDA(cudaStreamSynchronize(L.st));
-        return SU2G_OK;
+        int code = 0;
+        return su2g_heff_plan_status(p, &code);
       }
     }
   }

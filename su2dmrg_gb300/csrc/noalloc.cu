@@ -14,9 +14,12 @@
 // the last call.  Nothing needs clearing between calls: the work list is
 // copied in whole, every intermediate element is written by exactly one tile
 // of the first launch before the second launch reads it, and every element of
-// y is written by exactly one tile of the second launch.  Calls whose work
-// overlaps on the GPU (two host threads, or two streams) race on the arrays;
-// serialise them.
+// y is written by exactly one tile of the second launch.  Each call holds a
+// per-device host lock from its first copy into the arrays until its second
+// launch is queued, so calls from several host threads on ONE stream queue
+// whole (copy, copy, launch, launch) groups one after the other and stream
+// order keeps them apart.  Calls on different streams (or devices' streams
+// that overlap) still race on the arrays; the caller serialises those.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -43,6 +46,8 @@ struct DeviceArrays {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 DeviceArrays g_dev[kMaxDevices];
+// held by a call from its first copy into a device's arrays to its last launch
+std::mutex g_call_mu[kMaxDevices];
 
 int fail(int code, const std::string& msg) { return su2g::set_last_error(code, msg); }
 
@@ -50,7 +55,7 @@ int fail(int code, const std::string& msg) { return su2g::set_last_error(code, m
 // host code their names are host-side stand-ins, not device addresses, so the
 // addresses are looked up once per device (with that device current) and
 // cached.
-int device_arrays(DeviceArrays* out) {
+int device_arrays(DeviceArrays* out, int* device) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(SU2G_ECUDA, std::string("noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
@@ -66,6 +71,7 @@ int device_arrays(DeviceArrays* out) {
     d.ready = true;
   }
   *out = d;
+  *device = dev;
   return SU2G_OK;
 }
 
@@ -95,7 +101,8 @@ extern "C" int su2g_hamiltonian_vector_multiplication_noalloc(const int* vec_des
                                  std::to_string(SU2G_NOALLOC_MAX_SEGS) +
                                  "; use su2g_hamiltonian_vector_multiplication");
   DeviceArrays d;
-  rc = device_arrays(&d);
+  int dev = 0;
+  rc = device_arrays(&d, &dev);
   if (rc) return rc;
   // one work list: phase-2 tiles index the segments after phase 1's
   std::vector<su2g::GemmTile> tiles(w.tile1);
@@ -106,6 +113,7 @@ extern "C" int su2g_hamiltonian_vector_multiplication_noalloc(const int* vec_des
   std::vector<su2g::GemmSeg> segs(w.seg1);
   segs.insert(segs.end(), w.seg2.begin(), w.seg2.end());
   cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> call_lock(g_call_mu[dev]);
   // pageable sources: each call returns once its bytes are staged, so the
   // vectors may go out of scope afterwards
   cudaError_t e = cudaSuccess;

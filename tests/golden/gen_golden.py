@@ -4,7 +4,7 @@ Runs only where the reference sources exist (they are compiled by
 oracle/ref/build_ref.sh into oracle/_ref/libsu2ref.so); the fixtures it writes
 are committed and are what the tests read on every other machine.
 
-    python oracle/ref/build_ref.sh && python tests/golden/gen_golden.py
+    bash oracle/ref/build_ref.sh && python tests/golden/gen_golden.py
 
 Fixtures:
   fac_hamilt_vec.npy   fac_hamilt_vec[25][25][25] (dmrg_su2.cpp:759-766)

@@ -77,6 +77,78 @@ def test_noalloc_matches_allocating_entry_point(su2lib, oracle):
         assert np.linalg.norm(got - ref) <= TOL * np.linalg.norm(ref)
 
 
+def test_noalloc_matches_reference_output(su2lib, oracle):
+    """Against the reference's own tensor_su2::hamiltonian_vector_multiplication
+    output stored with the fixture (rx), on two calls in a row."""
+    import torch
+
+    from su2dmrg_gb300 import capi
+
+    L = capi.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    g = np.load(sorted(glob.glob(os.path.join(GOLDEN, "heff_term_*.npz")))[3])
+    vs = oracle.struct_from_desc(g["vdesc"], g["vflag"])
+    s1 = oracle.struct_from_desc(g["d1"], g["f1"])
+    s2 = oracle.struct_from_desc(g["d2"], g["f2"])
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    ref = oracle.to_layout(oracle.struct_from_desc(g["vdesc"], g["rflag"]), g["rx"], vs)
+    vx, x1, x2 = dev(g["vx"]), dev(g["x1"]), dev(g["x2"])
+    for _ in range(2):
+        y = torch.full_like(vx, np.nan)
+        capi.check(_call(L.su2g_hamiltonian_vector_multiplication_noalloc, vs, vx, s1, x1, s2, x2, y, stream))
+        torch.cuda.synchronize()
+        got = y.cpu().numpy()
+        assert np.linalg.norm(got - ref) <= TOL * np.linalg.norm(ref)
+
+
+def test_noalloc_threads_sharing_one_stream(su2lib, oracle):
+    """Host threads that call the entry point on one shared stream (the
+    reference's OpenMP loop over terms, each thread applying its own term)
+    get their own results: every call queues its copies and launches as one
+    group, so stream order keeps the shared arrays apart."""
+    import threading
+
+    import torch
+
+    from su2dmrg_gb300 import capi
+
+    L = capi.lib()
+    stream = torch.cuda.Stream()
+    sid = stream.cuda_stream
+    cases = _cases(torch, oracle)
+    torch.cuda.synchronize()
+    refs = []
+    for (vs, vx, s1, x1, s2, x2) in cases:
+        y = torch.zeros_like(vx)
+        capi.check(_call(L.su2g_hamiltonian_vector_multiplication, vs, vx, s1, x1, s2, x2, y, sid))
+        refs.append(y)
+    stream.synchronize()
+    nthreads, rounds = 4, 6
+    outs = [[torch.full_like(cases[t % len(cases)][1], np.nan) for _ in range(rounds)] for t in range(nthreads)]
+    codes = [[None] * rounds for _ in range(nthreads)]
+    go = threading.Barrier(nthreads)
+
+    def work(t):
+        vs, vx, s1, x1, s2, x2 = cases[t % len(cases)]
+        go.wait()
+        for r in range(rounds):
+            codes[t][r] = _call(L.su2g_hamiltonian_vector_multiplication_noalloc, vs, vx, s1, x1, s2, x2,
+                                outs[t][r], sid)
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(nthreads)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    stream.synchronize()
+    for t in range(nthreads):
+        ref = refs[t % len(cases)].cpu().numpy()
+        for r in range(rounds):
+            assert codes[t][r] == capi.SU2G_OK
+            got = outs[t][r].cpu().numpy()
+            assert np.linalg.norm(got - ref) <= TOL * np.linalg.norm(ref)
+
+
 def test_noalloc_refuses_terms_beyond_its_arrays(su2lib):
     """A single D=2000 spin-1 term needs about 4.3M doubles of intermediate
     blocks, more than the fixed 4,194,304: refused before any device work."""
