@@ -75,6 +75,10 @@ def parse():
     ap.add_argument("--rate", type=float, default=0.1, help="serve row: Poisson arrival rate (solves per second)")
     ap.add_argument("--sweeps-before", type=int, default=1,
                     help="sweep row: untimed split sweeps between the warm-up and the timed sweep")
+    ap.add_argument("--converge", action="store_true",
+                    help="sweep row: split sweeps until one changes the energy by less than 1e-6 before the "
+                         "timed split and FP64 sweeps")
+    ap.add_argument("--max-sweeps", type=int, default=8, help="sweep row: at most this many sweeps with --converge")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = 250 if a.row == "heff" else 10
@@ -652,24 +656,91 @@ def run_row(args):
     return 0
 
 
+def _bond_dims(d):
+    """Per site, the structure descriptor of its MPS tensor (its bonds'
+    sectors and multiplet counts)."""
+    return [d.uu[i][0].desc().tolist() for i in range(d.lat.ns)]
+
+
+def _retained_compare(da, db, wa, wb):
+    """Retained multiplets of two sweeps' MPS, bond by bond: identical sector
+    by sector, or (where two runs settled on different truncations of the same
+    quality) the same total with discarded weights within 1e-10."""
+    def legs(desc):
+        out, p = [], 2
+        for _ in range(desc[0]):
+            n = desc[p + 1]
+            out.append((desc[p], desc[p + 2: p + 2 + n], desc[p + 2 + n: p + 2 + 2 * n]))
+            p += 2 + 2 * n
+        return out
+
+    same, moved, bad = 0, 0, []
+    for i, (a, b) in enumerate(zip(da, db)):
+        if a == b:
+            same += 1
+            continue
+        la, lb = legs(a), legs(b)
+        ok = [x[:2] for x in la] == [x[:2] for x in lb]
+        for x, y in zip(la, lb):
+            if ok and x[2] != y[2]:
+                ok = sum(x[2]) == sum(y[2]) and abs(wa.get(i, 0.0) - wb.get(i, 0.0)) <= 1e-10
+        if ok:
+            moved += 1
+        else:
+            bad.append(i)
+    return {"sites_identical": same, "sites_same_totals_weights_within_1e-10": moved, "sites_differing": bad}
+
+
+def _discarded_by_site(d, first):
+    from su2dmrg_gb300.warmup import discarded_weight
+
+    out = {}
+    for il, ir, kept, w in d.truncations[first:]:
+        out[il] = out[ir] = discarded_weight(kept, w)
+    return out
+
+
+def _svd_trace_summary(path, first_line):
+    """Totals of the truncation trace lines written since first_line."""
+    try:
+        with open(path) as f:
+            lines = f.readlines()[first_line:]
+    except OSError:
+        return None, first_line
+    recs = [json.loads(x) for x in lines if x.strip()]
+    lev = [len(s["levels"]) for r in recs for s in r["sectors"]]
+    out = {"calls": len(recs), "seconds": sum(r["ms"] for r in recs) / 1e3,
+           "calls_refining_everything": sum(1 for r in recs if r["lam_cut"] == 0.0),
+           "max_levels": max(lev) if lev else 0, "mean_levels": float(np.mean(lev)) if lev else 0.0,
+           "slowest_call_ms": max((r["ms"] for r in recs), default=0.0)}
+    return out, first_line + len(lines)
+
+
 def run_sweep(args):
-    """One DMRG sweep (dmrg_su2::sweep) of an lx x ly J1-J2 cylinder at D
-    multiplets, every tensor on the device: the warm-up (do_idmrg) and
-    --sweeps-before sweeps in split mode, then the next sweep from that state
-    twice, with split-precision and with FP64 contractions (truncation,
-    Lanczos scalars and the tridiagonal problem are FP64 in both).  The first
-    sweep after the warm-up is not a comparison point: the warm-up's basis
-    holds rounding-noise Schmidt directions (every value above 1e-100 of the
-    largest is kept), the engine's own first sweep passes through energies far
-    below the ground state before it recovers, and two runs differing by
-    rounding follow different paths there.  Wall-clock seconds with the
-    device synchronised on both sides (every library call blocks)."""
+    """DMRG sweeps (dmrg_su2::sweep) of an lx x ly J1-J2(-Q) cylinder at D
+    multiplets, every tensor on the device.  The warm-up (do_idmrg), then
+    split-precision sweeps: --sweeps-before of them, or with --converge until
+    a sweep changes the energy by less than 1e-6 (main_omp's rule, at most
+    --max-sweeps).  From that state the next sweep runs twice, with
+    split-precision and with FP64 contractions (truncation, Lanczos scalars and
+    the tridiagonal problem are FP64 in both), and the two are compared step
+    by step (energies) and bond by bond (retained multiplets).  The first sweep
+    after the warm-up is no comparison point: the warm-up's basis holds
+    rounding-noise Schmidt directions and the engine's own first sweep passes
+    through energies far below the ground state.  Wall-clock seconds with the
+    device synchronised on both sides (every library call blocks); per-phase
+    seconds of each timed sweep; the truncation's own trace (SU2G_SVD_TRACE)."""
     import torch
 
     from su2dmrg_gb300 import capi
     from su2dmrg_gb300.sweep import Dmrg
     from su2dmrg_gb300.warmup import Lattice
 
+    trace = os.environ.get("SU2G_SVD_TRACE") or os.path.join(REPO, "gpurun_out", "svd_trace.jsonl")
+    os.makedirs(os.path.dirname(trace), exist_ok=True)
+    open(trace, "w").close()
+    os.environ["SU2G_SVD_TRACE"] = trace
+    tline = 0
     capi.lib()
     torch.cuda.set_device(0)
     lx, ly = (int(v) for v in args.lattice.lower().split("x"))
@@ -678,23 +749,39 @@ def run_sweep(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = Dmrg(lat, mode=split)
-    e_warm = d.run()
+    e_prev = d.run()
     torch.cuda.synchronize()
     warm_s = time.perf_counter() - t0
-    before_s = []
-    for _ in range(args.sweeps_before):
+    e_warm = e_prev
+    _, tline = _svd_trace_summary(trace, tline)
+    before = []
+    nmax = args.max_sweeps if args.converge else args.sweeps_before
+    for k in range(nmax):
+        d.phase_seconds.clear()
         t0 = time.perf_counter()
-        d.sweep()
+        e = d.sweep()
         torch.cuda.synchronize()
-        before_s.append(time.perf_counter() - t0)
+        dt = time.perf_counter() - t0
+        tsum, tline = _svd_trace_summary(trace, tline)
+        before.append({"seconds": dt, "energy_per_site": e / lat.ns, "delta_e": e - e_prev,
+                       "phase_seconds": dict(d.phase_seconds), "truncation_trace": tsum,
+                       "peak_hbm_gb": torch.cuda.max_memory_allocated() / 1e9})
+        print(json.dumps({"progress": "sweep", **before[-1]}), file=sys.stderr, flush=True)
+        converged = abs(e - e_prev) < 1e-6
+        e_prev = e
+        if args.converge and converged:
+            break
     nwarm = len(d.energies)
+    ntr = len(d.truncations)
     ref_state = None if args.skip_fp64 else d.clone(MODES["f64"])
     torch.cuda.synchronize()
+    d.phase_seconds.clear()
     with ClockSampler(torch.cuda.current_device()) as clk:
         t0 = time.perf_counter()
         e_split = d.sweep()
         torch.cuda.synchronize()
         split_s = time.perf_counter() - t0
+    tsum_split, tline = _svd_trace_summary(trace, tline)
     steps_split = np.array([e for _, _, e in d.energies[nwarm:]])
     line = {"metric": f"DMRG sweep seconds, {lx}x{ly} J1-J2 cylinder (delta {args.delta}, Q {args.qdelta}), "
                       f"D={args.D}, split-precision contractions",
@@ -702,11 +789,13 @@ def run_sweep(args):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 emulated by bf16 x7 (fp32 accumulate); FP64 truncation and Lanczos scalars",
             "data": "synthetic (lattice tables built here; the uniform warm-up start, as the engine)",
-            "config": {"workload": f"{lx}x{ly} cylinder, boundary 2, D={args.D}, sweep {args.sweeps_before + 1} "
+            "config": {"workload": f"{lx}x{ly} cylinder, boundary 2, D={args.D}, sweep {len(before) + 1} "
                                    f"after the warm-up",
                        "row": "sweep", "two_site_steps": len(steps_split), "warmup_seconds": warm_s,
-                       "earlier_sweep_seconds": before_s,
-                       "warmup_energy_per_site": e_warm / lat.ns, "sweep_energy_per_site_split": e_split / lat.ns},
+                       "warmup_energy_per_site": e_warm / lat.ns, "earlier_sweeps": before,
+                       "converged_before_timed_sweep": bool(before and abs(before[-1]["delta_e"]) < 1e-6),
+                       "sweep_energy_per_site_split": e_split / lat.ns,
+                       "phase_seconds_split": dict(d.phase_seconds), "truncation_trace_split": tsum_split},
             "clocks": clk.summary(), "cpu_baseline": None,
             "cpu_baseline_note": "the reference main_omp cannot run on the GPU host: its sources are not there"}
     if ref_state is not None:
@@ -715,12 +804,19 @@ def run_sweep(args):
         e_f64 = ref_state.sweep()
         torch.cuda.synchronize()
         f64_s = time.perf_counter() - t0
+        tsum_f64, tline = _svd_trace_summary(trace, tline)
         steps_f64 = np.array([e for _, _, e in ref_state.energies[nwarm:]])
         rel = np.abs(steps_split - steps_f64) / np.abs(steps_f64)
         line["config"].update({"fp64_sweep_seconds": f64_s, "split_speedup_vs_fp64": f64_s / split_s,
+                               "phase_seconds_fp64": dict(ref_state.phase_seconds),
+                               "truncation_trace_fp64": tsum_f64,
                                "sweep_energy_per_site_fp64": e_f64 / lat.ns,
                                "max_rel_step_energy_diff_split_vs_fp64": float(rel.max()),
-                               "final_rel_energy_diff_split_vs_fp64": float(abs(e_split - e_f64) / abs(e_f64))})
+                               "final_rel_energy_diff_split_vs_fp64": float(abs(e_split - e_f64) / abs(e_f64)),
+                               "retained_multiplets_split_vs_fp64": _retained_compare(
+                                   _bond_dims(d), _bond_dims(ref_state), _discarded_by_site(d, ntr),
+                                   _discarded_by_site(ref_state, ntr))})
+    line["config"]["peak_hbm_gb"] = torch.cuda.max_memory_allocated() / 1e9
     print(json.dumps(line))
     return 0
 

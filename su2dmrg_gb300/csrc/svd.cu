@@ -21,7 +21,10 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <functional>
 #include <map>
 #include <memory>
@@ -233,6 +236,9 @@ struct Sector {
 struct SectorEig {
   bool tall = true;
   int k = 0;
+  // trace: host wall time of the two passes, refinement subspace sizes
+  double ms_eig = 0, ms_finish = 0;
+  std::vector<int> levels;
   double* G = nullptr;   // eigenvectors (k x k)
   double* A0 = nullptr;  // the Gram matrix
   std::vector<double> w;  // eigenvalues, ascending
@@ -279,6 +285,7 @@ void sector_finish(Ctx& c, const double* blk, int m, int n, double p1, double p2
     np = k;
     std::vector<double> ws;
     do {
+      e.levels.push_back(npp);
       c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, npp, np, np, vp, np, ap, np, app, npp);
       c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, npp, npp, np, app, npp, vp, np, vpp, npp);
       c.copy(ap, vpp, (int64_t)npp * npp);
@@ -371,6 +378,12 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   P.set_layout(psi_flag);
   if (P.total > 0 && !psi) return fail(SU2G_EINVAL, "svd: null psi");
   cudaStream_t cst = (cudaStream_t)stream;
+  // SU2G_SVD_TRACE=<file>: one JSON line per call appended there (per sector:
+  // m, n, Gram size, host milliseconds of the two passes, the sizes of the
+  // refinement subspaces), for time breakdowns of whole sweeps
+  const char* trace = std::getenv("SU2G_SVD_TRACE");
+  if (trace && !*trace) trace = nullptr;
+  const auto t_call = std::chrono::steady_clock::now();
   const int n0 = P.legs[0].n(), n1 = P.legs[1].n();
   // sectors in the reference's loop order: leg-0 sector, then the leg-1 sector of equal spin
   struct Job {
@@ -416,7 +429,7 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   // eigendecompositions, then (with the global cut known) the refinements
   // and the factors
   std::vector<SectorEig> eig(jobs.size());
-  double lam_cut = 0.0;
+  double lam_cut = 0.0, lam_cut_raw = 0.0, noise_floor = 0.0;
   auto on_threads = [&](auto&& body) {
     std::vector<std::thread> threads;
     for (size_t q = 1; q < jobs.size(); ++q) threads.emplace_back(body, q);
@@ -426,7 +439,9 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   on_threads([&](size_t q) {
     Ctx& c = *ctx[q];
     if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
+    const auto t0 = std::chrono::steady_clock::now();
     if (c.ok()) sector_eig(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, &eig[q]);
+    eig[q].ms_eig = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   });
   {  // the max_dcut-th largest eigenvalue over all sectors; 0 (refine every
      // subspace, as the reference) when nothing is cut or when the cut lies
@@ -442,18 +457,22 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
     }
     if (max_dcut > 0 && (int64_t)all.size() > max_dcut) {
       std::nth_element(all.begin(), all.begin() + (max_dcut - 1), all.end(), std::greater<double>());
-      lam_cut = all[max_dcut - 1];
+      lam_cut = lam_cut_raw = all[max_dcut - 1];
       if (lam_cut < 1e3 * floor) lam_cut = 0.0;
     }
+    noise_floor = floor;
   }
   on_threads([&](size_t q) {
     Ctx& c = *ctx[q];
     if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
+    const auto t0 = std::chrono::steady_clock::now();
     if (c.ok()) {
       secs[q].i = jobs[q].i;
       sector_finish(c, psi + P.offset[jobs[q].b], jobs[q].m, jobs[q].n, p1, p2, max_dcut, lam_cut, eig[q],
                     &secs[q]);
     }
+    if (trace) cudaStreamSynchronize(c.st);
+    eig[q].ms_finish = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     const cudaError_t e = cudaEventRecord(res.lanes[q].done, c.st);
     if (e != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
   });
@@ -539,5 +558,24 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   }
   ce = cudaStreamSynchronize(cst);
   if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
+  if (trace) {
+    static std::mutex trace_mu;
+    std::lock_guard<std::mutex> tl(trace_mu);
+    if (FILE* f = std::fopen(trace, "a")) {
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
+      std::fprintf(f,
+                   "{\"ms\": %.3f, \"max_dcut\": %d, \"lam_cut\": %.6e, \"lam_cut_raw\": %.6e, "
+                   "\"noise_floor\": %.6e, \"kept\": %d, \"sectors\": [",
+                   ms, max_dcut, lam_cut, lam_cut_raw, noise_floor, total_kept);
+      for (size_t q = 0; q < jobs.size(); ++q) {
+        std::fprintf(f, "%s{\"m\": %d, \"n\": %d, \"k\": %d, \"ms_eig\": %.3f, \"ms_finish\": %.3f, \"levels\": [",
+                     q ? ", " : "", jobs[q].m, jobs[q].n, eig[q].k, eig[q].ms_eig, eig[q].ms_finish);
+        for (size_t l = 0; l < eig[q].levels.size(); ++l) std::fprintf(f, "%s%d", l ? ", " : "", eig[q].levels[l]);
+        std::fprintf(f, "]}");
+      }
+      std::fprintf(f, "]}\n");
+      std::fclose(f);
+    }
+  }
   return SU2G_OK;
 }

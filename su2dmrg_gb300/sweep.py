@@ -49,26 +49,47 @@ class Dmrg(Warmup):
         d.ww = self.ww
         return d
 
+    def _timed(self, phase: str, t0: float) -> float:
+        """Adds the wall time since t0 to phase_seconds[phase] (every library
+        call blocks, so this is the phase's device and host time)."""
+        t1 = time.perf_counter()
+        self.phase_seconds[phase] = self.phase_seconds.get(phase, 0.0) + (t1 - t0)
+        return t1
+
+    @property
+    def phase_seconds(self) -> dict:
+        if not hasattr(self, "_phase_seconds"):
+            self._phase_seconds = {}
+        return self._phase_seconds
+
     def _vectran(self, i: int, flag: int) -> None:
         """wavefunc_transformation(i, flag): right2left_vectran (0) or
         left2right_vectran (1) of uu[i]."""
+        t0 = time.perf_counter()
         s, y = S.vectran(*self.uu[i], flag)
         self.uu[i] = (s, y[: s.size()])
+        self._timed("vectran", t0)
 
     def _step(self, il: int, ir: int, p1: float, p2: float) -> float:
         L = self.lat
+        t = time.perf_counter()
         vs, vx = S.prepare_input_vector(*self.uu[il], *self.uu[ir], mode=self.mode)
         vx = vx[: vs.size()]
+        t = self._timed("input_vector", t)
         self.site_left(il, S.fuse_tensor(*self._legs01(self.uu[il])))
         self.site_right(ir, S.fuse_tensor(*self._legs01(self.uu[ir])))
+        t = self._timed("site_update_centre", t)
         plan = self.heff_plan(il, ir, vs)
+        t = self._timed("heff_plan", t)
         n = vs.size()
         e, _ = plan.lanczos(vx, mlanc=self.mlanc if self.mlanc <= n else n + 1)
         plan.close()
         self._keep.clear()
+        t = self._timed("lanczos", t)
         self.energies.append((il, ir, e))
         tu, xu, tv, xv, w = S.svd(vs, vx, self.uu[il][0], p1, self.uu[ir][0], p2, L.max_dcut)
         self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
+        self._timed("truncation", t)
         self.ww = w
         self.truncations.append((il, ir, int(sum(tu.bonds[2].dim)), np.asarray(w)))
         return e
@@ -78,15 +99,21 @@ class Dmrg(Warmup):
         ns, nf = self.lat.ns, self.nfree
         for i in range(ns // 2, nf + 1, -1):        # centre -> left end
             self._vectran(i - 1, 1)
+            t = time.perf_counter()
             self.site_right(i, self.uu[i], release=True)
+            self._timed("site_update", t)
             self._step(i - 2, i - 1, *((1.0, 0.0) if i > nf + 2 else (0.0, 1.0)))
         for i in range(nf, ns - nf - 2):             # left end -> right end
             self._vectran(i + 1, 0)
+            t = time.perf_counter()
             self.site_left(i, self.uu[i], release=True)
+            self._timed("site_update", t)
             self._step(i + 1, i + 2, *((0.0, 1.0) if i < ns - nf - 3 else (1.0, 0.0)))
         for i in range(ns - nf - 1, ns // 2, -1):   # right end -> centre
             self._vectran(i - 1, 1)
+            t = time.perf_counter()
             self.site_right(i, self.uu[i], release=True)
+            self._timed("site_update", t)
             self._step(i - 2, i - 1, 1.0, 0.0)
         return self.energies[-1][2]
 

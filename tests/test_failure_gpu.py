@@ -46,8 +46,8 @@ def test_lanczos_refuses_result_on_every_exit(su2lib, mode):
     four steps (lanczos_su2.cpp:178-188) and the final step (:189-194).  The
     error word is set from the host (su2g_heff_plan_mark_failed), so no device
     wait has to give up; an unmarked run from the same start vector shows
-    which exit the solve takes (5 matvecs = the check at step 4, 6 = the
-    final step)."""
+    which exit the solve takes (5 matvecs = the check at step 4 ends the
+    solve; 7 = that check fails, then the final step and its check)."""
     import torch
 
     from su2dmrg_gb300 import capi
@@ -67,7 +67,7 @@ def test_lanczos_refuses_result_on_every_exit(su2lib, mode):
         if nmv == 5:
             break
     assert nmv == 5
-    for start, want_nmv in ((conv, 5), (fresh, 6)):
+    for start, want_nmv in ((conv, 5), (fresh, 7)):
         v = start.clone()
         e, nmv = plan.lanczos(v, mlanc=5)
         assert nmv == want_nmv
