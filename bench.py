@@ -71,8 +71,11 @@ def parse():
                     help="sweep row: nearest-neighbour coupling (diagonal 1 - |qdelta|; 2.0 = J2/J1 0.5)")
     ap.add_argument("--qdelta", type=float, default=0.0, help="sweep row: plaquette coupling Q")
     ap.add_argument("--skip-fp64", action="store_true", help="sweep row: time the split sweep only")
-    ap.add_argument("--requests", type=int, default=6, help="serve row: requests in the sample")
-    ap.add_argument("--rate", type=float, default=0.1, help="serve row: Poisson arrival rate (solves per second)")
+    ap.add_argument("--requests", type=int, default=32, help="serve row: requests of the stream served")
+    ap.add_argument("--rate", type=float, default=2.0, help="serve row: Poisson arrival rate (solves per second)")
+    ap.add_argument("--slots", type=int, default=8, help="serve row: solves in flight at most")
+    ap.add_argument("--seq-requests", type=int, default=8,
+                    help="serve row: the first requests of the stream also run one after another")
     ap.add_argument("--sweeps-before", type=int, default=1,
                     help="sweep row: untimed split sweeps between the warm-up and the timed sweep")
     ap.add_argument("--converge", action="store_true",
@@ -821,66 +824,77 @@ def run_sweep(args):
     return 0
 
 
-def couplings(j2_over_j1, q_over_j1):
-    """The engine's (delta, qdelta) for a J1-J2-Q cylinder given as ratios: its
-    nearest-neighbour bond is delta + qdelta/2, its diagonal bond 1 - |qdelta|
-    and its plaquette term qdelta (up to the overall scale, which the ratios
-    do not fix)."""
-    r, q = float(j2_over_j1), float(q_over_j1)
-    qd = q / (r + q)
-    delta = (1.0 - qd) / r - qd / 2.0 if r > 0 else 1.0 / q - 0.5
-    return delta, qd
-
-
 def run_serve(args):
-    """Independent DMRG solves as requests (the survey's serving stream): seeded
-    Poisson arrivals at --rate; per request lx in {6, 8, 10, 12}, ly in {4, 6},
-    J2/J1 in U[0, 1], Q/J1 in U[0, 2], total spin 0 or 1, D in {128, 256, 512},
-    a warm-up and up to 4 sweeps in split mode.  The solves run one after
-    another on one GPU (no batching of concurrent solves): each request's
-    latency is its queueing on the arrival timeline plus its measured service
-    time.  A bounded sample of --requests solves; p99 of so few is their
-    maximum."""
+    """The serving stream (su2dmrg_gb300.serve.request_stream: seeded Poisson
+    arrivals at --rate; per request lx in {6, 8, 10, 12}, ly in {4, 6}, J2/J1 in
+    U[0, 1], Q/J1 in U[0, 2], total spin 0 or 1, D in {128, 256, 512}; the
+    warm-up and up to 4 sweeps in split mode) served with continuous batching
+    (su2dmrg_gb300.serve.Server: --slots solves in flight, admission by
+    device footprint, Lanczos solves in shared launches), then the first
+    --seq-requests of the same requests one after another on the plain
+    per-solve path; their results must be identical.  Wall-clock seconds on
+    the host, every library call blocking."""
+    import copy
+
     import torch
 
     from su2dmrg_gb300 import capi
-    from su2dmrg_gb300.sweep import Dmrg
-    from su2dmrg_gb300.warmup import Lattice
+    from su2dmrg_gb300.serve import Server, request_stream
 
     capi.lib()
     torch.cuda.set_device(0)
-    rng = np.random.default_rng(42)
-    t_arrive = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
-    free_at, lat, reqs = 0.0, [], []
-    for k in range(args.requests):
-        lx, ly = int(rng.choice([6, 8, 10, 12])), int(rng.choice([4, 6]))
-        r, q = rng.uniform(0.0, 1.0), rng.uniform(0.0, 2.0)
-        spin, d = int(rng.integers(0, 2)), int(rng.choice([128, 256, 512]))
-        delta, qd = couplings(r, q)
-        lattice = Lattice.cylinder(lx, ly, delta, qd, d, totspin=2 * spin)
+    reqs = request_stream(args.requests, args.rate, seed=42)
+    srv = Server(slots=args.slots, mode=MODES["split"], batch=True)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        res = srv.run(reqs)
         torch.cuda.synchronize()
+    lat = np.array([r.latency for r in res])
+    span = max(r.t_done for r in res) - min(r.t_arrive for r in res)
+    recs = []
+    for r in res:
+        e = r.energies
+        de = abs(e[-1] - e[-2]) if len(e) > 1 else None
+        recs.append({**r.meta, "sweeps": len(e) - 1, "energy_per_site": e[-1] / reqs[r.rid].lattice.ns,
+                     "last_delta_e": de, "converged": de is not None and de < 1e-6,
+                     "arrive_s": r.t_arrive, "admit_s": r.t_admit, "done_s": r.t_done,
+                     "service_s": r.service, "latency_s": r.latency, "footprint_gb": r.footprint / 1e9})
+    seq = None
+    k = min(args.seq_requests, len(reqs))
+    if k > 0:
+        sub = [copy.copy(r) for r in reqs[:k]]
+        for r in sub:
+            r.arrival = 0.0
+        s1 = Server(slots=1, mode=MODES["split"], batch=False)
         t0 = time.perf_counter()
-        e, _ = Dmrg(lattice, mode=MODES["split"]).run_dmrg(4)
+        res1 = s1.run(sub)
         torch.cuda.synchronize()
-        service = time.perf_counter() - t0
-        start = max(free_at, t_arrive[k])
-        free_at = start + service
-        lat.append(free_at - t_arrive[k])
-        reqs.append({"lattice": f"{lx}x{ly}", "j2_over_j1": round(r, 4), "q_over_j1": round(q, 4), "spin": spin,
-                     "D": d, "sweeps": len(e) - 1, "energy_per_site": e[-1] / lattice.ns, "service_s": service})
-    span = free_at - t_arrive[0]
-    line = {"metric": "DMRG solves per second (serving stream, one GPU, solves in sequence)",
-            "value": args.requests / span, "unit": "solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 0,
-            "ms_per_step": 1e3 * float(np.mean([q["service_s"] for q in reqs])), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+        total1 = time.perf_counter() - t0
+        same = all(a.energies == b.energies and a.mps_desc == b.mps_desc for a, b in zip(res1, res[:k]))
+        seq = {"requests": k, "seconds": total1, "solves_per_s": k / total1,
+               "mean_service_s": float(np.mean([r.service for r in res1])),
+               "results_identical_to_batched": bool(same)}
+    line = {"metric": "DMRG solves per second (serving stream, one GPU, continuous batching)",
+            "value": len(res) / span, "unit": "solves/s", "n_gpus": 1, "steps": len(res), "warmup": 0,
+            "ms_per_step": 1e3 * span / len(res), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
             "dtype": "f64 emulated by bf16 x7 (fp32 accumulate); FP64 truncation and Lanczos scalars",
             "data": "synthetic (seeded request stream, lattice tables built here)",
-            "config": {"workload": "serving stream: random J1-J2-Q cylinders, D in {128, 256, 512}, 4 sweeps",
-                       "row": "serve", "requests": reqs, "arrival_rate_per_s": args.rate, "seed": 42,
-                       "batching": "none (solves run in sequence)"},
+            "config": {"workload": f"serving stream of {len(res)} requests: random J1-J2-Q cylinders, "
+                                   "D in {128, 256, 512}, up to 4 sweeps", "row": "serve",
+                       "arrival_rate_per_s": args.rate, "seed": 42, "slots": args.slots,
+                       "batching": "Lanczos solves of concurrent requests in shared launches",
+                       "max_in_flight": srv.max_inflight, "max_reserved_gb": srv.max_reserved / 1e9,
+                       "hbm_budget_gb": srv.budget / 1e9,
+                       "lanczos_batches": len(srv.batch_sizes),
+                       "mean_lanczos_batch": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
+                       "requests": recs},
+            "throughput": {"arrival_span_per_s": len(res) / span,
+                           "note": "requests / (last completion - first arrival); equals the arrival rate "
+                                   "unless the server saturates"},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                          "max": float(np.max(lat)), "sample": args.requests},
-            "cpu_baseline": None}
+                          "max": float(lat.max()), "sample": len(res)},
+            "sequential": seq, "clocks": clk.summary(), "cpu_baseline": None}
     print(json.dumps(line))
     return 0
 

@@ -161,6 +161,38 @@ int su2g_operator_combine(int n, const su2g_tensor* ops, const double* coef, dou
 int su2g_hamiltonian_vector_multiplication(const int* vec_desc, const int* vec_flag, const double* vec,
                                            su2g_tensor op1, su2g_tensor op2, double* y, void* stream);
 
+/* ------------------------------------------ several plans, shared launches */
+/* Independent solves that share the GPU (a serving loop) reach their Lanczos
+ * solves at the same time.  A batch applies several H_eff plans (one
+ * precision mode) in shared launches: their work lists are concatenated and
+ * their tiles dealt together over the persistent grid, so one application of
+ * all of them costs the launches of one plan.  Each plan's result is
+ * bit-identical to its own su2g_heff_apply.  No counterpart in the reference,
+ * whose solves are separate processes; per plan this is
+ * dmrg_su2::hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664).
+ * The plans must outlive the batch and must not change (no new projectors)
+ * while it exists. */
+typedef struct su2g_heff_batch su2g_heff_batch;
+int su2g_heff_batch_create(su2g_heff_plan* const* plans, int n, su2g_heff_batch** batch);
+int su2g_heff_batch_destroy(su2g_heff_batch* batch);
+/* total_len: sum of the plans' psi lengths; plan i's vector lies at the sum
+ * of the lengths of plans 0..i-1 in the batch vectors */
+int su2g_heff_batch_info(const su2g_heff_batch* batch, int64_t* total_len, int* nplans);
+/* y = H x for every plan on its slice of the batch vectors x and y (device,
+ * total_len doubles each); asynchronous on `stream` */
+int su2g_heff_batch_apply(su2g_heff_batch* batch, const double* x, double* y, void* stream);
+/* reads and clears the batch's error word (SU2G_ETIMEOUT: a bounded wait of a
+ * shared split-GEMM launch gave up; every plan's result is then suspect) */
+int su2g_heff_batch_status(su2g_heff_batch* batch);
+/* lanczos_su2::lanczos1 (lanczos_su2.cpp:125-195) for every plan of the
+ * batch in lockstep: psi[i] (device, plan i's layout) is the start vector and
+ * receives the eigenvector; energy[i] and nmatvec[i] as su2g_lanczos returns
+ * them, bit for bit (the same kernels in the same order per plan, each plan's
+ * exits decided as there); the matvecs of all solves at a step share one set
+ * of launches.  Blocks until done; SU2G_ETIMEOUT refuses every result. */
+int su2g_heff_batch_lanczos(su2g_heff_batch* batch, double* const* psi, int mlanc, double* energy, int* nmatvec,
+                            void* stream);
+
 /* Allocation-free form of su2g_hamiltonian_vector_multiplication, for callers
  * that may not allocate device memory when they apply a term: engines that
  * reserve their whole HBM budget up front, per-term calls from many host

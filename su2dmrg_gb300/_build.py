@@ -19,7 +19,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["capi.cu", "kernels_f64.cu", "ozaki_pack.cu", "ozaki_gemm.cu", "noalloc.cu", "svd.cu", "combine.cu", "wavefunc.cu", "measure.cu"]
+CU_SOURCES = ["capi.cu", "devmem.cu", "heff_batch.cu", "kernels_f64.cu", "ozaki_pack.cu", "ozaki_gemm.cu", "noalloc.cu", "svd.cu", "combine.cu", "wavefunc.cu", "measure.cu"]
 CXX_SOURCES = ["su2_meta.cpp", "heff_plan.cpp", "ozaki_plan.cpp", "env_plan.cpp", "checkpoint.cpp"]
 LINK_LIBS = ["-lcudart", "-lcublas", "-lcusolver", "-lpthread"]
 

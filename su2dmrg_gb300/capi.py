@@ -73,6 +73,12 @@ _PROTOS = {
     "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp, _vp]),
     "su2g_heff_plan_status": (_i, [_vp, _vp]),
     "su2g_heff_plan_mark_failed": (_i, [_vp, _i]),
+    "su2g_heff_batch_create": (_i, [_vp, _i, _vp]),
+    "su2g_heff_batch_destroy": (_i, [_vp]),
+    "su2g_heff_batch_info": (_i, [_vp, _vp, _vp]),
+    "su2g_heff_batch_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "su2g_heff_batch_status": (_i, [_vp]),
+    "su2g_heff_batch_lanczos": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
     "su2g_selftest_bounded_wait": (_i, [ctypes.c_longlong, _vp]),
     "su2g_heff_plan_info": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "su2g_heff_apply": (_i, [_vp, _vp, _vp, _vp]),

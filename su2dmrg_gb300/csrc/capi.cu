@@ -11,6 +11,7 @@
 #include "heff_plan.hpp"
 #include "kernels.hpp"
 #include "ozaki_plan.hpp"
+#include "plan_internal.hpp"
 #include "su2_meta.hpp"
 #include "su2g.h"
 #include "tridiag.hpp"
@@ -36,101 +37,17 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 template <class T>
 cudaError_t upload(const std::vector<T>& v, T** dptr) {
-  *dptr = nullptr;
-  if (v.empty()) return cudaSuccess;
-  cudaError_t e = cudaMalloc((void**)dptr, v.size() * sizeof(T));
-  if (e != cudaSuccess) return e;
-  return cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return su2g::upload_bytes(v.data(), v.size() * sizeof(T), (void**)dptr);
+}
+
+template <class T>
+cudaError_t dalloc(T** dptr, size_t bytes) {
+  return su2g::dev_alloc((void**)dptr, bytes);
 }
 }  // namespace
 
 int su2g::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
 
-struct su2g_heff_plan {
-  su2g::HeffWork work;
-  int mode = SU2G_MODE_F64;
-  su2g::GemmSeg* d_seg1 = nullptr;
-  su2g::GemmSeg* d_seg2 = nullptr;
-  su2g::GemmTile* d_tile1 = nullptr;
-  su2g::GemmTile* d_tile2 = nullptr;
-  double* d_scratch = nullptr;
-  // split-precision work (S > 0)
-  int S = 0;
-  su2g::oz::OzWork oz;
-  uint8_t* d_packed = nullptr;
-  int* d_exps = nullptr;
-  su2g::oz::PackJob* d_jobs[3] = {nullptr, nullptr, nullptr};
-  int2* d_units[3] = {nullptr, nullptr, nullptr};
-  su2g::oz::OzSeg* d_oseg1 = nullptr;
-  su2g::oz::OzSeg* d_oseg2 = nullptr;
-  su2g::oz::OzTile* d_otile1 = nullptr;
-  su2g::oz::OzTile* d_otile2 = nullptr;
-  su2g::oz::RedTile* d_red2 = nullptr;
-  int* d_err = nullptr;
-  // Lanczos workspace (allocated on first use)
-  double* d_krylov = nullptr;
-  int krylov_vectors = 0;
-  double* d_red = nullptr;
-  // excited-state projectors y -= w (o . psi) o
-  std::vector<const double*> proj_vec;
-  std::vector<double> proj_w;
-  double* d_proj = nullptr;  // dot scratch, reduction_scratch_doubles() per projector
-  // graph-captured Lanczos steps: lanc_step[m] produces Krylov vector m
-  // (matvec, orthogonalisation, normalisation), lanc_last[m] the final
-  // matvec and alpha; captured on cap_stream for this plan's Krylov buffers
-  std::vector<cudaGraphExec_t> lanc_step, lanc_last;
-  cudaStream_t cap_stream = nullptr;
-  double* d_lcoef = nullptr;  // alpha[0..), beta[0..), reorthogonalisation and norm scratch
-  int lcoef_m = 0;            // largest mlanc the coefficient layout serves
-
-  void drop_graphs() {
-    for (cudaGraphExec_t g : lanc_step)
-      if (g) cudaGraphExecDestroy(g);
-    for (cudaGraphExec_t g : lanc_last)
-      if (g) cudaGraphExecDestroy(g);
-    lanc_step.clear();
-    lanc_last.clear();
-  }
-
-  void release() {
-    cudaFree(d_seg1);
-    cudaFree(d_seg2);
-    cudaFree(d_tile1);
-    cudaFree(d_tile2);
-    cudaFree(d_scratch);
-    cudaFree(d_krylov);
-    cudaFree(d_red);
-    cudaFree(d_packed);
-    cudaFree(d_exps);
-    for (int c = 0; c < 3; ++c) {
-      cudaFree(d_jobs[c]);
-      cudaFree(d_units[c]);
-      d_jobs[c] = nullptr;
-      d_units[c] = nullptr;
-    }
-    cudaFree(d_oseg1);
-    cudaFree(d_oseg2);
-    cudaFree(d_otile1);
-    cudaFree(d_otile2);
-    cudaFree(d_red2);
-    cudaFree(d_err);
-    cudaFree(d_proj);
-    d_proj = nullptr;
-    drop_graphs();
-    if (cap_stream) cudaStreamDestroy(cap_stream);
-    cap_stream = nullptr;
-    cudaFree(d_lcoef);
-    d_lcoef = nullptr;
-    d_seg1 = d_seg2 = nullptr;
-    d_tile1 = d_tile2 = nullptr;
-    d_scratch = d_krylov = d_red = nullptr;
-    d_packed = nullptr;
-    d_exps = d_err = nullptr;
-    d_oseg1 = d_oseg2 = nullptr;
-    d_otile1 = d_otile2 = nullptr;
-    d_red2 = nullptr;
-  }
-};
 
 namespace {
 int slices_of_mode(int mode) {
@@ -153,8 +70,8 @@ su2g::Bases make_bases(const su2g_heff_plan* p, const double* psi, double* y) {
 // the operators (they stay fixed for the lifetime of the plan)
 cudaError_t setup_split(su2g_heff_plan* p) {
   su2g::oz::OzWork& w = p->oz;
-  cudaError_t e = cudaMalloc((void**)&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
+  cudaError_t e = dalloc(&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
+  if (e == cudaSuccess) e = dalloc(&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
   for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
     e = upload(w.jobs[c], &p->d_jobs[c]);
     if (e == cudaSuccess) {
@@ -170,9 +87,12 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   if (e == cudaSuccess) e = upload(w.red2, &p->d_red2);
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
-  e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0], w.rows_pass[0], b, p->d_packed, p->d_exps,
-                            nullptr);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  cudaStream_t st = nullptr;
+  e = su2g::setup_stream(&st);
+  if (e == cudaSuccess)
+    e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0],
+                              w.rows_pass[0], b, p->d_packed, p->d_exps, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   // the GEMM's one-time setup happens here, never inside a graph capture
   if (e == cudaSuccess) e = su2g::oz::prepare_ozaki_gemm(p->S);
   return e;
@@ -279,12 +199,13 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
   if (e == cudaSuccess) e = upload(p->work.tile1, &p->d_tile1);
   if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
   const int64_t scratch_doubles = p->work.scratch_len + p->oz.partial_len;
-  if (e == cudaSuccess && scratch_doubles > 0)
-    e = cudaMalloc((void**)&p->d_scratch, scratch_doubles * sizeof(double));
+  if (e == cudaSuccess && scratch_doubles > 0) e = dalloc(&p->d_scratch, scratch_doubles * sizeof(double));
   // the error word: set by a bounded device wait that gave up, read by
   // su2g_heff_plan_status and every result-returning caller of the plan
-  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    const int zero = 0;
+    e = su2g::upload_bytes(&zero, sizeof(int), (void**)&p->d_err);
+  }
   if (e == cudaSuccess && S > 0) e = setup_split(p);
   if (e != cudaSuccess) {
     p->release();
@@ -508,15 +429,18 @@ int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
   if (!p || !code) return fail(SU2G_EINVAL, "plan_status: bad arguments");
   *code = 0;
   if (!p->d_err) return SU2G_OK;
-  SU2G_CUDA(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  SU2G_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+  // read after the plan's latest work, on its stream
+  SU2G_CUDA(cudaMemcpyAsync(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, p->last_st));
+  SU2G_CUDA(cudaMemsetAsync(p->d_err, 0, sizeof(int), p->last_st));
+  SU2G_CUDA(cudaStreamSynchronize(p->last_st));
   if (*code) return fail(SU2G_ETIMEOUT, "a bounded device wait gave up (code " + std::to_string(*code) + ")");
   return SU2G_OK;
 }
 
 int su2g_heff_plan_mark_failed(su2g_heff_plan* p, int code) {
   if (!p || !p->d_err || code == 0) return fail(SU2G_EINVAL, "plan_mark_failed: bad arguments");
-  SU2G_CUDA(cudaMemcpy(p->d_err, &code, sizeof(int), cudaMemcpyHostToDevice));
+  SU2G_CUDA(cudaMemcpyAsync(p->d_err, &code, sizeof(int), cudaMemcpyHostToDevice, p->last_st));
+  SU2G_CUDA(cudaStreamSynchronize(p->last_st));
   return SU2G_OK;
 }
 
@@ -541,8 +465,10 @@ int su2g_heff_plan_info(const su2g_heff_plan* p, double* flops, int64_t* psi_len
   return SU2G_OK;
 }
 
+}  // extern "C"
+
 // y -= w_j (o_j . psi) o_j for every projector, the dot product kept on the device
-static cudaError_t apply_projectors(su2g_heff_plan* p, const double* psi, double* y, cudaStream_t st) {
+cudaError_t su2g::apply_projectors(su2g_heff_plan* p, const double* psi, double* y, cudaStream_t st) {
   const int64_t n = p->work.psi.total;
   const int ns = su2g::reduction_scratch_doubles();
   for (size_t j = 0; j < p->proj_vec.size(); ++j) {
@@ -554,29 +480,31 @@ static cudaError_t apply_projectors(su2g_heff_plan* p, const double* psi, double
   return cudaSuccess;
 }
 
+extern "C" {
+
 int su2g_heff_plan_add_projector(su2g_heff_plan* p, const double* o, double weight) {
   if (!p || (!o && p->work.psi.total > 0)) return fail(SU2G_EINVAL, "add_projector: bad arguments");
   const int ns = su2g::reduction_scratch_doubles();
   double* d = nullptr;
-  SU2G_CUDA(cudaMalloc((void**)&d, (p->proj_vec.size() + 1) * ns * sizeof(double)));
+  SU2G_CUDA(dalloc(&d, (p->proj_vec.size() + 1) * ns * sizeof(double)));
   p->drop_graphs();  // captured Lanczos steps lack the new projector
-  cudaFree(p->d_proj);
+  su2g::dev_free(p->d_proj, p->last_st);
   p->d_proj = d;
   p->proj_vec.push_back(o);
   p->proj_w.push_back(weight);
   return SU2G_OK;
 }
 
-int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* stream) {
-  if (!p) return fail(SU2G_EINVAL, "heff_apply: null plan");
-  if (p->work.psi.total > 0 && (!psi || !y)) return fail(SU2G_EINVAL, "heff_apply: null vector");
-  if (psi == y && psi) return fail(SU2G_EINVAL, "heff_apply: psi and y must not alias");
-  cudaStream_t st = (cudaStream_t)stream;
+}  // extern "C"
+
+int su2g::cuda_status(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+
+int su2g::heff_apply_impl(su2g_heff_plan* p, const double* psi, double* y, cudaStream_t st) {
   const su2g::Bases b = make_bases(p, psi, y);
   if (p->S == 0) {
     SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile1, (int)p->work.tile1.size(), p->d_seg1, b, st));
     SU2G_CUDA(su2g::launch_gemm_f64(p->d_tile2, (int)p->work.tile2.size(), p->d_seg2, b, st));
-    SU2G_CUDA(apply_projectors(p, psi, y, st));
+    SU2G_CUDA(su2g::apply_projectors(p, psi, y, st));
     return SU2G_OK;
   }
   const su2g::oz::OzWork& w = p->oz;
@@ -592,8 +520,18 @@ int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* strea
   SU2G_CUDA(su2g::oz::launch_ozaki_gemm(p->S, p->d_otile2, (int)w.tile2.size(), p->d_oseg2, p->d_packed, p->d_exps, b,
                                         p->d_err, st));
   SU2G_CUDA(su2g::oz::launch_reduce(p->d_red2, (int)w.red2.size(), b, st));
-  SU2G_CUDA(apply_projectors(p, psi, y, st));
+  SU2G_CUDA(su2g::apply_projectors(p, psi, y, st));
   return SU2G_OK;
+}
+
+extern "C" {
+
+int su2g_heff_apply(su2g_heff_plan* p, const double* psi, double* y, void* stream) {
+  if (!p) return fail(SU2G_EINVAL, "heff_apply: null plan");
+  if (p->work.psi.total > 0 && (!psi || !y)) return fail(SU2G_EINVAL, "heff_apply: null vector");
+  if (psi == y && psi) return fail(SU2G_EINVAL, "heff_apply: psi and y must not alias");
+  p->last_st = (cudaStream_t)stream;
+  return su2g::heff_apply_impl(p, psi, y, (cudaStream_t)stream);
 }
 
 int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, void* stream, double* ms,
@@ -601,6 +539,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
   if (!p || !ms || !nlaunch) return fail(SU2G_EINVAL, "apply_profile: bad arguments");
   if (psi == y && psi) return fail(SU2G_EINVAL, "apply_profile: psi and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
+  p->last_st = st;
   const su2g::Bases b = make_bases(p, psi, y);
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) SU2G_CUDA(cudaEventCreate(&ev[i]));
@@ -643,7 +582,7 @@ int su2g_heff_apply_profile(su2g_heff_plan* p, const double* psi, double* y, voi
     ms[i] = t;
   }
   if (e == cudaSuccess && !p->proj_vec.empty()) {  // untimed: the projectors complete y
-    e = apply_projectors(p, psi, y, st);
+    e = su2g::apply_projectors(p, psi, y, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
@@ -721,7 +660,7 @@ struct LanczosCtx {
   }
   int matvec(const double* x, double* y) {
     ++nmatvec;
-    return su2g_heff_apply(p, x, y, st);
+    return su2g::heff_apply_impl(p, x, y, st);
   }
   int axpy(double a, const double* x, double* y) {
     cudaError_t e = su2g::launch_axpy(a, x, y, n, st);
@@ -749,7 +688,7 @@ struct LanczosCtx {
   // normalisation -- the same kernels in the same order as the host-driven
   // sequence, with every scalar kept on the device.
   cudaError_t enqueue_step(int m, cudaStream_t s) {
-    if (su2g_heff_apply(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
+    if (su2g::heff_apply_impl(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
     cudaError_t e = su2g::launch_dot_to(ff(m - 1), ff(m), n, p->d_red, alpha(m - 1), s);
     if (e == cudaSuccess) e = su2g::launch_axpy_neg_dev(alpha(m - 1), ff(m - 1), ff(m), n, s);
     if (m >= 2) {
@@ -765,7 +704,7 @@ struct LanczosCtx {
   }
   // the final matvec and its alpha (lanczos_su2.cpp:189-194)
   cudaError_t enqueue_last(int m, cudaStream_t s) {
-    if (su2g_heff_apply(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
+    if (su2g::heff_apply_impl(p, ff(m - 1), ff(m), s) != SU2G_OK) return cudaErrorUnknown;
     return su2g::launch_dot_to(ff(m - 1), ff(m), n, p->d_red, alpha(m - 1), s);
   }
   // runs a step as a CUDA graph, captured on first use
@@ -833,21 +772,22 @@ int su2g_lanczos(su2g_heff_plan* p, double* psi, int mlanc, double* energy, int*
   const int need = mlanc + 2;         // ff[0..mlanc] + one work vector
   if (p->krylov_vectors < need) {
     p->drop_graphs();  // captured with the old buffers
-    cudaFree(p->d_krylov);
+    su2g::dev_free(p->d_krylov, p->last_st);
     p->d_krylov = nullptr;
     p->krylov_vectors = 0;
-    SU2G_CUDA(cudaMalloc((void**)&p->d_krylov, (size_t)need * n * sizeof(double)));
+    SU2G_CUDA(dalloc(&p->d_krylov, (size_t)need * n * sizeof(double)));
     p->krylov_vectors = need;
   }
-  if (!p->d_red) SU2G_CUDA(cudaMalloc((void**)&p->d_red, su2g::reduction_scratch_doubles() * sizeof(double)));
+  if (!p->d_red) SU2G_CUDA(dalloc(&p->d_red, su2g::reduction_scratch_doubles() * sizeof(double)));
   if (p->lcoef_m < mlanc) {
     p->drop_graphs();
-    cudaFree(p->d_lcoef);
+    su2g::dev_free(p->d_lcoef, p->last_st);
     p->d_lcoef = nullptr;
     p->lcoef_m = 0;
-    SU2G_CUDA(cudaMalloc((void**)&p->d_lcoef, (size_t)(3 * (mlanc + 1) + 1) * sizeof(double)));
+    SU2G_CUDA(dalloc(&p->d_lcoef, (size_t)(3 * (mlanc + 1) + 1) * sizeof(double)));
     p->lcoef_m = mlanc;
   }
+  p->last_st = (cudaStream_t)stream;
   LanczosCtx L{p, (cudaStream_t)stream, n};
   const double tol = 1.e-6;  // lanczos_su2.cpp:128
   std::vector<double> aal(mlanc, 0.0), nnl(mlanc + 1, 0.0), eig, z;

@@ -12,6 +12,17 @@ namespace su2g {
 // records the calling thread's su2g_last_error() text and returns code
 int set_last_error(int code, const std::string& msg);
 
+// Device memory from a per-device stream-ordered pool (devmem.cu): usable on
+// any stream when dev_alloc returns; dev_free releases it once `after` has
+// passed the point of the call (pass the stream of its last use).  Neither
+// synchronises the device.
+cudaError_t dev_alloc(void** p, size_t bytes);
+void dev_free(void* p, cudaStream_t after);
+// dev_alloc + a copy of `bytes` host bytes, complete on return
+cudaError_t upload_bytes(const void* host, size_t bytes, void** dptr);
+// the calling thread's private non-blocking stream on the current device
+cudaError_t setup_stream(cudaStream_t* out);
+
 cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
                             cudaStream_t stream);
 

@@ -186,6 +186,8 @@ void split_phase2(OzWork& w) {
   w.tile2.swap(out);
 }
 
+}  // namespace
+
 // Static schedule of the persistent GEMM, whose CTA b walks the tiles b, b +
 // G, b + 2G, ... (G = grid).  Each tile's cost in stage units counts its
 // stages, one drain of the TMEM group sums per chunk (about five stages of
@@ -233,8 +235,6 @@ void schedule_tiles(std::vector<OzTile>* tiles, const std::vector<OzSeg>& segs, 
     for (size_t k = 0; k < lists[b].size(); ++k) out[b + k * grid] = (*tiles)[lists[b][k]];
   tiles->swap(out);
 }
-
-}  // namespace
 
 int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   OzWork& w = *out;

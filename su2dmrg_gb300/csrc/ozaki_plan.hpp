@@ -36,6 +36,10 @@ struct OzWork {
 // The operand that is not an operator (psi or an intermediate) carries no
 // scale factor: a product's alpha is folded into its operator operand.
 int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err);
+// The static schedule of the persistent GEMM over `grid` CTAs: tiles dealt
+// longest first to the least-loaded CTA and laid out so that CTA b walks
+// b, b + grid, ...; empty tiles pad the walks.
+void schedule_tiles(std::vector<OzTile>* tiles, const std::vector<OzSeg>& segs, int grid);
 int validate_ozaki_work(const OzWork& w, std::string* err);
 
 }  // namespace oz

@@ -22,6 +22,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -80,12 +82,12 @@ __global__ void __launch_bounds__(256) canonical_signs_kernel(double* z, int row
     for (int i = threadIdx.x; i < rows; i += blockDim.x) col[i] = -col[i];
 }
 
-// Per-device resources kept across calls: one stream and one pair of
-// cuBLAS / cuSOLVER handles per concurrently processed sector (creating
-// handles costs milliseconds), and a library-private memory pool whose freed
-// blocks stay reserved (stream-ordered allocation without device-wide
-// synchronisation, unlike cudaMalloc).  One su2g_svd call holds them at a
-// time.
+// Per-device resources kept across calls: lanes (one stream and one pair of
+// cuBLAS / cuSOLVER handles each; creating handles costs milliseconds), lent
+// to a call for each sector it processes and returned after it, so calls from
+// several host threads (independent solves) run at the same time; and a
+// library-private memory pool whose freed blocks stay reserved (stream-ordered
+// allocation without device-wide synchronisation, unlike cudaMalloc).
 struct Lane {
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
@@ -94,13 +96,16 @@ struct Lane {
 };
 struct DeviceRes {
   cudaMemPool_t pool = nullptr;
-  std::vector<Lane> lanes;
+  std::vector<Lane> free_lanes;
 };
 std::mutex g_res_mutex;
 std::map<int, DeviceRes> g_res;
 
-// Grows the device's lanes to n; returns an error message or "".
-std::string acquire_lanes(DeviceRes& r, int dev, int n) {
+// Lends n lanes of device dev (creating what is missing) and the pool;
+// returns an error message or "".
+std::string take_lanes(int dev, int n, std::vector<Lane>* out, cudaMemPool_t* pool) {
+  std::lock_guard<std::mutex> lock(g_res_mutex);
+  DeviceRes& r = g_res[dev];
   if (!r.pool) {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
@@ -113,7 +118,13 @@ std::string acquire_lanes(DeviceRes& r, int dev, int n) {
     uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool
     cudaMemPoolSetAttribute(r.pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  while ((int)r.lanes.size() < n) {
+  *pool = r.pool;
+  out->clear();
+  while ((int)out->size() < n && !r.free_lanes.empty()) {
+    out->push_back(r.free_lanes.back());
+    r.free_lanes.pop_back();
+  }
+  while ((int)out->size() < n) {
     Lane l;
     if (cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking) != cudaSuccess) return "cannot create a stream";
     if (cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming) != cudaSuccess) {
@@ -128,10 +139,76 @@ std::string acquire_lanes(DeviceRes& r, int dev, int n) {
     }
     cublasSetStream(l.blas, l.st);
     cusolverDnSetStream(l.sol, l.st);
-    r.lanes.push_back(l);
+    out->push_back(l);
   }
   return "";
 }
+
+void give_lanes(int dev, const std::vector<Lane>& lanes) {
+  std::lock_guard<std::mutex> lock(g_res_mutex);
+  DeviceRes& r = g_res[dev];
+  r.free_lanes.insert(r.free_lanes.end(), lanes.begin(), lanes.end());
+}
+
+// Host threads that run the sectors of a call (the refinement loop reads
+// eigenvalues back between its steps, so each sector needs its own thread).
+// Kept across calls and grown on demand, instead of one thread per sector per
+// call; never joined (the process ends with them).
+class SectorThreads {
+ public:
+  static SectorThreads& get() {
+    static SectorThreads* t = new SectorThreads();
+    return *t;
+  }
+  // runs body(0..n-1), body(0) on the calling thread, and returns when all are done
+  void run(size_t n, const std::function<void(size_t)>& body) {
+    if (n == 0) return;
+    struct Latch {
+      std::mutex mu;
+      std::condition_variable cv;
+      size_t left;
+    } latch;
+    latch.left = n - 1;
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      for (size_t q = 1; q < n; ++q)
+        queue_.push_back([&, q] {
+          body(q);
+          std::lock_guard<std::mutex> l(latch.mu);
+          if (--latch.left == 0) latch.cv.notify_all();
+        });
+      while (idle_ < queue_.size()) {  // a thread per waiting task
+        std::thread(&SectorThreads::loop, this).detach();
+        ++idle_;
+      }
+    }
+    cv_.notify_all();
+    body(0);
+    std::unique_lock<std::mutex> l(latch.mu);
+    latch.cv.wait(l, [&] { return latch.left == 0; });
+  }
+
+ private:
+  void loop() {
+    for (;;) {
+      std::function<void()> task;
+      {
+        std::unique_lock<std::mutex> lock(mu_);
+        cv_.wait(lock, [&] { return !queue_.empty(); });
+        task = std::move(queue_.front());
+        queue_.pop_front();
+        --idle_;
+      }
+      task();
+      std::lock_guard<std::mutex> lock(mu_);
+      ++idle_;
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> queue_;
+  size_t idle_ = 0;
+};
 
 // The work of one sector: its lane, its allocations (from the pool, on the
 // lane's stream; released on `free_st` once the caller's stream has used
@@ -399,10 +476,19 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return fail(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(ce));
-  std::unique_lock<std::mutex> lock(g_res_mutex);
-  DeviceRes& res = g_res[dev];
-  const std::string rerr = acquire_lanes(res, dev, (int)jobs.size());
-  if (!rerr.empty()) return fail(SU2G_ECUDA, "svd: " + rerr);
+  std::vector<Lane> lanes;
+  cudaMemPool_t pool = nullptr;
+  const std::string rerr = take_lanes(dev, (int)jobs.size(), &lanes, &pool);
+  if (!rerr.empty()) {
+    give_lanes(dev, lanes);
+    return fail(SU2G_ECUDA, "svd: " + rerr);
+  }
+  // the lanes go back to the device's free list when the call returns
+  struct LaneReturn {
+    int dev;
+    const std::vector<Lane>& lanes;
+    ~LaneReturn() { give_lanes(dev, lanes); }
+  } lane_return{dev, lanes};
   // every sector on its own lane (stream + handles) and host thread: the
   // eigendecompositions and the refinement loops of all sectors overlap
   cudaEvent_t ready = nullptr;
@@ -417,11 +503,11 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   for (size_t q = 0; q < jobs.size(); ++q) {
     ctx[q].reset(new Ctx());
     Ctx& c = *ctx[q];
-    c.st = res.lanes[q].st;
+    c.st = lanes[q].st;
     c.free_st = cst;
-    c.pool = res.pool;
-    c.blas = res.lanes[q].blas;
-    c.sol = res.lanes[q].sol;
+    c.pool = pool;
+    c.blas = lanes[q].blas;
+    c.sol = lanes[q].sol;
     const cudaError_t we = cudaStreamWaitEvent(c.st, ready, 0);  // psi is written on the caller's stream
     if (we != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(we));
   }
@@ -430,12 +516,7 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
   // and the factors
   std::vector<SectorEig> eig(jobs.size());
   double lam_cut = 0.0, lam_cut_raw = 0.0, noise_floor = 0.0;
-  auto on_threads = [&](auto&& body) {
-    std::vector<std::thread> threads;
-    for (size_t q = 1; q < jobs.size(); ++q) threads.emplace_back(body, q);
-    if (!jobs.empty()) body(0);
-    for (std::thread& t : threads) t.join();
-  };
+  auto on_threads = [&](const std::function<void(size_t)>& body) { SectorThreads::get().run(jobs.size(), body); };
   on_threads([&](size_t q) {
     Ctx& c = *ctx[q];
     if (cudaSetDevice(dev) != cudaSuccess) c.set(SU2G_ECUDA, "svd: cannot select the device");
@@ -473,11 +554,11 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
     }
     if (trace) cudaStreamSynchronize(c.st);
     eig[q].ms_finish = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    const cudaError_t e = cudaEventRecord(res.lanes[q].done, c.st);
+    const cudaError_t e = cudaEventRecord(lanes[q].done, c.st);
     if (e != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
   });
   // the caller's stream continues after every sector (placement copies, frees)
-  for (size_t q = 0; q < jobs.size(); ++q) cudaStreamWaitEvent(cst, res.lanes[q].done, 0);
+  for (size_t q = 0; q < jobs.size(); ++q) cudaStreamWaitEvent(cst, lanes[q].done, 0);
   cudaEventDestroy(ready);
   for (const auto& c : ctx)
     if (!c->ok()) return fail(c->code, c->err);

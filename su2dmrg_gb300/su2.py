@@ -253,6 +253,56 @@ class HeffPlan:
             pass
 
 
+class HeffBatch:
+    """Several HeffPlans (one precision mode) applied in shared launches
+    (su2g_heff_batch_*): plan i's vector lies at offsets()[i] of the batch
+    vectors.  The plans must outlive the batch."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        arr = (ctypes.c_void_p * len(self.plans))(*[p.handle.value for p in self.plans])
+        h = ctypes.c_void_p()
+        check(lib().su2g_heff_batch_create(ctypes.addressof(arr), len(self.plans), ctypes.addressof(h)))
+        self._h = h
+        tot = ctypes.c_int64()
+        check(lib().su2g_heff_batch_info(self._h, ctypes.addressof(tot), None))
+        self.total = tot.value
+        lens = [p.info()["psi_len"] for p in self.plans]
+        self._off = [int(x) for x in np.concatenate([[0], np.cumsum(lens)[:-1]])]
+
+    def offsets(self):
+        return list(self._off)
+
+    def apply(self, x, y, stream=None) -> None:
+        """y = H x for every plan on its slice of the batch vectors."""
+        check(lib().su2g_heff_batch_apply(self._h, ptr(x), ptr(y), stream_handle(stream)))
+
+    def status(self) -> None:
+        check(lib().su2g_heff_batch_status(self._h))
+
+    def lanczos(self, psis, mlanc: int = 5, stream=None):
+        """Lockstep Lanczos of every plan (psis[i]: plan i's start vector,
+        overwritten with its eigenvector); returns [(energy, nmatvec)]."""
+        n = len(self.plans)
+        arr = (ctypes.c_void_p * n)(*[ptr(v) for v in psis])
+        e = (ctypes.c_double * n)()
+        nm = (ctypes.c_int * n)()
+        check(lib().su2g_heff_batch_lanczos(self._h, ctypes.addressof(arr), int(mlanc), ctypes.addressof(e),
+                                            ctypes.addressof(nm), stream_handle(stream)))
+        return [(e[i], nm[i]) for i in range(n)]
+
+    def close(self) -> None:
+        if self._h:
+            lib().su2g_heff_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def hamiltonian_vector_multiplication(vec: Su2Struct, vec_data, op1: Su2Struct, x1, op2: Su2Struct, x2, y,
                                       stream=None) -> None:
     keep = []

@@ -82,7 +82,7 @@ class Dmrg(Warmup):
         plan = self.heff_plan(il, ir, vs)
         t = self._timed("heff_plan", t)
         n = vs.size()
-        e, _ = plan.lanczos(vx, mlanc=self.mlanc if self.mlanc <= n else n + 1)
+        e, _ = self.eigensolve(plan, vx, self.mlanc if self.mlanc <= n else n + 1)
         plan.close()
         self._keep.clear()
         t = self._timed("lanczos", t)

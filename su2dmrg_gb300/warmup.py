@@ -383,6 +383,15 @@ class Warmup:
                 self.plq[i][name[1]] = t
 
     # ------------------------------------------------------- two-site step
+    # the Lanczos solve of a two-site step; a serving loop replaces it with
+    # one that shares launches with other solves (same results, bit for bit)
+    lanczos_hook = None
+
+    def eigensolve(self, plan, vx, mlanc: int):
+        if self.lanczos_hook is not None:
+            return self.lanczos_hook(plan, vx, mlanc)
+        return plan.lanczos(vx, mlanc=mlanc)
+
     def heff_plan(self, il: int, ir: int, vs):
         """The terms of hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664)."""
         L, ns = self.lat, self.lat.ns
@@ -445,7 +454,7 @@ class Warmup:
                 self.site_right(ir, S.fuse_tensor(*self._legs01(ur)))
                 plan = self.heff_plan(il, ir, vs)
                 n = vs.size()
-                e, _ = plan.lanczos(vx, mlanc=self.mlanc if self.mlanc <= n else n + 1)
+                e, _ = self.eigensolve(plan, vx, self.mlanc if self.mlanc <= n else n + 1)
                 plan.close()
                 self._keep.clear()
                 self.energies.append((il, ir, e))
