@@ -342,6 +342,14 @@ int su2g_fuse_tensor(const int* bonds_desc, double* out, void* stream);
  * 79-80): the structure of su2g_prepare_input_vector's vector with every
  * element 1/sqrt(N), N its length. */
 int su2g_initial_vector(su2g_tensor ul, su2g_tensor ur, double* out, void* stream);
+/* The seeded random start vector: tensor_su2::random_initialize_tensor
+ * (tensor_su2.cpp:2375-2393) followed by normalize_vector, in place of
+ * initialize_input_vector at dmrg_su2_omp.cpp:79 (the -seed option added on
+ * both sides).  out[k] = ran()*2 - 1 for k = 0..n-1 (the packed order of any
+ * tensor's stored blocks), ran() the generator of ran.f90:2-16 continuing
+ * from *state (initran: *state = seed), then out is divided by its norm
+ * twice.  *state is advanced by n steps on return.  Blocks until done. */
+int su2g_random_vector(int64_t* state, double* out, int64_t n, void* stream);
 
 /* dmrg_su2::prepare_input_vector(il, ir, vec) (dmrg_su2_omp.cpp:229-254):
  * the initial two-site vector of a step from ul = uu[il] and ur = uu[ir]

@@ -38,6 +38,10 @@ double ran_(void) {
 /* The reference calls initran_ with a pointer to a C int (main_omp.cpp:38-40). */
 void initran_(const int *w) { ran64_state = (int64_t)(*w); }
 
+/* the generator's state, for tests that continue the stream across calls */
+int64_t or_ran_state(void) { return ran64_state; }
+void or_set_ran_state(int64_t s) { ran64_state = s; }
+
 void isort_(const int *n, int *a) {
   int len = *n;
   for (int gap = len / 2; gap > 0; gap /= 2) {

@@ -1055,3 +1055,26 @@ def synthetic_heff(D: int = 2000, nspin1: int = 18, seed: int = 1234, max2j: int
                 blk = rng.standard_normal((a, c)) / np.sqrt(a)
                 hx[side][hoff[i]: hoff[i] + a * c] = (0.5 * (blk + blk.T)).ravel(order="F")
     return HeffProblem(psi, terms, (hs, hx[0], 1.0), (hs, hx[1], 1.0)), x
+
+
+# --------------------------------------------------------------------------
+# seeded random start vector
+# --------------------------------------------------------------------------
+def random_vector(state: int, n: int):
+    """tensor_su2::random_initialize_tensor (tensor_su2.cpp:2375-2393) of an
+    n-element packed vector followed by normalize_vector (tensor_su2.cpp:324-356)
+    twice, the generator ran() of ran.f90:2-16 (fhelpers.c) continuing from
+    `state`.  Returns (values, raw draws ran()*2-1, new state)."""
+    L = lib()
+    L.or_ran_state.restype = ctypes.c_int64
+    L.or_set_ran_state.argtypes = [ctypes.c_int64]
+    L.ran_.restype = ctypes.c_double
+    L.or_set_ran_state(int(state))
+    raw = np.array([L.ran_() * 2.0 - 1.0 for _ in range(n)])
+    x = raw.copy()
+    for _ in range(2):
+        nor = 0.0
+        for v in x:
+            nor += v * v
+        x = x / np.sqrt(nor)
+    return x, raw, int(L.or_ran_state())

@@ -25,6 +25,19 @@ void scipy_openblas_set_num_threads(int);
 int su2ref_idmrg_mlanc = 5;
 void su2ref_set_idmrg_mlanc(int m) { su2ref_idmrg_mlanc = m; }
 
+/* The -seed option of the parity runs (patch_ref.py hooks dmrg_su2_omp.cpp:79
+ * to it): when set, the warm-up starts each two-site step from
+ * random_initialize_tensor instead of initialize_input_vector, the generator
+ * seeded once here with initran (the reference seeds it from the clock,
+ * main_omp.cpp:39-41).  Off by default. */
+int su2ref_seeded = 0;
+void initran_(const int* w);
+void su2ref_set_seed(int seed) {
+  su2ref_seeded = 1;
+  initran_(&seed);
+}
+void su2ref_clear_seed(void) { su2ref_seeded = 0; }
+
 static int sign_convention = 0;
 void su2ref_set_sign_convention(int on) { sign_convention = on; }
 

@@ -16,6 +16,11 @@ unchanged unless a test sets it).  A warm-up with five Lanczos vectors from
 the uniform start vector stops near an invariant subspace and follows
 rounding noise; with enough vectors to converge its result is a property of
 the model, which is what the warm-up fixtures of the larger lattices pin.
+
+A second hook adds the -seed option of the parity runs: the warm-up's start
+vector (dmrg_su2_omp.cpp:79) is random_initialize_tensor when the global
+su2ref_seeded is set (blas_shim.c su2ref_set_seed, which also seeds the
+generator with initran), else the engine's own initialize_input_vector.
 """
 import sys
 from pathlib import Path
@@ -32,7 +37,10 @@ SITES = {
 
 # (file, line, expected text, replacement)
 HOOKS = [("dmrg_su2.cpp", 530, "  int mlanc=5,nele1,nele2;",
-          "  extern int su2ref_idmrg_mlanc;\n  int mlanc=su2ref_idmrg_mlanc,nele1,nele2;")]
+          "  extern int su2ref_idmrg_mlanc;\n  int mlanc=su2ref_idmrg_mlanc,nele1,nele2;"),
+         ("dmrg_su2_omp.cpp", 79, "      vec.initialize_input_vector();",
+          "      { extern int su2ref_seeded; if (su2ref_seeded) vec.random_initialize_tensor(); "
+          "else vec.initialize_input_vector(); }")]
 
 
 def main(workdir: str) -> None:

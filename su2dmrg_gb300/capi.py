@@ -106,6 +106,7 @@ _PROTOS = {
     "su2g_fuse_tensor_layout": (_i, [_vp, _vp, _i, _vp, _i, _vp]),
     "su2g_fuse_tensor": (_i, [_vp, _vp, _vp]),
     "su2g_initial_vector": (_i, [Tensor, Tensor, _vp, _vp]),
+    "su2g_random_vector": (_i, [_vp, _vp, ctypes.c_int64, _vp]),
     "su2g_prepare_input_vector": (_i, [Tensor, Tensor, _vp, _i, _vp]),
     "su2g_take_trace": (_i, [Tensor, _vp, _vp]),
     "su2g_ss_inner_prod": (_i, [Tensor, Tensor, _vp, _vp]),

@@ -406,3 +406,94 @@ extern "C" int su2g_initial_vector(su2g_tensor ul, su2g_tensor ur, double* out, 
   return SU2G_OK;
 }
 
+
+// ------------------------------------------------- seeded random start vector
+// tensor_su2::random_initialize_tensor (tensor_su2.cpp:2375-2393): every
+// stored block filled with ran()*2 - 1 in block order, each block column-major
+// (tensor::random_init, tensor.cpp:155-160), which is the packed order of the
+// vector; then normalize_vector (tensor_su2.cpp:324-356) -- once inside
+// random_initialize_tensor and once more by the caller (dmrg_su2_omp.cpp:80).
+// ran() is the 64-bit linear congruential generator of ran.f90:2-16,
+//     s <- s * 2862933555777941757 + 1013904243 (mod 2^64),
+//     ran = 0.5 + (0.5 / (2^63 - 1)) * (double)(signed) s,
+// element k taking the state after k + 1 steps.  Each thread jumps ahead to
+// its first element (composition of the affine step, by squaring) and then
+// strides by the grid with the step composed grid-size times, so the values
+// are those of the sequential generator, bit for bit.
+namespace {
+
+constexpr uint64_t kLcgMul = 2862933555777941757ull;
+constexpr uint64_t kLcgAdd = 1013904243ull;
+
+// (mul, add) of the LCG applied n times
+__host__ __device__ inline void lcg_power(uint64_t n, uint64_t* mul, uint64_t* add) {
+  uint64_t am = 1, aa = 0;              // accumulated map x -> am x + aa
+  uint64_t bm = kLcgMul, ba = kLcgAdd;  // the step applied 2^i times
+  while (n) {
+    if (n & 1) {
+      am = am * bm;
+      aa = aa * bm + ba;
+    }
+    ba = ba * bm + ba;
+    bm = bm * bm;
+    n >>= 1;
+  }
+  *mul = am;
+  *add = aa;
+}
+
+__device__ inline double lcg_value(uint64_t s) {
+  const double dmu64 = 0.5 / 9223372036854775807.0;
+  const double r = __dadd_rn(0.5, __dmul_rn(dmu64, (double)(long long)s));
+  return __dadd_rn(__dmul_rn(r, 2.0), -1.0);
+}
+
+__global__ void lcg_fill_kernel(double* x, int64_t n, uint64_t s0, uint64_t stride_mul, uint64_t stride_add) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint64_t m, a;
+  lcg_power((uint64_t)t + 1, &m, &a);
+  uint64_t s = m * s0 + a;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = t; k < n; k += stride) {
+    x[k] = lcg_value(s);
+    s = stride_mul * s + stride_add;
+  }
+}
+
+// x /= sqrt(*nn), as normalize_vector divides
+__global__ void div_sqrt_kernel(double* x, int64_t n, const double* nn) {
+  const double nor = sqrt(*nn);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    x[k] = __ddiv_rn(x[k], nor);
+}
+
+}  // namespace
+
+extern "C" int su2g_random_vector(int64_t* state, double* out, int64_t n, void* stream) {
+  if (!state || n < 0 || (n > 0 && !out)) return fail(SU2G_EINVAL, "random_vector: bad arguments");
+  if (n == 0) return SU2G_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 4);
+  uint64_t sm, sa;
+  lcg_power((uint64_t)grid * 256, &sm, &sa);
+  lcg_fill_kernel<<<grid, 256, 0, st>>>(out, n, (uint64_t)*state, sm, sa);
+  cudaError_t e = cudaGetLastError();
+  const int ns = su2g::reduction_scratch_doubles();
+  double* scratch = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&scratch, ns * sizeof(double), st);
+  for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {  // random_initialize_tensor, then the caller
+    e = su2g::launch_dot(out, out, n, scratch, st);
+    if (e == cudaSuccess) {
+      div_sqrt_kernel<<<grid, 256, 0, st>>>(out, n, scratch + ns - 1);
+      e = cudaGetLastError();
+    }
+  }
+  if (scratch) cudaFreeAsync(scratch, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "random_vector");
+  uint64_t m, a;
+  lcg_power((uint64_t)n, &m, &a);
+  *state = (int64_t)(m * (uint64_t)*state + a);
+  return SU2G_OK;
+}

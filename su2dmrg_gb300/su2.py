@@ -602,6 +602,14 @@ def fuse_tensor_layout(b1: Su2Bond, b2: Su2Bond) -> Su2Struct:
     return _layout_out(lib().su2g_fuse_tensor_layout, ptr(bd))
 
 
+def random_vector(x, state: int, stream=None) -> int:
+    """Fills the device vector x with the seeded random start vector
+    (su2g_random_vector); returns the generator's state after it."""
+    st = ctypes.c_int64(int(state))
+    check(lib().su2g_random_vector(ctypes.addressof(st), ptr(x), int(x.numel()), stream_handle(stream)))
+    return st.value
+
+
 def initial_vector(ul: Su2Struct, xl, ur: Su2Struct, xr, stream=None):
     """The warm-up's start vector on prepare_input_vector's structure."""
     import torch

@@ -40,6 +40,7 @@ class Dmrg(Warmup):
             return None if t is None else (t[0], t[1].clone())
 
         d = Dmrg(self.lat, mode=self.mode if mode is None else mode, mlanc=self.mlanc)
+        d.ran_state = self.ran_state
         d.uu = [cp(t) for t in self.uu]
         d.hh = [cp(t) for t in self.hh]
         d.opr = [[cp(t) for t in row] for row in self.opr]

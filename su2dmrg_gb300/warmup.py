@@ -212,8 +212,12 @@ def discarded_weight(kept: int, w) -> float:
 class Warmup:
     """do_idmrg on the device.  mode: capi.MODE_* for every contraction."""
 
-    def __init__(self, lat: Lattice, mode: int = capi.MODE_F64, mlanc: int = 5):
+    def __init__(self, lat: Lattice, mode: int = capi.MODE_F64, mlanc: int = 5, seed: int = None):
         self.lat, self.mode, self.mlanc = lat, mode, mlanc
+        # seed: start every two-site step of the warm-up from a random vector
+        # of the ran() generator (initran(seed), random_initialize_tensor)
+        # instead of the uniform one; the stream continues across steps
+        self.ran_state = None if seed is None else int(seed)
         ns = lat.ns
         self.uu = [None] * ns
         self.hh = [None] * ns
@@ -450,6 +454,8 @@ class Warmup:
                 ul, ur = self.uu[il], self.uu[ir]
                 vs, vx = S.initial_vector(ul[0], ul[1], ur[0], ur[1])
                 vx = vx[: vs.size()]
+                if self.ran_state is not None:
+                    self.ran_state = S.random_vector(vx, self.ran_state)
                 self.site_left(il, S.fuse_tensor(*self._legs01(ul)))
                 self.site_right(ir, S.fuse_tensor(*self._legs01(ur)))
                 plan = self.heff_plan(il, ir, vs)

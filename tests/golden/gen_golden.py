@@ -18,6 +18,7 @@ Fixtures:
   svd_*.npz            tensor_su2::svd truncation cases (singular values, kept
                        multiplets per sector)
   dmrg_energies.json   whole reference DMRG runs (E0 - 1000 per sweep)
+  dmrg_seeded.json     whole runs from the seeded random start (-seed), and ran()
 """
 from __future__ import annotations
 
@@ -425,6 +426,45 @@ def dmrg_runs(L):
     return out
 
 
+def seeded_runs(L):
+    """Whole runs with the seeded random start (the -seed option of the parity
+    runs, patch_ref.py): the warm-up's two-site steps start from
+    random_initialize_tensor with the generator seeded once by initran.  The
+    6x4 J1-J2 run at D = 200 is the benchmark's CPU-runnable configuration
+    (4 sweeps from a seeded random MPS).  Also the first draws of ran() for
+    seed 1234 (the generator of ran.f90 as the reference build links it)."""
+    runs = [
+        # (lx, ly, sec, D, niter, jcoup, qcoup, boundary, seed)
+        (4, 2, 0, 64, 4, 0.5, 0.0, 2, 7),
+        (3, 4, 0, 64, 4, 0.5, 1.0, 2, 99),
+        (6, 4, 0, 200, 4, 2.0, 0.0, 2, 1234),
+    ]
+    out = {"runs": []}
+    L.ran_.restype = ctypes.c_double
+    seed = ctypes.c_int(1234)
+    L.initran_(ctypes.byref(seed))
+    out["ran_seed1234"] = [L.ran_() for _ in range(16)]
+    cwd = os.getcwd()
+    for (lx, ly, sec, d, niter, jc, qc, bd, sd) in runs:
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            e = np.zeros(64)
+            L.su2ref_set_seed(sd)
+            n = L.ref_run_dmrg(lx, ly, sec, d, niter, ctypes.c_double(jc), ctypes.c_double(qc), bd, 1, p(e))
+            L.su2ref_clear_seed()
+            os.chdir(cwd)
+        descs = []
+        for i in range(lx * ly):
+            assert L.ref_select_mps(i) == 0
+            dd = np.zeros(1024, np.int32)
+            nd = L.ref_result_desc(p(dd))
+            descs.append([int(v) for v in dd[:nd]])
+        out["runs"].append(dict(lx=lx, ly=ly, sec=sec, d=d, niter=niter, jcoup=jc, qcoup=qc, boundary=bd, seed=sd,
+                                energies_minus_1000=[float(v) for v in e[:n]], mps_desc=descs))
+        print("seeded", lx, ly, d, sd, out["runs"][-1]["energies_minus_1000"], file=sys.stderr)
+    return out
+
+
 def input_vector_cases(L, rng):
     """prepare_input_vector (the initial two-site vector of a step) and the
     vectran permutations of wavefunc_transformation, on random MPS tensors."""
@@ -706,6 +746,11 @@ def main():
         L.ref_setup(1, 25)
         with open(os.path.join(HERE, "dmrg_energies.json"), "w") as f:
             json.dump(dmrg_runs(L), f, indent=1)
+        return
+    if "--only-seeded" in sys.argv:
+        L.ref_setup(1, 25)
+        with open(os.path.join(HERE, "dmrg_seeded.json"), "w") as f:
+            json.dump(seeded_runs(L), f, indent=1)
         return
     if "--only-lattices" in sys.argv:
         # lattice tables of the other boundary conditions (0 square, 1 J1-J3,

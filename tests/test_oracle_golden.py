@@ -289,3 +289,13 @@ def test_mea_enr_matches_reference(oracle, path):
     hl, hr, ww, pairs = mea_case(oracle, g)
     e = oracle.mea_enr(hl, hr, ww, pairs)
     assert abs(e - g["parts"][4]) <= 1e-12 * abs(g["parts"][4])
+
+
+def test_oracle_generator_matches_reference_draws(oracle):
+    """ran() of the reference build (ran.f90 as linked there) for seed 1234:
+    the oracle's seeded random vector draws the same numbers."""
+    import json
+
+    g = json.load(open(os.path.join(GOLDEN, "dmrg_seeded.json")))
+    _, raw, _ = oracle.random_vector(1234, 16)
+    assert np.array_equal(raw, np.array(g["ran_seed1234"]) * 2.0 - 1.0)
