@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--nspin1", type=int, default=18)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--row", default="heff",
-                    choices=["heff", "input_vector", "vectran", "env", "svd", "sweep", "serve"],
+                    choices=["heff", "input_vector", "vectran", "env", "svd", "sweep", "serve", "tune"],
                     help="heff (the headline) or another operation of the site step, timed on the "
                          "D-multiplet site-step workload (workloads.synthetic_site_step); sweep: one whole "
                          "DMRG sweep of a J1-J2 cylinder after the device warm-up, split and FP64 contractions "
@@ -82,6 +82,8 @@ def parse():
                     help="sweep row: split sweeps until one changes the energy by less than 1e-6 before the "
                          "timed split and FP64 sweeps")
     ap.add_argument("--max-sweeps", type=int, default=8, help="sweep row: at most this many sweeps with --converge")
+    ap.add_argument("--table-out", default=None, help="tune row: where to write the measured tile table (JSON)")
+    ap.add_argument("--seed", type=int, default=None, help="sweep row: seeded random start of the warm-up")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = 250 if a.row == "heff" else 10
@@ -751,7 +753,7 @@ def run_sweep(args):
     split = MODES["split"]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    d = Dmrg(lat, mode=split)
+    d = Dmrg(lat, mode=split, seed=args.seed)
     e_prev = d.run()
     torch.cuda.synchronize()
     warm_s = time.perf_counter() - t0
@@ -791,7 +793,9 @@ def run_sweep(args):
             "value": split_s, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": split_s * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 emulated by bf16 x7 (fp32 accumulate); FP64 truncation and Lanczos scalars",
-            "data": "synthetic (lattice tables built here; the uniform warm-up start, as the engine)",
+            "data": "synthetic (lattice tables built here; " + (
+                f"seeded random warm-up start, seed {args.seed})" if args.seed is not None
+                else "the uniform warm-up start, as the engine)"),
             "config": {"workload": f"{lx}x{ly} cylinder, boundary 2, D={args.D}, sweep {len(before) + 1} "
                                    f"after the warm-up",
                        "row": "sweep", "two_site_steps": len(steps_split), "warmup_seconds": warm_s,
@@ -899,6 +903,90 @@ def run_serve(args):
     return 0
 
 
+def run_tune(args):
+    """The block-size autotuner of the FP64 engine (su2dmrg_gb300.autotune):
+    measures the four tile classes on every (M, N) size bucket, installs the
+    fastest per bucket, writes the table to --table-out, and times FP64 H_eff
+    applications with 64 x 64 tiles only and with the tuned table: synthetic
+    two-site steps from small to large blocks (D = 100 .. 2000) and the centre
+    step of a real J1-J2 8x4 warm-up at D = 256.  Results are bit-identical
+    either way (the tile shape does not change any summation order)."""
+    import torch
+
+    from su2dmrg_gb300 import autotune as A
+    from su2dmrg_gb300 import capi
+    from su2dmrg_gb300 import su2 as S
+    from su2dmrg_gb300.sweep import Dmrg
+    from su2dmrg_gb300.warmup import Lattice
+    from su2dmrg_gb300.workloads import synthetic_heff
+
+    capi.lib()
+    torch.cuda.set_device(0)
+    A.reset()
+    t0 = time.perf_counter()
+    table = A.tune()
+    tune_s = time.perf_counter() - t0
+    if args.table_out:
+        A.save(table, args.table_out)
+
+    def time_plan(make, reps):
+        out = {}
+        for name, tab in (("64x64", None), ("tuned", table)):
+            if tab is None:
+                A.reset()
+            else:
+                A.install(tab)
+            plan, psi = make()
+            y = torch.empty_like(psi)
+            for _ in range(2):
+                plan.apply(psi, y)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                plan.apply(psi, y)
+            e1.record()
+            torch.cuda.synchronize()
+            out[name] = (e0.elapsed_time(e1) / reps, y.clone(), plan.info()["flops"])
+            plan.close()
+        same = bool(torch.equal(out["64x64"][1], out["tuned"][1]))
+        return {"ms_64x64": out["64x64"][0], "ms_tuned": out["tuned"][0],
+                "speedup": out["64x64"][0] / out["tuned"][0], "bit_identical": same,
+                "tflops_tuned": out["tuned"][2] / out["tuned"][0] / 1e9}
+
+    rows = {}
+    for D in (100, 200, 500, 2000):
+        w = synthetic_heff(D=D, nspin1=18, seed=1234)
+        dev = w.to_device()
+
+        def make(w=w, dev=dev):
+            psi, terms, hl, hr = dev
+            return S.HeffPlan(w.psi, terms, hl, hr, mode=MODES["f64"]), psi
+        rows[f"synthetic D={D}"] = time_plan(make, 3 if D == 2000 else 20)
+    lat = Lattice.cylinder(8, 4, 2.0, 0.0, 256)
+    d = Dmrg(lat, mode=MODES["f64"])
+    d.run()
+    il, ir = lat.ns // 2 - 1, lat.ns // 2
+    vs, vx = S.prepare_input_vector(*d.uu[il], *d.uu[ir], mode=MODES["f64"])
+    vx = vx[: vs.size()].clone()
+
+    def make_real():
+        return d.heff_plan(il, ir, vs), vx
+    rows["8x4 J1-J2 D=256 warm-up, centre step"] = time_plan(make_real, 20)
+    A.install(table)
+    line = {"metric": "FP64 H_eff*psi speed-up of the tuned tile table over 64x64 tiles", "value":
+            rows["synthetic D=200"]["speedup"], "unit": "x", "n_gpus": 1, "steps": 20, "warmup": 2,
+            "ms_per_step": rows["synthetic D=200"]["ms_tuned"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "FP64 engine tile autotuning; H_eff steps from small to large blocks",
+                       "row": "tune", "tune_seconds": tune_s, "table": {k: table[k] for k in
+                                                                       ("m_edges", "n_edges", "cls")},
+                       "steps": rows},
+            "cpu_baseline": None}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -907,6 +995,8 @@ def main():
         return run_sweep(args)
     if args.row == "serve":
         return run_serve(args)
+    if args.row == "tune":
+        return run_tune(args)
     if args.row != "heff":
         return run_row(args)
     return run_su2g(args)

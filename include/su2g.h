@@ -112,6 +112,18 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
 /* Reads and clears the plan's device error word (the split-precision kernels
  * record a bounded wait that gave up there).  SU2G_ETIMEOUT if one did. */
 int su2g_heff_plan_status(su2g_heff_plan* plan, int* code);
+/* Tile shapes of the FP64 engine by block-size class (the autotuner of
+ * su2dmrg_gb300.autotune fills it from measurements; no counterpart in the
+ * reference, whose per-block loop tensor_su2_dmrg_src.cpp:977-1006 calls one
+ * DGEMM per block).  Buckets: M <= m_edges[i] (i < nm), N <= n_edges[j], the
+ * last bucket of each open-ended; cls[i * nn + j] in 0..3 = tiles of 64 x 64,
+ * 64 x 32, 32 x 64, 32 x 32.  Plans built afterwards use it; without a table
+ * every block uses 64 x 64. */
+int su2g_f64_tile_table(const int* m_edges, int nm, const int* n_edges, int nn, const int* cls);
+/* The autotuner's measurement: nblocks independent M x N x K block products
+ * in tiles of class cls, one launch, repeated reps times; *ms = device
+ * milliseconds per launch. */
+int su2g_f64_tile_bench(int M, int N, int K, int nblocks, int cls, int reps, double* ms, void* stream);
 /* Test hook, no counterpart in the reference: stores a nonzero `code` in the
  * plan's error word from the host, as a device wait that gave up would, so a
  * test can check on the CPU side, without any device fault, that every later

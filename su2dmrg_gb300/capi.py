@@ -73,6 +73,8 @@ _PROTOS = {
     "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp, _vp]),
     "su2g_heff_plan_status": (_i, [_vp, _vp]),
     "su2g_heff_plan_mark_failed": (_i, [_vp, _i]),
+    "su2g_f64_tile_table": (_i, [_vp, _i, _vp, _i, _vp]),
+    "su2g_f64_tile_bench": (_i, [_i, _i, _i, _i, _i, _i, _vp, _vp]),
     "su2g_heff_batch_create": (_i, [_vp, _i, _vp]),
     "su2g_heff_batch_destroy": (_i, [_vp]),
     "su2g_heff_batch_info": (_i, [_vp, _vp, _vp]),

@@ -437,6 +437,82 @@ int su2g_heff_plan_status(su2g_heff_plan* p, int* code) {
   return SU2G_OK;
 }
 
+int su2g_f64_tile_table(const int* m_edges, int nm, const int* n_edges, int nn, const int* cls) {
+  if (nm <= 0 || nn <= 0 || !m_edges || !n_edges || !cls) return fail(SU2G_EINVAL, "f64_tile_table: bad arguments");
+  if (su2g::set_tile_table(m_edges, nm, n_edges, nn, cls))
+    return fail(SU2G_EINVAL, "f64_tile_table: edges must increase and classes lie in 0..3");
+  return SU2G_OK;
+}
+
+int su2g_f64_tile_bench(int M, int N, int K, int nblocks, int cls, int reps, double* ms, void* stream) {
+  if (M <= 0 || N <= 0 || K <= 0 || nblocks <= 0 || cls < 0 || cls >= su2g::kTileClasses || reps <= 0 || !ms)
+    return fail(SU2G_EINVAL, "f64_tile_bench: bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t na = (int64_t)M * K, nb = (int64_t)K * N, nc = (int64_t)M * N;
+  double* buf = nullptr;
+  SU2G_CUDA(dalloc(&buf, (size_t)nblocks * (na + nb + nc) * sizeof(double)));
+  std::vector<su2g::GemmSeg> segs;
+  std::vector<su2g::GemmTile> tiles;
+  const int tm = su2g::kTileClassM[cls], tn = su2g::kTileClassN[cls];
+  for (int b = 0; b < nblocks; ++b) {
+    const int64_t base = (int64_t)b * (na + nb + nc);
+    su2g::GemmSeg g{};
+    g.a = base;
+    g.b = base + na;
+    g.a_len = na;
+    g.b_len = nb;
+    g.a_buf = g.b_buf = su2g::kBufScratch;
+    g.lda = M;
+    g.ldb = K;
+    g.K = K;
+    g.transA = 0;
+    g.alpha = 1.0;
+    segs.push_back(g);
+    for (int m0 = 0; m0 < M; m0 += tm)
+      for (int n0 = 0; n0 < N; n0 += tn) {
+        su2g::GemmTile t{};
+        t.c = base + na + nb;
+        t.c_len = nc;
+        t.c_buf = su2g::kBufScratch;
+        t.ldc = M;
+        t.m0 = m0;
+        t.n0 = n0;
+        t.mlen = std::min(tm, M - m0);
+        t.nlen = std::min(tn, N - n0);
+        t.seg0 = b;
+        t.nseg = 1;
+        t.kwork = K;
+        t.cls = cls;
+        tiles.push_back(t);
+      }
+  }
+  su2g::GemmSeg* dseg = nullptr;
+  su2g::GemmTile* dtile = nullptr;
+  cudaError_t e = cudaMemsetAsync(buf, 0, (size_t)nblocks * (na + nb + nc) * sizeof(double), st);
+  if (e == cudaSuccess) e = upload(segs, &dseg);
+  if (e == cudaSuccess) e = upload(tiles, &dtile);
+  su2g::Bases bases{};
+  bases.p[su2g::kBufScratch] = reinterpret_cast<uintptr_t>(buf);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = su2g::launch_gemm_f64(dtile, (int)tiles.size(), dseg, bases, st);  // warm
+  if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+  for (int r = 0; r < reps && e == cudaSuccess; ++r) e = su2g::launch_gemm_f64(dtile, (int)tiles.size(), dseg, bases, st);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float t = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  su2g::dev_free(dseg, st);
+  su2g::dev_free(dtile, st);
+  su2g::dev_free(buf, st);
+  if (e != cudaSuccess) return cuda_fail(e, "f64_tile_bench");
+  *ms = t / reps;
+  return SU2G_OK;
+}
+
 int su2g_heff_plan_mark_failed(su2g_heff_plan* p, int code) {
   if (!p || !p->d_err || code == 0) return fail(SU2G_EINVAL, "plan_mark_failed: bad arguments");
   SU2G_CUDA(cudaMemcpyAsync(p->d_err, &code, sizeof(int), cudaMemcpyHostToDevice, p->last_st));

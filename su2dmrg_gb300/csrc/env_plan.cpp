@@ -66,26 +66,6 @@ int parse_dev(const su2g_tensor& t, int legs, Struct* s, uintptr_t* base, const 
 
 int64_t abs_off(uintptr_t base, int64_t elem) { return (int64_t)(base / 8) + elem; }
 
-void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int64_t c_len, int c_buf, int ldc, int M, int N, int seg0,
-               int nseg, int64_t kwork) {
-  for (int m0 = 0; m0 < M; m0 += kTileM)
-    for (int n0 = 0; n0 < N; n0 += kTileN) {
-      GemmTile t;
-      t.c = c_off;
-      t.c_len = c_len;
-      t.c_buf = c_buf;
-      t.ldc = ldc;
-      t.m0 = m0;
-      t.n0 = n0;
-      t.mlen = std::min(kTileM, M - m0);
-      t.nlen = std::min(kTileN, N - n0);
-      t.seg0 = seg0;
-      t.nseg = nseg;
-      t.kwork = kwork;
-      tiles.push_back(t);
-    }
-}
-
 struct Contrib {
   int job;
   int xj;  // X block, -1: none (U^T V)

@@ -41,6 +41,8 @@ struct GemmTile {
   int mlen, nlen; // rows / columns of this tile (<= tile size)
   int seg0, nseg; // segments [seg0, seg0 + nseg)
   int64_t kwork;  // sum of K over the segments (scheduling weight)
+  int cls;        // tile class (kTileClassM/N): the FP64 engine's tile shape
+  int pad;
 };
 
 struct Bases {
@@ -54,7 +56,13 @@ inline double* resolve(const Bases& b, int buf, int64_t off) {
   return reinterpret_cast<double*>(b.p[buf] + (uintptr_t)(off * 8));
 }
 
-constexpr int kTileM = 64;
+constexpr int kTileM = 64;  // largest tile
 constexpr int kTileN = 64;
+// Tile classes of the FP64 engine: 64x64, 64x32, 32x64, 32x32.  Which class an
+// output block uses follows its size class (a table an autotuner fills from
+// measurements, tile_class_for in heff_plan.cpp).
+constexpr int kTileClasses = 4;
+constexpr int kTileClassM[kTileClasses] = {64, 64, 32, 32};
+constexpr int kTileClassN[kTileClasses] = {64, 32, 64, 32};
 
 }  // namespace su2g

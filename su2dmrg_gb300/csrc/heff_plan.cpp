@@ -2,6 +2,7 @@
 #include "heff_plan.hpp"
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 
@@ -42,29 +43,64 @@ int parse_tensor(const su2g_tensor& t, int want_legs, Op* op, const char* what, 
   return SU2G_OK;
 }
 
+int64_t abs_off(uintptr_t base, int64_t elem_off) { return (int64_t)(base / 8) + elem_off; }
+
+}  // namespace
+
+// ---- tile classes by block size (filled by the autotuner; default 64 x 64) ----
+namespace {
+std::mutex g_tile_mu;
+std::vector<int> g_tile_m_edges, g_tile_n_edges, g_tile_cls;  // buckets: size <= edge
+}  // namespace
+
+int set_tile_table(const int* m_edges, int nm, const int* n_edges, int nn, const int* cls) {
+  std::vector<int> me(m_edges, m_edges + nm), ne(n_edges, n_edges + nn), c(cls, cls + (size_t)nm * nn);
+  for (int v : c)
+    if (v < 0 || v >= kTileClasses) return SU2G_EINVAL;
+  for (int i = 1; i < nm; ++i)
+    if (me[i] <= me[i - 1]) return SU2G_EINVAL;
+  for (int i = 1; i < nn; ++i)
+    if (ne[i] <= ne[i - 1]) return SU2G_EINVAL;
+  std::lock_guard<std::mutex> lock(g_tile_mu);
+  g_tile_m_edges.swap(me);
+  g_tile_n_edges.swap(ne);
+  g_tile_cls.swap(c);
+  return SU2G_OK;
+}
+
+int tile_class_for(int M, int N) {
+  std::lock_guard<std::mutex> lock(g_tile_mu);
+  if (g_tile_cls.empty()) return 0;
+  auto bucket = [](const std::vector<int>& edges, int v) {
+    int b = 0;
+    while (b + 1 < (int)edges.size() && v > edges[b]) ++b;
+    return b;
+  };
+  return g_tile_cls[(size_t)bucket(g_tile_m_edges, M) * g_tile_n_edges.size() + bucket(g_tile_n_edges, N)];
+}
+
 void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int64_t c_len, int c_buf, int ldc, int M, int N,
                int seg0, int nseg, int64_t kwork) {
-  for (int m0 = 0; m0 < M; m0 += kTileM)
-    for (int n0 = 0; n0 < N; n0 += kTileN) {
-      GemmTile t;
+  const int cls = tile_class_for(M, N);
+  const int tm = kTileClassM[cls], tn = kTileClassN[cls];
+  for (int m0 = 0; m0 < M; m0 += tm)
+    for (int n0 = 0; n0 < N; n0 += tn) {
+      GemmTile t{};
       t.c = c_off;
       t.c_len = c_len;
       t.c_buf = c_buf;
       t.ldc = ldc;
       t.m0 = m0;
       t.n0 = n0;
-      t.mlen = std::min(kTileM, M - m0);
-      t.nlen = std::min(kTileN, N - n0);
+      t.mlen = std::min(tm, M - m0);
+      t.nlen = std::min(tn, N - n0);
       t.seg0 = seg0;
       t.nseg = nseg;
       t.kwork = kwork;
+      t.cls = cls;
       tiles.push_back(t);
     }
 }
-
-int64_t abs_off(uintptr_t base, int64_t elem_off) { return (int64_t)(base / 8) + elem_off; }
-
-}  // namespace
 
 int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                     const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, HeffWork* out,
@@ -327,7 +363,8 @@ int64_t last_index(int64_t r0, int64_t nr, int64_t c0, int64_t nc, int64_t ld) {
 int check_list(const std::vector<GemmTile>& tiles, const std::vector<GemmSeg>& segs, const HeffWork& w,
                const char* phase, std::string* err) {
   for (const GemmTile& t : tiles) {
-    if (t.mlen <= 0 || t.nlen <= 0 || t.mlen > kTileM || t.nlen > kTileN || t.m0 < 0 || t.n0 < 0 ||
+    if (t.cls < 0 || t.cls >= kTileClasses || t.mlen <= 0 || t.nlen <= 0 || t.mlen > kTileClassM[t.cls] ||
+        t.nlen > kTileClassN[t.cls] || t.m0 < 0 || t.n0 < 0 ||
         !within(t.c, t.c_len, t.c_buf, w) || last_index(t.m0, t.mlen, t.n0, t.nlen, t.ldc) >= t.c_len ||
         t.ldc < t.m0 + t.mlen || t.seg0 < 0 || t.nseg < 0 || t.seg0 + t.nseg > (int)segs.size()) {
       *err = std::string(phase) + ": tile out of bounds";

@@ -33,6 +33,15 @@ struct OutBlock {
   int seg0, nseg;
 };
 
+// Tile classes by output-block size (see kTileClassM/N): the table maps size
+// buckets (M <= m_edges[i], N <= n_edges[j], the last bucket open-ended) to a
+// class; without a table every block uses 64 x 64 tiles.
+int set_tile_table(const int* m_edges, int nm, const int* n_edges, int nn, const int* cls);
+int tile_class_for(int M, int N);
+// the FP64 tiles of one M x N output block, in the class its size selects
+void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int64_t c_len, int c_buf, int ldc, int M, int N,
+               int seg0, int nseg, int64_t kwork);
+
 struct HeffWork {
   Struct psi;  // layout of psi and y
   std::vector<GemmSeg> seg1, seg2;

@@ -14,8 +14,7 @@ namespace su2g {
 namespace {
 
 constexpr int kBK = 16;       // K per shared-memory stage
-constexpr int kLds = 68;      // padded row (64 + 4 doubles): conflict-free fragment reads
-constexpr int kThreads = 128; // 4 warps, each a 32x32 quadrant of the 64x64 tile
+constexpr int kThreads = 128; // 4 warps, each a quadrant of the tile
 
 __device__ __forceinline__ void dmma_m8n8k4(double (&d)[2], double a, double b) {
   asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
@@ -23,85 +22,90 @@ __device__ __forceinline__ void dmma_m8n8k4(double (&d)[2], double a, double b) 
                : "d"(a), "d"(b));
 }
 
-// C_tile = sum_s alpha_s * op(A_s) B_s ; every segment is accumulated on its
-// own, scaled by its alpha and added (the reference scales each block product
-// by its recoupling factor before summing, tensor_su2_dmrg_src.cpp:997-1004).
-__global__ void __launch_bounds__(kThreads) gemm_f64_tiles(const GemmTile* __restrict__ tiles,
-                                                           const GemmSeg* __restrict__ segs, Bases bases) {
-  __shared__ double As[kBK][kLds];  // As[k][m]
-  __shared__ double Bs[kBK][kLds];  // Bs[k][n]
-  const GemmTile t = tiles[blockIdx.x];
+// One TM x TN output tile: C_tile = sum_s alpha_s * op(A_s) B_s; every
+// segment is accumulated on its own, scaled by its alpha and added (the
+// reference scales each block product by its recoupling factor before
+// summing, tensor_su2_dmrg_src.cpp:997-1004).  Warp w computes the quadrant
+// (w / 2, w % 2) of (TM / 2) x (TN / 2) as FM x FN fragments of 8 x 8.
+// Operands are staged K = 16 at a time in shared memory, rows padded by 4
+// doubles (conflict-free fragment reads).
+template <int TM, int TN>
+__device__ __forceinline__ void f64_tile(const GemmTile& t, const GemmSeg* __restrict__ segs, const Bases& bases,
+                                         double* __restrict__ As, double* __restrict__ Bs) {
+  constexpr int FM = TM / 16, FN = TN / 16;
+  constexpr int LA = TM + 4, LB = TN + 4;
+  constexpr int PA = TM / 8, PB = TN / 8;  // elements each thread stages per operand per stage
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int wm = (warp >> 1) * (TM / 2), wn = (warp & 1) * (TN / 2);
   const int fr = lane >> 2, fc = lane & 3;
 
-  double acc[4][4][2];
+  double acc[FM][FN][2];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < FM; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+    for (int j = 0; j < FN; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
 
   for (int s = t.seg0; s < t.seg0 + t.nseg; ++s) {
     const GemmSeg g = segs[s];
     const double* __restrict__ A = resolve(bases, g.a_buf, g.a);
     const double* __restrict__ B = resolve(bases, g.b_buf, g.b);
-    double sacc[4][4][2];
+    double sacc[FM][FN][2];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < FM; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) sacc[i][j][0] = sacc[i][j][1] = 0.0;
+      for (int j = 0; j < FN; ++j) sacc[i][j][0] = sacc[i][j][1] = 0.0;
 
     for (int k0 = 0; k0 < g.K; k0 += kBK) {
-      // ---- stage A (64 x 16) and B (16 x 64) into shared memory, zero padded ----
+      // ---- stage A (TM x 16) and B (16 x TN), zero padded ----
       if (g.transA) {  // A stored K x M: (k, m) at A[k + m*lda], contiguous in k
-        const int m = tid >> 1, kb = (tid & 1) * 8;
+        const int m = tid / (kBK / PA), kb = (tid % (kBK / PA)) * PA;
         const bool mok = m < t.mlen;
         const double* src = A + (int64_t)(t.m0 + m) * g.lda + k0 + kb;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < PA; ++i) {
           const int k = kb + i;
-          As[k][m] = (mok && k0 + k < g.K) ? __ldg(src + i) : 0.0;
+          As[k * LA + m] = (mok && k0 + k < g.K) ? __ldg(src + i) : 0.0;
         }
       } else {  // A stored M x K: (m, k) at A[m + k*lda], contiguous in m
-        const int k = tid >> 3, mb = (tid & 7) * 8;
+        const int k = tid >> 3, mb = (tid & 7) * PA;
         const bool kok = k0 + k < g.K;
         const double* src = A + (int64_t)(k0 + k) * g.lda + t.m0 + mb;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < PA; ++i) {
           const int m = mb + i;
-          As[k][m] = (kok && m < t.mlen) ? __ldg(src + i) : 0.0;
+          As[k * LA + m] = (kok && m < t.mlen) ? __ldg(src + i) : 0.0;
         }
       }
       {  // B stored K x N: (k, n) at B[k + n*ldb], contiguous in k
-        const int n = tid >> 1, kb = (tid & 1) * 8;
+        const int n = tid / (kBK / PB), kb = (tid % (kBK / PB)) * PB;
         const bool nok = n < t.nlen;
         const double* src = B + (int64_t)(t.n0 + n) * g.ldb + k0 + kb;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < PB; ++i) {
           const int k = kb + i;
-          Bs[k][n] = (nok && k0 + k < g.K) ? __ldg(src + i) : 0.0;
+          Bs[k * LB + n] = (nok && k0 + k < g.K) ? __ldg(src + i) : 0.0;
         }
       }
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < kBK; kk += 4) {
-        double af[4], bf[4];
+        double af[FM], bf[FN];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) af[i] = As[kk + fc][wm + i * 8 + fr];
+        for (int i = 0; i < FM; ++i) af[i] = As[(kk + fc) * LA + wm + i * 8 + fr];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf[j] = Bs[kk + fc][wn + j * 8 + fr];
+        for (int j = 0; j < FN; ++j) bf[j] = Bs[(kk + fc) * LB + wn + j * 8 + fr];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < FM; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) dmma_m8n8k4(sacc[i][j], af[i], bf[j]);
+          for (int j = 0; j < FN; ++j) dmma_m8n8k4(sacc[i][j], af[i], bf[j]);
       }
       __syncthreads();
     }
     const double alpha = g.alpha;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < FM; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < FN; ++j) {
         acc[i][j][0] += alpha * sacc[i][j][0];
         acc[i][j][1] += alpha * sacc[i][j][1];
       }
@@ -109,11 +113,11 @@ __global__ void __launch_bounds__(kThreads) gemm_f64_tiles(const GemmTile* __res
 
   double* C = resolve(bases, t.c_buf, t.c);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < FM; ++i) {
     const int r = wm + i * 8 + fr;
     if (r >= t.mlen) continue;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < FN; ++j) {
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int c = wn + j * 8 + 2 * fc + q;
@@ -122,6 +126,32 @@ __global__ void __launch_bounds__(kThreads) gemm_f64_tiles(const GemmTile* __res
     }
   }
 }
+
+// One CTA per tile of the work list; the tile's class picks its shape (the
+// branch is uniform over the CTA).
+__global__ void __launch_bounds__(kThreads) gemm_f64_tiles(const GemmTile* __restrict__ tiles,
+                                                           const GemmSeg* __restrict__ segs, Bases bases) {
+  __shared__ double As[kBK * (kTileM + 4)];
+  __shared__ double Bs[kBK * (kTileN + 4)];
+  const GemmTile t = tiles[blockIdx.x];
+  switch (t.cls) {
+    case 1: f64_tile<64, 32>(t, segs, bases, As, Bs); break;
+    case 2: f64_tile<32, 64>(t, segs, bases, As, Bs); break;
+    case 3: f64_tile<32, 32>(t, segs, bases, As, Bs); break;
+    default: f64_tile<64, 64>(t, segs, bases, As, Bs); break;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
+                            cudaStream_t stream) {
+  if (ntiles <= 0) return cudaSuccess;
+  gemm_f64_tiles<<<ntiles, kThreads, 0, stream>>>(tiles, segs, bases);
+  return cudaGetLastError();
+}
+
+namespace {
 
 // ---------------------------------------------------------------- BLAS-1 --
 constexpr int kRedBlocks = 512;  // fixed: the summation order never depends on the device
@@ -168,13 +198,6 @@ __global__ void scale_kernel(double alpha, double* __restrict__ x, int64_t n) {
 }
 
 }  // namespace
-
-cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
-                            cudaStream_t stream) {
-  if (ntiles <= 0) return cudaSuccess;
-  gemm_f64_tiles<<<ntiles, kThreads, 0, stream>>>(tiles, segs, bases);
-  return cudaGetLastError();
-}
 
 int reduction_scratch_doubles() { return kRedBlocks + 1; }
 
