@@ -97,7 +97,10 @@ int su2g_fac_operator_transformation(int side, int j, int m, int l, int i, int k
  * terms (tensor_su2.cpp:1255-1345, called at dmrg_su2.cpp:563-570).
  * psi_desc/psi_flag describe psi and y (2 legs, locspin 0).  hl/hr may be
  * NULL.  Operator data pointers are captured and must stay valid until the plan
- * is destroyed.  Allocates the work list and its scratch on the device. */
+ * is destroyed; their contents must be complete when the plan is created (in
+ * split mode the operators are split into digit slices here, on a stream of
+ * the library's own: synchronise the stream that wrote them first).
+ * Allocates the work list and its scratch on the device. */
 int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                           const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
                           su2g_heff_plan** plan);

@@ -142,6 +142,9 @@ def lib():
             fn.restype = res
             fn.argtypes = args
         _lib = L
+        from . import autotune
+
+        autotune.load()  # the FP64 engine's tile table measured on GB300 (shipped with the package)
     return _lib
 
 

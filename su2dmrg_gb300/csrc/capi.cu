@@ -67,8 +67,13 @@ su2g::Bases make_bases(const su2g_heff_plan* p, const double* psi, double* y) {
 }
 
 // device buffers of the split-precision work, and the one-time packing of
-// the operators (they stay fixed for the lifetime of the plan)
-cudaError_t setup_split(su2g_heff_plan* p) {
+// the operators (they stay fixed for the lifetime of the plan).  The pack
+// reads the caller's operator data: with `caller` given (the one-shot work
+// lists, whose operands may still be in flight on the caller's stream, such
+// as transposes queued just before) it runs on that stream, ordered after
+// them; without (su2g_heff_plan_create, whose operands must be complete) on
+// the thread's own stream, waited for.
+cudaError_t setup_split(su2g_heff_plan* p, const cudaStream_t* caller) {
   su2g::oz::OzWork& w = p->oz;
   cudaError_t e = dalloc(&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
   if (e == cudaSuccess) e = dalloc(&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
@@ -88,11 +93,12 @@ cudaError_t setup_split(su2g_heff_plan* p) {
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
   cudaStream_t st = nullptr;
-  e = su2g::setup_stream(&st);
+  if (caller) st = *caller;
+  else e = su2g::setup_stream(&st);
   if (e == cudaSuccess)
     e = su2g::oz::launch_pack(p->S, p->d_jobs[0], p->d_units[0], (int)w.units[0].size(), w.max_nkt[0],
                               w.rows_pass[0], b, p->d_packed, p->d_exps, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && !caller) e = cudaStreamSynchronize(st);
   // the GEMM's one-time setup happens here, never inside a graph capture
   if (e == cudaSuccess) e = su2g::oz::prepare_ozaki_gemm(p->S);
   return e;
@@ -178,7 +184,7 @@ int su2g_fac_operator_transformation(int side, int j, int m, int l, int i, int k
 namespace {
 // device side of a plan whose host work lists are built: work lists, scratch
 // (intermediates + split partial tiles) and, in split mode, the packed operands
-int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
+int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan, const cudaStream_t* caller = nullptr) {
   *plan = nullptr;
   const int S = slices_of_mode(mode);
   if (S < 0) return fail(SU2G_EINVAL, "plan_create: unknown mode");
@@ -206,7 +212,8 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
     const int zero = 0;
     e = su2g::upload_bytes(&zero, sizeof(int), (void**)&p->d_err);
   }
-  if (e == cudaSuccess && S > 0) e = setup_split(p);
+  if (e == cudaSuccess && S > 0) e = setup_split(p, caller);
+  if (caller) p->last_st = *caller;
   if (e != cudaSuccess) {
     p->release();
     delete p;
@@ -223,7 +230,8 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan) {
 int su2g::run_work_once(HeffWork&& w, int mode, void* stream) {
   if (w.tile1.empty() && w.tile2.empty()) return SU2G_OK;
   su2g_heff_plan* p = nullptr;
-  int rc = plan_from_work(std::move(w), mode, &p);
+  const cudaStream_t st = (cudaStream_t)stream;
+  int rc = plan_from_work(std::move(w), mode, &p, &st);
   if (rc) return rc;
   rc = su2g_heff_apply(p, nullptr, nullptr, stream);
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);

@@ -379,18 +379,6 @@ void sector_finish(Ctx& c, const double* blk, int m, int n, double p1, double p2
   std::vector<double>& w = e.w;
   if (!c.ok()) return;
   int np = small_count(w, k);
-  // The levels whose whole subspace lies above the noise band change values
-  // and vectors only at rounding level: start the cascade at the subspace of
-  // the first pass's eigenvalues below 1e6 times its noise floor k eps
-  // lambda_max (the refinement then runs as the reference's from there).
-  // Measured on Gram matrices with 12-30 decades of spectrum: the kept values
-  // and vectors then differ from the full cascade's by less than the full
-  // cascade's own result moves when its input is perturbed by one rounding.
-  {
-    const double band = 1e6 * (double)k * 2.3e-16 * w[k - 1];
-    const int nb = (int)(std::lower_bound(w.begin(), w.begin() + k, band) - w.begin());
-    if (nb < np) np = nb;
-  }
   if (np > 1 && !(lam_cut > 0 && w[np - 1] < 0.1 * lam_cut)) {
     double* ap = c.dalloc((int64_t)k * k);
     double* vp = c.dalloc((int64_t)k * k);

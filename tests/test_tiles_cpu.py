@@ -13,7 +13,7 @@ def test_tile_table_rejects_bad_tables(su2lib):
         A.install({"m_edges": [], "n_edges": [], "cls": [4]})  # classes 0..3
     with pytest.raises(ValueError):
         A.install({"m_edges": [16], "n_edges": [], "cls": [0]})  # 2 x 1 buckets need 2 classes
-    A.reset()
+    A.load()
 
 
 @pytest.mark.parametrize("cls", [0, 1, 2, 3])
@@ -27,5 +27,5 @@ def test_tiled_work_lists_validate(su2lib, cls):
     ref = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr, mode=0)
     A.install({"m_edges": [20, 40], "n_edges": [30], "cls": [cls, 3 - cls, 0, cls, 1, 2]})
     got = HeffPlan.validate(w.psi, w.terms, w.hl, w.hr, mode=0)
-    A.reset()
+    A.load()
     assert got["flops"] == ref["flops"]

@@ -14,7 +14,7 @@ def tables(su2lib):
     from su2dmrg_gb300 import autotune as A
 
     yield A
-    A.reset()
+    A.load()
 
 
 @pytest.mark.parametrize("cls", [1, 2, 3])
