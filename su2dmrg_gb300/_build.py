@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["capi.cu", "devmem.cu", "heff_batch.cu", "kernels_f64.cu", "ozaki_pack.cu", "ozaki_gemm.cu", "noalloc.cu", "svd.cu", "combine.cu", "wavefunc.cu", "measure.cu"]
 CXX_SOURCES = ["su2_meta.cpp", "heff_plan.cpp", "ozaki_plan.cpp", "env_plan.cpp", "checkpoint.cpp"]
-LINK_LIBS = ["-lcudart", "-lcublas", "-lcusolver", "-lpthread"]
+LINK_LIBS = ["-lcudart", "-lcusolver", "-lpthread"]
 
 
 def _headers():

@@ -1,22 +1,28 @@
 // Truncation of a two-site vector (tensor_su2::svd, tensor_su2.cpp:1619-1758,
 // with the per-sector tensor::svd of tensor.cpp:1472-1700), on the GPU:
-//   * per sector, the Gram matrix of the smaller side (cuBLAS DGEMM) and its
-//     FP64 eigendecomposition (cuSOLVER syevd, eigenvalues ascending like
-//     dsyev), then the reference's refinement: while more than one eigenvalue
+//   * per sector, the Gram matrix of the smaller side and its FP64
+//     eigendecomposition (cuSOLVER syevd in its deterministic mode,
+//     eigenvalues ascending like dsyev), then the reference's refinement:
+//     while more than one eigenvalue
 //     lies below 0.1 of the largest of the current subspace, re-diagonalise
 //     the original Gram matrix projected on that subspace;
 //   * the other factor by one more product, singular values = sqrt of the
 //     eigenvalues above 1e-100 of the largest, columns scaled by s^(p1-1) and
 //     s^p2 (or the mirror for wide blocks);
-//   * the sectors are independent: each runs on its own stream, cuBLAS /
-//     cuSOLVER handles and host thread (the refinement reads eigenvalues back
-//     between steps), so their eigendecompositions overlap on the GPU;
+//   * every product (Gram matrices, the refinement's projections and
+//     rotations, the other factor) runs on the library's FP64 tile engine,
+//     whose sums have a fixed order: the result of a truncation does not
+//     depend on what else shares the GPU (a library GEMM picks its internal
+//     implementation by the concurrent load, and near a cut in the rounding
+//     noise that changes which multiplets are kept);
+//   * the sectors are independent: each runs on its own stream, cuSOLVER
+//     handle and host thread (the refinement reads eigenvalues back between
+//     steps), so their eigendecompositions overlap on the GPU;
 //   * on the host: all kept singular values sorted by the Shell sort of
 //     sort2.f (dsort2, whose handling of equal values decides ties), the
 //     largest max_dcut multiplets kept (no (2j+1) weighting), and the
 //     singular values reported kept-then-discarded as the reference writes
 //     them.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
@@ -35,6 +41,7 @@
 #include <thread>
 #include <vector>
 
+#include "heff_plan.hpp"
 #include "kernels.hpp"
 #include "su2_meta.hpp"
 #include "su2g.h"
@@ -48,6 +55,21 @@ __global__ void scale_columns(double* a, int rows, int c0, int ncol, int ld, con
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(idx % rows), c = (int)(idx / rows);
     a[(int64_t)(c0 + c) * ld + r] *= f[c];
+  }
+}
+
+// out (cols x rows) = in^T, 32 x 32 tiles through shared memory
+__global__ void transpose_kernel(const double* __restrict__ in, int rows, int cols, double* __restrict__ out) {
+  __shared__ double t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = r0 + threadIdx.x, c = c0 + j;
+    if (r < rows && c < cols) t[j][threadIdx.x] = in[(int64_t)c * rows + r];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int c = c0 + threadIdx.x, r = r0 + j;
+    if (r < rows && c < cols) out[(int64_t)r * cols + c] = t[threadIdx.x][j];
   }
 }
 
@@ -90,7 +112,6 @@ __global__ void __launch_bounds__(256) canonical_signs_kernel(double* z, int row
 // allocation without device-wide synchronisation, unlike cudaMalloc).
 struct Lane {
   cudaStream_t st = nullptr;
-  cublasHandle_t blas = nullptr;
   cusolverDnHandle_t sol = nullptr;
   cudaEvent_t done = nullptr;
 };
@@ -131,14 +152,20 @@ std::string take_lanes(int dev, int n, std::vector<Lane>* out, cudaMemPool_t* po
       cudaStreamDestroy(l.st);
       return "cannot create an event";
     }
-    if (cublasCreate(&l.blas) != CUBLAS_STATUS_SUCCESS || cusolverDnCreate(&l.sol) != CUSOLVER_STATUS_SUCCESS) {
-      if (l.blas) cublasDestroy(l.blas);
+    if (cusolverDnCreate(&l.sol) != CUSOLVER_STATUS_SUCCESS) {
       cudaEventDestroy(l.done);
       cudaStreamDestroy(l.st);
-      return "cannot create cuBLAS/cuSOLVER handles";
+      return "cannot create a cuSOLVER handle";
     }
-    cublasSetStream(l.blas, l.st);
     cusolverDnSetStream(l.sol, l.st);
+    // the eigensolver's deterministic mode: a truncation's result must not
+    // depend on what else runs on the GPU
+    if (cusolverDnSetDeterministicMode(l.sol, CUSOLVER_DETERMINISTIC_RESULTS) != CUSOLVER_STATUS_SUCCESS) {
+      cusolverDnDestroy(l.sol);
+      cudaEventDestroy(l.done);
+      cudaStreamDestroy(l.st);
+      return "cannot set the eigensolver's deterministic mode";
+    }
     out->push_back(l);
   }
   return "";
@@ -217,7 +244,6 @@ struct Ctx {
   cudaStream_t st = nullptr;
   cudaStream_t free_st = nullptr;
   cudaMemPool_t pool = nullptr;
-  cublasHandle_t blas = nullptr;
   cusolverDnHandle_t sol = nullptr;
   std::vector<void*> allocs;
   std::string err;
@@ -246,12 +272,44 @@ struct Ctx {
     allocs.push_back(p);
     return (double*)p;
   }
-  void gemm(cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const double* a, int lda, const double* b,
-            int ldb, double* c, int ldc) {
-    if (!ok() || m == 0 || n == 0) return;
-    const double one = 1.0, zero = 0.0;
-    if (cublasDgemm(blas, ta, tb, m, n, k, &one, a, lda, b, ldb, &zero, c, ldc) != CUBLAS_STATUS_SUCCESS)
-      set(SU2G_ECUDA, "svd: cublasDgemm failed");
+  // C (M x N, ld ldc) = op(A) B with op(A) = A (M x K, ld lda) or, for
+  // transA, A^T with A stored K x M; B stored K x N (ld ldb).  The library's
+  // FP64 tile engine (gemm_f64_tiles): every element sums its K products in a
+  // fixed order, whatever else runs on the GPU.
+  void gemm(bool transA, int M, int N, int K, const double* A, int lda, const double* B, int ldb, double* C,
+            int ldc) {
+    if (!ok() || M == 0 || N == 0) return;
+    su2g::GemmSeg g{};
+    g.a = (int64_t)((uintptr_t)A / 8);
+    g.b = (int64_t)((uintptr_t)B / 8);
+    g.a_len = transA ? (int64_t)lda * M : (int64_t)lda * K;
+    g.b_len = (int64_t)ldb * N;
+    g.a_buf = g.b_buf = su2g::kBufAbs;
+    g.lda = lda;
+    g.ldb = ldb;
+    g.K = K;
+    g.transA = transA ? 1 : 0;
+    g.alpha = 1.0;
+    std::vector<su2g::GemmTile> tiles;
+    su2g::add_tiles(tiles, (int64_t)((uintptr_t)C / 8), (int64_t)ldc * N, su2g::kBufAbs, ldc, M, N, 0, 1, K);
+    su2g::GemmSeg* dseg = (su2g::GemmSeg*)dalloc((sizeof(su2g::GemmSeg) + 7) / 8);
+    su2g::GemmTile* dtile = (su2g::GemmTile*)dalloc((tiles.size() * sizeof(su2g::GemmTile) + 7) / 8);
+    if (!ok()) return;
+    // pageable sources: each copy returns once its bytes are staged
+    cudaError_t e = cudaMemcpyAsync(dseg, &g, sizeof(g), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dtile, tiles.data(), tiles.size() * sizeof(su2g::GemmTile), cudaMemcpyHostToDevice, st);
+    const su2g::Bases bases{};
+    if (e == cudaSuccess) e = su2g::launch_gemm_f64(dtile, (int)tiles.size(), dseg, bases, st);
+    if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
+  }
+  // out (cols x rows) = in^T (in: rows x cols, column-major)
+  void transpose(const double* in, int rows, int cols, double* out) {
+    if (!ok() || rows == 0 || cols == 0) return;
+    const dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(in, rows, cols, out);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
   }
   void copy(double* dst, const double* src, int64_t n) {
     if (!ok()) return;
@@ -260,42 +318,22 @@ struct Ctx {
   }
   // symmetric eigendecomposition in place (a: n x n, ld n), eigenvector signs
   // by the canonical rule; w: host eigenvalues
-  void eigh(double* a, int n, std::vector<double>* w, bool jacobi = false) {
+  void eigh(double* a, int n, std::vector<double>* w) {
     if (!ok()) return;
     int lwork = 0;
     double* dw = dalloc(n);
     if (!ok()) return;
-    syevjInfo_t jp = nullptr;
-    if (jacobi) {
-      if (cusolverDnCreateSyevjInfo(&jp) != CUSOLVER_STATUS_SUCCESS) {
-        set(SU2G_ECUDA, "svd: syevj info");
-        return;
-      }
-      if (cusolverDnDsyevj_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, &lwork,
-                                      jp) != CUSOLVER_STATUS_SUCCESS) {
-        cusolverDnDestroySyevjInfo(jp);
-        set(SU2G_ECUDA, "svd: syevj buffer query failed");
-        return;
-      }
-    } else if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw,
-                                           &lwork) != CUSOLVER_STATUS_SUCCESS) {
+    if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS) {
       set(SU2G_ECUDA, "svd: syevd buffer query failed");
       return;
     }
     double* work = dalloc(lwork);
     double* dinfo = dalloc(1);
-    if (!ok()) {
-      if (jp) cusolverDnDestroySyevjInfo(jp);
-      return;
-    }
-    const cusolverStatus_t cs =
-        jacobi ? cusolverDnDsyevj(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, work, lwork,
-                                  (int*)dinfo, jp)
-               : cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, work, lwork,
-                                  (int*)dinfo);
-    if (jp) cusolverDnDestroySyevjInfo(jp);
-    if (cs != CUSOLVER_STATUS_SUCCESS) {
-      set(SU2G_ECUDA, "svd: eigensolver failed");
+    if (!ok()) return;
+    if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, a, n, dw, work, lwork,
+                         (int*)dinfo) != CUSOLVER_STATUS_SUCCESS) {
+      set(SU2G_ECUDA, "svd: syevd failed");
       return;
     }
     w->assign(n, 0.0);
@@ -311,15 +349,6 @@ struct Ctx {
     else if (info != 0) set(SU2G_ECUDA, "svd: syevd did not converge (info " + std::to_string(info) + ")");
   }
 };
-
-// experiment: the refinement levels' eigendecompositions by Jacobi rotations
-bool refine_jacobi() {
-  static const bool on = [] {
-    const char* v = std::getenv("SU2G_SVD_REFINE_JACOBI");
-    return v && *v == '1';
-  }();
-  return on;
-}
 
 // index after the last eigenvalue below tol1 of the largest (tensor.cpp:1492-1497)
 int small_count(const std::vector<double>& w, int n) {
@@ -356,8 +385,13 @@ void sector_eig(Ctx& c, const double* blk, int m, int n, SectorEig* e) {
   e->G = c.dalloc((int64_t)k * k);
   e->A0 = c.dalloc((int64_t)k * k);
   if (!c.ok()) return;
-  if (e->tall) c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, blk, m, blk, m, e->G, n);
-  else c.gemm(CUBLAS_OP_N, CUBLAS_OP_T, m, m, n, blk, m, blk, m, e->G, m);
+  if (e->tall) {
+    c.gemm(true, n, n, m, blk, m, blk, m, e->G, n);  // blk^T blk
+  } else {  // blk blk^T = (blk^T)^T (blk^T)
+    double* bt = c.dalloc((int64_t)m * n);
+    c.transpose(blk, m, n, bt);
+    c.gemm(true, m, m, n, bt, n, bt, n, e->G, m);
+  }
   c.copy(e->A0, e->G, (int64_t)k * k);
   c.eigh(e->G, k, &e->w);  // G now holds the eigenvectors
 }
@@ -392,13 +426,13 @@ void sector_finish(Ctx& c, const double* blk, int m, int n, double p1, double p2
     std::vector<double> ws;
     do {
       e.levels.push_back(npp);
-      c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, npp, np, np, vp, np, ap, np, app, npp);
-      c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, npp, npp, np, app, npp, vp, np, vpp, npp);
+      c.gemm(true, npp, np, np, vp, np, ap, np, app, npp);
+      c.gemm(false, npp, npp, np, app, npp, vp, np, vpp, npp);
       c.copy(ap, vpp, (int64_t)npp * npp);
-      c.eigh(vpp, npp, &ws, refine_jacobi());
+      c.eigh(vpp, npp, &ws);
       if (!c.ok()) return;
       for (int q = 0; q < npp; ++q) w[q] = ws[q];
-      c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, k, npp, npp, G, k, vpp, npp, tmp, k);
+      c.gemm(false, k, npp, npp, G, k, vpp, npp, tmp, k);
       c.copy(G, tmp, (int64_t)k * npp);
       c.copy(vp, vpp, (int64_t)npp * npp);
       const int j = small_count(ws, npp);
@@ -412,11 +446,11 @@ void sector_finish(Ctx& c, const double* blk, int m, int n, double p1, double p2
   if (tall) {  // V = eigenvectors (n x n), U = blk V (m x n)
     V = G;
     U = c.dalloc((int64_t)m * n);
-    c.gemm(CUBLAS_OP_N, CUBLAS_OP_N, m, n, n, blk, m, V, n, U, m);
+    c.gemm(false, m, n, n, blk, m, V, n, U, m);
   } else {  // U = eigenvectors (m x m), V = blk^T U (n x m)
     U = G;
     V = c.dalloc((int64_t)n * m);
-    c.gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, m, m, blk, m, U, m, V, n);
+    c.gemm(true, n, m, m, blk, m, U, m, V, n);
   }
   if (!c.ok()) return;
   // singular values above 1e-100 of the largest, scaling (tensor.cpp:1532-1567)
@@ -535,7 +569,6 @@ extern "C" int su2g_svd(const int* psi_desc, const int* psi_flag, const double* 
     c.st = lanes[q].st;
     c.free_st = cst;
     c.pool = pool;
-    c.blas = lanes[q].blas;
     c.sol = lanes[q].sol;
     const cudaError_t we = cudaStreamWaitEvent(c.st, ready, 0);  // psi is written on the caller's stream
     if (we != cudaSuccess) c.set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(we));

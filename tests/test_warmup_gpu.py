@@ -77,7 +77,11 @@ def _steps(w):
 def test_warmup_matches_reference_4x2(torch_cuda, mode):
     """J1 4x2 at D=16 with the engine's five Lanczos vectors: the eigenvalue
     of every step to 1e-10 relative and the last truncation's singular values
-    to 1e-8 (in split mode those above 1e-6 of the largest)."""
+    above 1e-6 of the largest to 1e-8.  D does not bind here, so the
+    truncation keeps every positive Gram eigenvalue above 1e-100 of the
+    largest, rounding-noise ones included (around 1e-9 as singular values):
+    how many of those there are depends on the GEMM's summation order, so
+    they are not compared."""
     from su2dmrg_gb300.warmup import Warmup
 
     g = np.load(os.path.join(GOLDEN, "warmup_0.npz"))
@@ -85,13 +89,8 @@ def test_warmup_matches_reference_4x2(torch_cuda, mode):
     e = w.run()
     assert abs(e - g["energy"]) <= 1e-10 * abs(g["energy"])
     assert np.allclose(_steps(w), g["step_energies"], rtol=1e-10, atol=0)
-    if mode == 0:
-        ww = np.zeros_like(g["ww"])
-        ww[: min(len(w.ww), len(ww))] = w.ww[: len(ww)]
-        assert np.allclose(ww, g["ww"], rtol=0, atol=1e-8)
-    else:
-        big = lambda v: np.sort(v[v > 1e-6 * np.max(v)])
-        assert np.allclose(big(np.asarray(w.ww)), big(g["ww"]), rtol=0, atol=1e-8)
+    big = lambda v: np.sort(v[v > 1e-6 * np.max(v)])
+    assert np.allclose(big(np.asarray(w.ww)), big(g["ww"]), rtol=0, atol=1e-8)
 
 
 @pytest.mark.parametrize("mode", [0, 1])
