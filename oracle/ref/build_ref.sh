@@ -25,8 +25,18 @@ if [ ! -f "$SRC/tensor_su2.cpp" ]; then
   # --if-present: a machine without the reference sources (the GPU hosts)
   # uses the committed fixtures instead; nothing to build there
   if [ "${1:-}" = "--if-present" ]; then exit 0; fi
+  if [ "${1:-}" = "--shim-check" ]; then exit 77; fi
   echo "build_ref.sh: reference sources not found at $SRC (set SU2REF_SRC)" >&2
   exit 2
+fi
+# --shim-check: compile include/su2g_tensor_su2_shim.hpp (the binding a
+# maintainer adds to the reference tree) against the reference's own headers
+if [ "${1:-}" = "--shim-check" ]; then
+  CHK="$(mktemp -d /tmp/su2shim.XXXXXX)"
+  trap 'rm -rf "$CHK"' EXIT
+  echo '#include "su2g_tensor_su2_shim.hpp"' > "$CHK/shim_check.cpp"
+  g++ -std=c++17 -fsyntax-only -Wall -I "$SRC" -I "$REPO/include" -I /usr/local/cuda/include "$CHK/shim_check.cpp"
+  exit $?
 fi
 WORK="$(mktemp -d /tmp/su2ref.XXXXXX)"
 trap 'rm -rf "$WORK"' EXIT
