@@ -44,6 +44,43 @@ template <class T>
 cudaError_t dalloc(T** dptr, size_t bytes) {
   return su2g::dev_alloc((void**)dptr, bytes);
 }
+
+// Host arrays gathered into one staging buffer (256-byte aligned pieces) and
+// sent to the device in one allocation and one copy: a plan's work lists
+// cost one transfer instead of one allocation, copy and wait each.
+struct Staging {
+  std::vector<uint8_t> host;
+  std::vector<std::pair<void**, size_t>> slots;
+  void add_bytes(const void* src, size_t n, void** slot) {
+    *slot = nullptr;
+    if (n == 0) return;
+    const size_t off = (host.size() + 255) & ~(size_t)255;
+    host.resize(off + n);
+    std::memcpy(host.data() + off, src, n);
+    slots.push_back({slot, off});
+  }
+  template <class T>
+  void add(const std::vector<T>& v, T** slot) {
+    add_bytes(v.data(), v.size() * sizeof(T), (void**)slot);
+  }
+  // with `caller`, the copy is queued on that stream (pageable source: it is
+  // staged before the call returns); else on the thread's own stream, waited for
+  cudaError_t send(void** base, const cudaStream_t* caller) {
+    *base = nullptr;
+    if (host.empty()) return cudaSuccess;
+    cudaError_t e = su2g::dev_alloc(base, host.size());
+    cudaStream_t st = nullptr;
+    if (e == cudaSuccess) {
+      if (caller) st = *caller;
+      else e = su2g::setup_stream(&st);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(*base, host.data(), host.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !caller) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (auto& sl : slots) *sl.first = static_cast<uint8_t*>(*base) + sl.second;
+    return cudaSuccess;
+  }
+};
 }  // namespace
 
 int su2g::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
@@ -77,19 +114,6 @@ cudaError_t setup_split(su2g_heff_plan* p, const cudaStream_t* caller) {
   su2g::oz::OzWork& w = p->oz;
   cudaError_t e = dalloc(&p->d_packed, std::max<int64_t>(w.packed_bytes, 16));
   if (e == cudaSuccess) e = dalloc(&p->d_exps, std::max<int64_t>(w.exp_len, 1) * sizeof(int));
-  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
-    e = upload(w.jobs[c], &p->d_jobs[c]);
-    if (e == cudaSuccess) {
-      std::vector<int2> u(w.units[c].size());
-      for (size_t i = 0; i < u.size(); ++i) u[i] = make_int2(w.units[c][i].job, w.units[c][i].rt);
-      e = upload(u, &p->d_units[c]);
-    }
-  }
-  if (e == cudaSuccess) e = upload(w.seg1, &p->d_oseg1);
-  if (e == cudaSuccess) e = upload(w.seg2, &p->d_oseg2);
-  if (e == cudaSuccess) e = upload(w.tile1, &p->d_otile1);
-  if (e == cudaSuccess) e = upload(w.tile2, &p->d_otile2);
-  if (e == cudaSuccess) e = upload(w.red2, &p->d_red2);
   if (e != cudaSuccess) return e;
   const su2g::Bases b = make_bases(p, nullptr, nullptr);
   cudaStream_t st = nullptr;
@@ -200,18 +224,35 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan, const
       return fail(rc, err);
     }
   }
-  cudaError_t e = upload(p->work.seg1, &p->d_seg1);
-  if (e == cudaSuccess) e = upload(p->work.seg2, &p->d_seg2);
-  if (e == cudaSuccess) e = upload(p->work.tile1, &p->d_tile1);
-  if (e == cudaSuccess) e = upload(p->work.tile2, &p->d_tile2);
+  // every work list of the mode and the error word (set by a bounded device
+  // wait that gave up, read by su2g_heff_plan_status and every
+  // result-returning caller of the plan) in one block and one copy
+  Staging stage;
+  const int zero = 0;
+  stage.add_bytes(&zero, sizeof(int), (void**)&p->d_err);
+  std::vector<int2> units[3];
+  if (S == 0) {
+    stage.add(p->work.seg1, &p->d_seg1);
+    stage.add(p->work.seg2, &p->d_seg2);
+    stage.add(p->work.tile1, &p->d_tile1);
+    stage.add(p->work.tile2, &p->d_tile2);
+  } else {
+    const su2g::oz::OzWork& w = p->oz;
+    for (int c = 0; c < 3; ++c) {
+      stage.add(w.jobs[c], &p->d_jobs[c]);
+      units[c].resize(w.units[c].size());
+      for (size_t i = 0; i < units[c].size(); ++i) units[c][i] = make_int2(w.units[c][i].job, w.units[c][i].rt);
+      stage.add(units[c], &p->d_units[c]);
+    }
+    stage.add(w.seg1, &p->d_oseg1);
+    stage.add(w.seg2, &p->d_oseg2);
+    stage.add(w.tile1, &p->d_otile1);
+    stage.add(w.tile2, &p->d_otile2);
+    stage.add(w.red2, &p->d_red2);
+  }
+  cudaError_t e = stage.send(&p->d_lists, caller);
   const int64_t scratch_doubles = p->work.scratch_len + p->oz.partial_len;
   if (e == cudaSuccess && scratch_doubles > 0) e = dalloc(&p->d_scratch, scratch_doubles * sizeof(double));
-  // the error word: set by a bounded device wait that gave up, read by
-  // su2g_heff_plan_status and every result-returning caller of the plan
-  if (e == cudaSuccess) {
-    const int zero = 0;
-    e = su2g::upload_bytes(&zero, sizeof(int), (void**)&p->d_err);
-  }
   if (e == cudaSuccess && S > 0) e = setup_split(p, caller);
   if (caller) p->last_st = *caller;
   if (e != cudaSuccess) {

@@ -33,6 +33,7 @@ struct su2g_heff_plan {
   su2g::oz::OzTile* d_otile2 = nullptr;
   su2g::oz::RedTile* d_red2 = nullptr;
   int* d_err = nullptr;
+  void* d_lists = nullptr;  // one device block holding every work list above and d_err
   // Lanczos workspace (allocated on first use)
   double* d_krylov = nullptr;
   int krylov_vectors = 0;
@@ -61,27 +62,18 @@ struct su2g_heff_plan {
   }
 
   void release() {
-    su2g::dev_free(d_seg1, last_st);
-    su2g::dev_free(d_seg2, last_st);
-    su2g::dev_free(d_tile1, last_st);
-    su2g::dev_free(d_tile2, last_st);
+    // the work lists and the error word lie in one block (d_lists)
+    su2g::dev_free(d_lists, last_st);
+    d_lists = nullptr;
     su2g::dev_free(d_scratch, last_st);
     su2g::dev_free(d_krylov, last_st);
     su2g::dev_free(d_red, last_st);
     su2g::dev_free(d_packed, last_st);
     su2g::dev_free(d_exps, last_st);
     for (int c = 0; c < 3; ++c) {
-      su2g::dev_free(d_jobs[c], last_st);
-      su2g::dev_free(d_units[c], last_st);
       d_jobs[c] = nullptr;
       d_units[c] = nullptr;
     }
-    su2g::dev_free(d_oseg1, last_st);
-    su2g::dev_free(d_oseg2, last_st);
-    su2g::dev_free(d_otile1, last_st);
-    su2g::dev_free(d_otile2, last_st);
-    su2g::dev_free(d_red2, last_st);
-    su2g::dev_free(d_err, last_st);
     su2g::dev_free(d_proj, last_st);
     d_proj = nullptr;
     drop_graphs();
