@@ -25,6 +25,11 @@ cudaError_t setup_stream(cudaStream_t* out);
 
 cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
                             cudaStream_t stream);
+// one dense product C (M x N, ld ldc) = op(A) B with the same tile code
+// (op(A) = A, M x K, or for transA A^T with A stored K x M; B stored K x N),
+// tiles of class cls, the work formed from the arguments
+cudaError_t launch_gemm_f64_dense(bool transA, int M, int N, int K, const double* A, int lda, const double* B,
+                                  int ldb, double* C, int ldc, int cls, cudaStream_t stream);
 
 // deterministic dot product: partial sums in scratch[0..reduction_scratch_doubles()-1),
 // the result in scratch[reduction_scratch_doubles()-1]

@@ -142,7 +142,58 @@ __global__ void __launch_bounds__(kThreads) gemm_f64_tiles(const GemmTile* __res
   }
 }
 
+// One dense product C = op(A) B in tiles of class cls, the tile and its
+// segment formed from the kernel's arguments (no work list to upload): the
+// same tile code, so the same sums in the same order as a work-list launch.
+__global__ void __launch_bounds__(kThreads) gemm_f64_dense(int transA, int M, int N, int K, const double* A, int lda,
+                                                           const double* B, int ldb, double* C, int ldc, int cls) {
+  __shared__ double As[kBK * (kTileM + 4)];
+  __shared__ double Bs[kBK * (kTileN + 4)];
+  GemmSeg g;
+  g.a = (int64_t)((uintptr_t)A / 8);
+  g.b = (int64_t)((uintptr_t)B / 8);
+  g.a_len = 0;
+  g.b_len = 0;
+  g.a_buf = g.b_buf = kBufAbs;
+  g.lda = lda;
+  g.ldb = ldb;
+  g.K = K;
+  g.transA = transA;
+  g.alpha = 1.0;
+  GemmTile t;
+  t.c = (int64_t)((uintptr_t)C / 8);
+  t.c_len = 0;
+  t.c_buf = kBufAbs;
+  t.ldc = ldc;
+  const int tm = cls == 2 || cls == 3 ? 32 : 64, tn = cls == 1 || cls == 3 ? 32 : 64;
+  t.m0 = blockIdx.x * tm;
+  t.n0 = blockIdx.y * tn;
+  t.mlen = min(tm, M - t.m0);
+  t.nlen = min(tn, N - t.n0);
+  t.seg0 = 0;
+  t.nseg = 1;
+  t.kwork = K;
+  t.cls = cls;
+  t.pad = 0;
+  const Bases bases{};
+  switch (cls) {
+    case 1: f64_tile<64, 32>(t, &g, bases, As, Bs); break;
+    case 2: f64_tile<32, 64>(t, &g, bases, As, Bs); break;
+    case 3: f64_tile<32, 32>(t, &g, bases, As, Bs); break;
+    default: f64_tile<64, 64>(t, &g, bases, As, Bs); break;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_gemm_f64_dense(bool transA, int M, int N, int K, const double* A, int lda, const double* B,
+                                  int ldb, double* C, int ldc, int cls, cudaStream_t stream) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  if (cls < 0 || cls >= kTileClasses) return cudaErrorInvalidValue;
+  const dim3 grid((M + kTileClassM[cls] - 1) / kTileClassM[cls], (N + kTileClassN[cls] - 1) / kTileClassN[cls]);
+  gemm_f64_dense<<<grid, kThreads, 0, stream>>>(transA ? 1 : 0, M, N, K, A, lda, B, ldb, C, ldc, cls);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_gemm_f64(const GemmTile* tiles, int ntiles, const GemmSeg* segs, const Bases& bases,
                             cudaStream_t stream) {

@@ -59,8 +59,15 @@ struct Builder {
   }
 };
 
+// The exact combination of a tile's group sums holds at most 2^17 contracted
+// values (and kMaxSegs products) per output tile.  A phase-2 block fed by more
+// (many terms at large D) is computed as partial tiles over runs of its
+// products, each within the bounds, written into scratch and summed in run
+// order by the reduction (RedTile), as the split tiles are.
+constexpr int64_t kMaxKPerTile = (int64_t)1 << 17;
+
 int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<OutBlock>& blks,
-                std::vector<OzSeg>* oseg, std::vector<OzTile>* otile, std::string* err) {
+                std::vector<OzSeg>* oseg, std::vector<OzTile>* otile, std::string* err, bool may_split) {
   const int S = B.S;
   for (const OutBlock& ob : blks) {
     // pack jobs of every product of this block
@@ -83,47 +90,85 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
       ids.push_back({ja, jb});
       bufs.push_back({g.a_buf, g.b_buf});
     }
-    int64_t ktot = 0;
-    for (int s = 0; s < ob.nseg; ++s) ktot += (int64_t)segs[ob.seg0 + s].K;
-    if (ktot >= (int64_t)1 << 17) {
-      *err = "split mode: more than 2^17 contracted values feed one output block";
-      return SU2G_EUNSUPPORTED;
+    // runs of products within the bounds of one tile (one run: the whole block)
+    std::vector<std::pair<int, int>> runs;  // (first product, count) relative to ob.seg0
+    {
+      int r0 = 0;
+      int64_t k = 0;
+      for (int s = 0; s < ob.nseg; ++s) {
+        const int64_t ks = segs[ob.seg0 + s].K;
+        if (ks >= kMaxKPerTile) {
+          *err = "split mode: one product contracts 2^17 values or more";
+          return SU2G_EUNSUPPORTED;
+        }
+        if (s > r0 && (k + ks >= kMaxKPerTile || s - r0 >= kMaxSegs)) {
+          runs.push_back({r0, s - r0});
+          r0 = s;
+          k = 0;
+        }
+        k += ks;
+      }
+      if (ob.nseg > 0) runs.push_back({r0, ob.nseg - r0});
     }
-    if (ob.nseg > kMaxSegs) {
-      *err = "split mode: more than 1024 products feed one output block";
+    if (runs.size() > 1 && !may_split) {
+      *err = "split mode: more than 2^17 contracted values or 1024 products feed one intermediate block";
       return SU2G_EUNSUPPORTED;
     }
     for (int m0 = 0; m0 < ob.M; m0 += kTM)
       for (int n0 = 0; n0 < ob.N; n0 += kTN) {
-        OzTile t;
-        t.c = ob.c;
-        t.c_buf = ob.c_buf;
-        t.ldc = ob.ldc;
-        t.m0 = m0;
-        t.n0 = n0;
-        t.mlen = std::min(kTM, ob.M - m0);
-        t.nlen = std::min(kTN, ob.N - n0);
-        t.seg0 = (int)oseg->size();
-        t.nseg = ob.nseg;
-        t.work = 0;
-        t.rowmax = -1;
-        t.rms = 1;
-        t.pad2 = 0;
-        for (int s = 0; s < ob.nseg; ++s) {
-          const PackJob& a = B.get(bufs[s].first, ids[s].first);
-          const PackJob& b = B.get(bufs[s].second, ids[s].second);
-          OzSeg z;
-          z.a_unit = a.dst + (int64_t)(m0 / kTM) * a.nkt * a_unit_bytes(S);
-          z.b_unit = b.dst + (int64_t)(n0 / kTN) * b.nkt * b_unit_bytes(S);
-          z.a_exp = a.exp + m0;
-          z.b_exp = b.exp + n0;
-          z.a_tmax = a.texp + m0 / kTM;
-          z.nks = a.nkt;
-          z.pad = 0;
-          t.work += z.nks;
-          oseg->push_back(z);
+        RedTile r{};
+        const bool parts = runs.size() > 1;
+        if (parts) {
+          r.c = ob.c;
+          r.c_buf = ob.c_buf;
+          r.ldc = ob.ldc;
+          r.m0 = m0;
+          r.n0 = n0;
+          r.mlen = std::min(kTM, ob.M - m0);
+          r.nlen = std::min(kTN, ob.N - n0);
+          r.part = B.w->scratch_base + B.w->partial_len;
+          r.nparts = (int)runs.size();
         }
-        otile->push_back(t);
+        for (const auto& run : runs) {
+          OzTile t;
+          t.c = ob.c;
+          t.c_buf = ob.c_buf;
+          t.ldc = ob.ldc;
+          t.m0 = m0;
+          t.n0 = n0;
+          t.mlen = std::min(kTM, ob.M - m0);
+          t.nlen = std::min(kTN, ob.N - n0);
+          if (parts) {  // a partial tile of the scratch (kTM x kTN, column-major)
+            t.c = B.w->scratch_base + B.w->partial_len;
+            t.c_buf = kBufScratch;
+            t.ldc = kTM;
+            t.m0 = 0;
+            t.n0 = 0;
+            B.w->partial_len += (int64_t)kTM * kTN;
+          }
+          t.seg0 = (int)oseg->size();
+          t.nseg = run.second;
+          t.work = 0;
+          t.rowmax = -1;
+          t.rms = 1;
+          t.pad2 = 0;
+          for (int s = run.first; s < run.first + run.second; ++s) {
+            const PackJob& a = B.get(bufs[s].first, ids[s].first);
+            const PackJob& b = B.get(bufs[s].second, ids[s].second);
+            OzSeg z;
+            z.a_unit = a.dst + (int64_t)(m0 / kTM) * a.nkt * a_unit_bytes(S);
+            z.b_unit = b.dst + (int64_t)(n0 / kTN) * b.nkt * b_unit_bytes(S);
+            z.a_exp = a.exp + m0;
+            z.b_exp = b.exp + n0;
+            z.a_tmax = a.texp + m0 / kTM;
+            z.nks = a.nkt;
+            z.pad = 0;
+            t.work += z.nks;
+            oseg->push_back(z);
+          }
+          otile->push_back(t);
+        }
+        if (parts) B.w->red2.push_back(r);
       }
   }
   return SU2G_OK;
@@ -138,7 +183,7 @@ void split_phase2(OzWork& w) {
   const int want = (kTargetCtas + ntiles - 1) / ntiles;
   std::vector<OzTile> out;
   for (const OzTile& t : w.tile2) {
-    const int parts = std::min(want, t.nseg);
+    const int parts = t.c_buf == kBufScratch ? 1 : std::min(want, t.nseg);  // partial tiles stay whole
     if (parts <= 1) {
       out.push_back(t);
       continue;
@@ -247,9 +292,9 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   B.lists[0] = &w.jobs[0];
   B.lists[1] = &w.jobs[1];
   B.lists[2] = &w.jobs[2];
-  int rc = build_phase(B, hw.seg1, hw.blk1, &w.seg1, &w.tile1, err);
+  int rc = build_phase(B, hw.seg1, hw.blk1, &w.seg1, &w.tile1, err, false);
   if (rc) return rc;
-  rc = build_phase(B, hw.seg2, hw.blk2, &w.seg2, &w.tile2, err);
+  rc = build_phase(B, hw.seg2, hw.blk2, &w.seg2, &w.tile2, err, true);
   if (rc) return rc;
   // Phase-1 outputs become phase-2 operands: when a phase-1 block feeds exactly
   // one unit-scaled pack job as its rows (row i = block columns i*rms ..

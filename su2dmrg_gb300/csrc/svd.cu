@@ -279,28 +279,8 @@ struct Ctx {
   void gemm(bool transA, int M, int N, int K, const double* A, int lda, const double* B, int ldb, double* C,
             int ldc) {
     if (!ok() || M == 0 || N == 0) return;
-    su2g::GemmSeg g{};
-    g.a = (int64_t)((uintptr_t)A / 8);
-    g.b = (int64_t)((uintptr_t)B / 8);
-    g.a_len = transA ? (int64_t)lda * M : (int64_t)lda * K;
-    g.b_len = (int64_t)ldb * N;
-    g.a_buf = g.b_buf = su2g::kBufAbs;
-    g.lda = lda;
-    g.ldb = ldb;
-    g.K = K;
-    g.transA = transA ? 1 : 0;
-    g.alpha = 1.0;
-    std::vector<su2g::GemmTile> tiles;
-    su2g::add_tiles(tiles, (int64_t)((uintptr_t)C / 8), (int64_t)ldc * N, su2g::kBufAbs, ldc, M, N, 0, 1, K);
-    su2g::GemmSeg* dseg = (su2g::GemmSeg*)dalloc((sizeof(su2g::GemmSeg) + 7) / 8);
-    su2g::GemmTile* dtile = (su2g::GemmTile*)dalloc((tiles.size() * sizeof(su2g::GemmTile) + 7) / 8);
-    if (!ok()) return;
-    // pageable sources: each copy returns once its bytes are staged
-    cudaError_t e = cudaMemcpyAsync(dseg, &g, sizeof(g), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dtile, tiles.data(), tiles.size() * sizeof(su2g::GemmTile), cudaMemcpyHostToDevice, st);
-    const su2g::Bases bases{};
-    if (e == cudaSuccess) e = su2g::launch_gemm_f64(dtile, (int)tiles.size(), dseg, bases, st);
+    const cudaError_t e =
+        su2g::launch_gemm_f64_dense(transA, M, N, K, A, lda, B, ldb, C, ldc, su2g::tile_class_for(M, N), st);
     if (e != cudaSuccess) set(SU2G_ECUDA, std::string("svd: ") + cudaGetErrorString(e));
   }
   // out (cols x rows) = in^T (in: rows x cols, column-major)

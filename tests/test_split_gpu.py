@@ -44,6 +44,29 @@ def test_split_matches_oracle(torch_cuda, oracle, mode, D, nspin1, spin0):
     assert _rel(y.cpu().numpy(), ref) <= TOL[mode]
 
 
+def test_split_block_fed_by_many_products(torch_cuda, oracle):
+    """1100 terms, each feeding every output block: more products than one
+    tile's exact combination holds, so each block is summed from partial
+    tiles in a fixed order; same tolerance as any 7-slice result."""
+    from su2dmrg_gb300.su2 import HeffPlan
+    from su2dmrg_gb300.workloads import synthetic_heff
+
+    torch = torch_cuda
+    w = synthetic_heff(D=8, nspin1=1100, seed=3, max2j=2)
+    psi, terms, hl, hr = w.to_device()
+    plan = HeffPlan(w.psi, terms, hl, hr, mode=1)
+    y = torch.empty_like(psi)
+    plan.apply(psi, y)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    ref = oracle.heff_apply(oracle.HeffProblem(w.psi, w.terms, w.hl, w.hr), w.psi_data)
+    assert _rel(y.cpu().numpy(), ref) <= TOL[1]
+    y2 = torch.empty_like(psi)
+    plan.apply(psi, y2)
+    torch.cuda.synchronize()
+    assert torch.equal(y, y2)
+
+
 def test_split_scaled_terms_and_zero_blocks(torch_cuda, oracle):
     """Coefficients folded into the operator slices, an all-zero psi block and
     an operator with no stored block."""
