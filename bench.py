@@ -71,6 +71,9 @@ def parse():
                     help="sweep row: nearest-neighbour coupling (diagonal 1 - |qdelta|; 2.0 = J2/J1 0.5)")
     ap.add_argument("--qdelta", type=float, default=0.0, help="sweep row: plaquette coupling Q")
     ap.add_argument("--skip-fp64", action="store_true", help="sweep row: time the split sweep only")
+    ap.add_argument("--step-log", action="store_true", help="sweep row: one stderr line per two-site step")
+    ap.add_argument("--offload", action="store_true",
+                    help="sweep row: block tensors of positions the sweep has passed live in host memory")
     ap.add_argument("--requests", type=int, default=32, help="serve row: requests of the stream served")
     ap.add_argument("--rate", type=float, default=2.0, help="serve row: Poisson arrival rate (solves per second)")
     ap.add_argument("--slots", type=int, default=8, help="serve row: solves in flight at most")
@@ -756,9 +759,27 @@ def run_sweep(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = Dmrg(lat, mode=split, seed=args.seed)
+    d.offload = args.offload
+    last = [0.0]
+    if args.step_log:  # one stderr line per sweep step: a run cut short still shows its step times
+
+        def log_step(il, ir, e):
+            torch.cuda.synchronize()
+            now = time.perf_counter()
+            print(json.dumps({"progress": "step", "il": il, "ir": ir, "seconds": now - last[0],
+                              "energy_per_site": e / lat.ns, "kept_multiplets": d.truncations[-1][2],
+                              "torch_hbm_gb": torch.cuda.memory_allocated() / 1e9,
+                              "host_resident_gb": getattr(d, "host_bytes", 0) / 1e9,
+                              "phase_seconds": dict(d.phase_seconds)}), file=sys.stderr, flush=True)
+            last[0] = now
+
+        d.step_hook = log_step
     e_prev = d.run()
     torch.cuda.synchronize()
     warm_s = time.perf_counter() - t0
+    last[0] = time.perf_counter()
+    print(json.dumps({"progress": "warmup", "seconds": warm_s, "energy_per_site": e_prev / lat.ns}),
+          file=sys.stderr, flush=True)
     e_warm = e_prev
     _, tline = _svd_trace_summary(trace, tline)
     before = []
@@ -801,6 +822,7 @@ def run_sweep(args):
             "config": {"workload": f"{lx}x{ly} cylinder, boundary 2, D={args.D}, sweep {len(before) + 1} "
                                    f"after the warm-up",
                        "row": "sweep", "two_site_steps": len(steps_split), "warmup_seconds": warm_s,
+                       "block_tensors": "host-resident once passed" if args.offload else "device-resident",
                        "warmup_energy_per_site": e_warm / lat.ns, "earlier_sweeps": before,
                        "converged_before_timed_sweep": bool(before and abs(before[-1]["delta_e"]) < 1e-6),
                        "sweep_energy_per_site_split": e_split / lat.ns,

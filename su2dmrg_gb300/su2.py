@@ -128,6 +128,8 @@ class _Pinned:
 
 
 def _tensor(struct: Su2Struct, data, keep: list) -> capi.Tensor:
+    if getattr(data, "is_cuda", True) is False:  # a torch tensor in host memory
+        raise ValueError("tensor data must be in device memory (numpy arrays for one-site operators)")
     p = _Pinned(struct)
     keep.append(p)
     return capi.Tensor(ptr(p.desc), ptr(p.flag), ptr(data))

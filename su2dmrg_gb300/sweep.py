@@ -23,7 +23,7 @@ import time
 import numpy as np
 
 from . import su2 as S
-from .warmup import Warmup
+from .warmup import Warmup, host_available_bytes
 
 
 class Dmrg(Warmup):
@@ -31,6 +31,7 @@ class Dmrg(Warmup):
     does not reach (dmrg_su2.cpp:54 sets 2)."""
 
     nfree = 2
+    step_hook = None  # called as step_hook(il, ir, energy) after each two-site step
 
     def clone(self, mode: int = None) -> "Dmrg":
         """A copy of the whole device state (MPS, block Hamiltonians, site and
@@ -39,7 +40,14 @@ class Dmrg(Warmup):
         def cp(t):
             return None if t is None else (t[0], t[1].clone())
 
+        host = sum(t[1].numel() * t[1].element_size() for row in self.opr + self.plq + [self.hh] for t in row
+                   if t is not None and not t[1].is_cuda)
+        if host and host > self.host_fraction * host_available_bytes():
+            raise MemoryError(f"clone: {host / 1e9:.1f} GB of host-resident block tensors do not fit the host")
         d = Dmrg(self.lat, mode=self.mode if mode is None else mode, mlanc=self.mlanc)
+        d.offload, d.host_fraction = self.offload, self.host_fraction
+        if hasattr(self, "host_bytes"):
+            d.host_bytes, d.host_cap, d._device = 2 * self.host_bytes, self.host_cap, getattr(self, "_device", None)
         d.ran_state = self.ran_state
         d.uu = [cp(t) for t in self.uu]
         d.hh = [cp(t) for t in self.hh]
@@ -88,11 +96,13 @@ class Dmrg(Warmup):
         self._keep.clear()
         t = self._timed("lanczos", t)
         self.energies.append((il, ir, e))
-        tu, xu, tv, xv, w = S.svd(vs, vx, self.uu[il][0], p1, self.uu[ir][0], p2, L.max_dcut)
+        tu, xu, tv, xv, w = self._freeing(S.svd, vs, vx, self.uu[il][0], p1, self.uu[ir][0], p2, L.max_dcut)
         self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
         self._timed("truncation", t)
         self.ww = w
         self.truncations.append((il, ir, int(sum(tu.bonds[2].dim)), np.asarray(w)))
+        if self.step_hook is not None:
+            self.step_hook(il, ir, e)
         return e
 
     def sweep(self) -> float:

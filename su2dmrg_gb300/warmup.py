@@ -209,6 +209,18 @@ def discarded_weight(kept: int, w) -> float:
     return float(np.sum(w[kept:] ** 2)) / tot if tot > 0 else 0.0
 
 
+def host_available_bytes() -> int:
+    """MemAvailable of the host (bytes), 0 when it cannot be read."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
 class Warmup:
     """do_idmrg on the device.  mode: capi.MODE_* for every contraction."""
 
@@ -229,10 +241,26 @@ class Warmup:
         self._keep = []
 
     # ---------------------------------------------------------- helpers
+    @staticmethod
+    def _freeing(f, *a, **k):
+        """f(*a, **k); when the library's device pool is refused memory, the
+        blocks torch keeps cached are returned to the device and f runs once
+        more (the two allocators share the HBM; every call retried here
+        leaves its inputs unchanged when it fails)."""
+        try:
+            return f(*a, **k)
+        except capi.Su2gError as e:
+            if e.code != capi.SU2G_ENOMEM:
+                raise
+            import torch
+
+            torch.cuda.empty_cache()
+            return f(*a, **k)
+
     def _run(self, u, flag, b: _Jobs):
         if not b.jobs:
             return {}
-        res = S.env_batch(u[0], u[1], u[0], u[1], flag, b.jobs, mode=self.mode)
+        res = self._freeing(S.env_batch, u[0], u[1], u[0], u[1], flag, b.jobs, mode=self.mode)
         return {name: (st, x[: st.size()]) for name, (st, x) in zip(b.names, res)}
 
     def _combine(self, lst):
@@ -248,6 +276,59 @@ class Warmup:
     @staticmethod
     def _legs01(u):
         return u[0].bonds[0], u[0].bonds[1]
+
+    # ------------------------------------------ host-resident block tensors
+    # offload: the block tensors stored at a position (its site operators,
+    # plaquette operators and block Hamiltonian) move to host memory once the
+    # sweep has passed it and come back when a site update or an H_eff reads
+    # them: the reference's memory_flag mode, which writes a position to disk
+    # after the update next to it (save_memory + release_memory_all,
+    # dmrg_su2_omp.cpp:449-450 and :591-592) and reads the one three sites
+    # ahead before each update (read_memory, :341 and :482), with host memory
+    # in place of files.  The bytes held on the host stay below host_fraction
+    # of the memory the host had available at the first move; past that,
+    # tensors stay on the device.
+    offload = False
+    host_fraction = 0.5
+
+    def _position_slots(self, p: int):
+        """(list, index) of every block tensor slot of position p."""
+        ns = self.lat.ns
+        return [(self.opr[p], k) for k in range(ns)] + [(self.plq[p], m) for m in range(2 * ns)] + [(self.hh, p)]
+
+    def _fetch(self, p: int) -> None:
+        """Brings the block tensors of position p to the device."""
+        if not self.offload or p < 0 or p >= self.lat.ns:
+            return
+        for lst, k in self._position_slots(p):
+            t = lst[k]
+            if t is not None and not t[1].is_cuda:
+                self.host_bytes -= t[1].numel() * t[1].element_size()
+                lst[k] = (t[0], t[1].to(self._device))
+
+    def _evict(self, p: int) -> None:
+        """Moves the block tensors of position p to host memory (within the cap)."""
+        if not self.offload or p < 0 or p >= self.lat.ns:
+            return
+        import torch
+
+        if not hasattr(self, "host_bytes"):
+            self.host_bytes = 0
+            self.host_cap = int(self.host_fraction * host_available_bytes())
+        moved = 0
+        for lst, k in self._position_slots(p):
+            t = lst[k]
+            if t is None or not t[1].is_cuda:
+                continue
+            nb = t[1].numel() * t[1].element_size()
+            if self.host_bytes + nb > self.host_cap:
+                continue
+            self._device = t[1].device
+            lst[k] = (t[0], t[1].to("cpu"))
+            self.host_bytes += nb
+            moved += nb
+        if moved:
+            torch.cuda.empty_cache()  # the freed blocks return to the device for the library's own pool
 
     def _release(self, p: int, lr: int) -> None:
         """release_memory2(p, lr) (dmrg_su2_omp.cpp:1804-1824), which the
@@ -281,6 +362,8 @@ class Warmup:
         if release:
             self._release(i + 1, 1)
             self._release(i + 2, 1)
+            self._fetch(i + 3)
+        self._fetch(i - 1)
         b = _Jobs()
         if self.hh[i - 1] is not None:
             b.add("hh", "overlap", x=self.hh[i - 1])
@@ -325,6 +408,8 @@ class Warmup:
                 self.opr[i][name[1]] = t
             elif isinstance(name, tuple):
                 self.plq[i][name[1]] = t
+        if release:
+            self._evict(i - 1)
 
     def site_right(self, i: int, u, release: bool = False):
         """prepare_site_operator_from_right(i[, flag]) with MPS tensor u at site
@@ -340,6 +425,8 @@ class Warmup:
         if release:
             self._release(i - 1, 0)
             self._release(i - 2, 0)
+            self._fetch(i - 3)
+        self._fetch(i + 1)
         b = _Jobs()
         if self.hh[i + 1] is not None:
             b.add("hh", "overlap", x=self.hh[i + 1])
@@ -385,6 +472,8 @@ class Warmup:
                 self.opr[i][name[1]] = t
             elif isinstance(name, tuple):
                 self.plq[i][name[1]] = t
+        if release:
+            self._evict(i + 1)
 
     # ------------------------------------------------------- two-site step
     # the Lanczos solve of a two-site step; a serving loop replaces it with
@@ -394,11 +483,13 @@ class Warmup:
     def eigensolve(self, plan, vx, mlanc: int):
         if self.lanczos_hook is not None:
             return self.lanczos_hook(plan, vx, mlanc)
-        return plan.lanczos(vx, mlanc=mlanc)
+        return self._freeing(plan.lanczos, vx, mlanc=mlanc)
 
     def heff_plan(self, il: int, ir: int, vs):
         """The terms of hamiltonian_vector_multiplication_idmrg (dmrg_su2.cpp:543-664)."""
         L, ns = self.lat, self.lat.ns
+        self._fetch(il)
+        self._fetch(ir)
         terms = []
 
         def term(a, b, coef):
@@ -433,7 +524,7 @@ class Warmup:
                     term(self.plq[il][m], self.opr[ir][q[3]], -L.qdelta)
         hl = (self.hh[il][0], self.hh[il][1], 1.0) if self.hh[il] is not None else None
         hr = (self.hh[ir][0], self.hh[ir][1], 1.0) if self.hh[ir] is not None else None
-        return S.HeffPlan(vs, terms, hl, hr, mode=self.mode)
+        return self._freeing(S.HeffPlan, vs, terms, hl, hr, mode=self.mode)
 
     def run(self):
         """do_idmrg: returns the eigenvalue of the last two-site step."""
@@ -465,7 +556,7 @@ class Warmup:
                 self._keep.clear()
                 self.energies.append((il, ir, e))
                 p1, p2 = (1.0, 0.0) if i == ns // 2 - 2 else (0.0, 0.0)
-                tu, xu, tv, xv, w = S.svd(vs, vx, ul[0], p1, ur[0], p2, L.max_dcut)
+                tu, xu, tv, xv, w = self._freeing(S.svd, vs, vx, ul[0], p1, ur[0], p2, L.max_dcut)
                 self.uu[il], self.uu[ir] = (tu, xu), (tv, xv)
                 self.ww = w
                 self.truncations.append((il, ir, int(sum(tu.bonds[2].dim)), np.asarray(w)))

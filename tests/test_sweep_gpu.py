@@ -100,3 +100,30 @@ def test_split_sweep_matches_fp64(torch_cuda, c):
             if x[2] != y[2]:
                 assert sum(x[2]) == sum(y[2]), i
                 assert abs(w0[i] - w1[i]) <= 1e-10, (i, w0[i], w1[i])
+
+
+@pytest.mark.parametrize("c", [1, 2])
+def test_host_resident_blocks_change_nothing(torch_cuda, c):
+    """Block tensors moved to host memory once the sweep has passed their
+    position (the reference's memory_flag mode, with host memory for its
+    files) and brought back when read: the same run, bit for bit, as with
+    every tensor on the device, on a J1-J2 and a J-Q lattice (plaquette
+    operators included)."""
+    from su2dmrg_gb300.sweep import Dmrg
+
+    lat = _lattice(c)
+    res = []
+    for offload in (False, True):
+        d = Dmrg(lat, mode=1, seed=7)
+        d.offload = offload
+        d.run()
+        moved = 0
+        for _ in range(2):
+            d.sweep()
+            moved = max(moved, getattr(d, "host_bytes", 0))
+        res.append((d, [e for _, _, e in d.energies], moved))
+    (d0, e0, _), (d1, e1, moved) = res
+    assert moved > 0
+    assert e0 == e1
+    for i in range(lat.ns):
+        assert torch_cuda.equal(d0.uu[i][1], d1.uu[i][1])
