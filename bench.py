@@ -927,7 +927,10 @@ def run_serve(args):
                        "requests": recs},
             "throughput": {"arrival_span_per_s": len(res) / span,
                            "note": "requests / (last completion - first arrival); equals the arrival rate "
-                                   "unless the server saturates"},
+                                   "unless the server saturates",
+                           "per_service_second": len(res) / float(sum(r.service for r in res)),
+                           "per_service_second_note": "requests / the sum of their service times (each "
+                                                      "solve's own start to finish; concurrent solves overlap)"},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max()), "sample": len(res)},
             "sequential": seq, "clocks": clk.summary(), "cpu_baseline": None}

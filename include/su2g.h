@@ -217,8 +217,10 @@ int su2g_heff_batch_lanczos(su2g_heff_batch* batch, double* const* psi, int mlan
  * file-scope device arrays (SU2G_NOALLOC_* below, about 40 MiB), held by every
  * GPU that loads libsu2g.so until the process exits; terms that need more are
  * refused with SU2G_EINVAL.  The first call on a device looks up the arrays'
- * device addresses (cudaGetSymbolAddress), so make it before any stream
- * capture.  Calls share the arrays.  Calls from several host threads on the
+ * device addresses (cudaGetSymbolAddress).  The call cannot be captured into
+ * a CUDA graph (it copies its work list from host memory it frees on
+ * return): on a capturing stream it returns SU2G_EUNSUPPORTED.  Calls share
+ * the arrays.  Calls from several host threads on the
  * same stream are safe: each call queues its copies and launches under a
  * per-device lock, so stream order keeps them apart.  Calls on different
  * streams race on the arrays and must be serialised by the caller.  Same

@@ -113,6 +113,11 @@ extern "C" int su2g_hamiltonian_vector_multiplication_noalloc(const int* vec_des
   std::vector<su2g::GemmSeg> segs(w.seg1);
   segs.insert(segs.end(), w.seg2.begin(), w.seg2.end());
   cudaStream_t st = (cudaStream_t)stream;
+  // the work list is copied from host vectors freed on return: a captured
+  // copy would replay from freed memory
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return fail(SU2G_EUNSUPPORTED, "noalloc: the stream is being captured; this entry point cannot be captured");
   std::lock_guard<std::mutex> call_lock(g_call_mu[dev]);
   // pageable sources: each call returns once its bytes are staged, so the
   // vectors may go out of scope afterwards

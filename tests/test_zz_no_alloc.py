@@ -165,3 +165,26 @@ def test_noalloc_refuses_terms_beyond_its_arrays(su2lib):
                torch.cuda.current_stream().cuda_stream)
     assert rc == capi.SU2G_EINVAL
     assert b"noalloc" in L.su2g_last_error()
+
+
+def test_noalloc_refuses_stream_capture(su2lib, oracle):
+    """The work list is copied from host memory that is freed on return, so a
+    captured call could only replay from freed memory: on a capturing stream
+    the entry point returns SU2G_EUNSUPPORTED and queues nothing."""
+    import torch
+
+    from su2dmrg_gb300 import capi
+
+    L = capi.lib()
+    vs, vx, s1, x1, s2, x2 = _cases(torch, oracle)[0]
+    y = torch.zeros_like(vx)
+    fn = L.su2g_hamiltonian_vector_multiplication_noalloc
+    capi.check(_call(fn, vs, vx, s1, x1, s2, x2, y, torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    codes = []
+    with torch.cuda.graph(g, stream=side):
+        codes.append(_call(fn, vs, vx, s1, x1, s2, x2, y, side.cuda_stream))
+    assert codes == [capi.SU2G_EUNSUPPORTED]
+    assert "captured" in L.su2g_last_error().decode()
