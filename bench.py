@@ -38,6 +38,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -746,7 +747,7 @@ def run_sweep(args):
     from su2dmrg_gb300.sweep import Dmrg
     from su2dmrg_gb300.warmup import Lattice
 
-    trace = os.environ.get("SU2G_SVD_TRACE") or os.path.join(REPO, "gpurun_out", "svd_trace.jsonl")
+    trace = os.environ.get("SU2G_SVD_TRACE") or os.path.join(tempfile.gettempdir(), "su2g_svd_trace.jsonl")
     os.makedirs(os.path.dirname(trace), exist_ok=True)
     open(trace, "w").close()
     os.environ["SU2G_SVD_TRACE"] = trace
