@@ -269,7 +269,10 @@ int plan_from_work(su2g::HeffWork&& work, int mode, su2g_heff_plan** plan, const
 // one application of a work list on absolute addresses: build, run, wait,
 // check, free
 int su2g::run_work_once(HeffWork&& w, int mode, void* stream) {
-  if (w.tile1.empty() && w.tile2.empty()) return SU2G_OK;
+  bool any = false;  // some block has a tile
+  for (const auto* v : {&w.blk1, &w.blk2})
+    for (const OutBlock& b : *v) any = any || (b.M > 0 && b.N > 0);
+  if (!any) return SU2G_OK;
   su2g_heff_plan* p = nullptr;
   const cudaStream_t st = (cudaStream_t)stream;
   int rc = plan_from_work(std::move(w), mode, &p, &st);
@@ -292,7 +295,7 @@ int env_batch_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2
   su2g::HeffWork w;
   std::vector<su2g::Struct> ys;
   std::string err;
-  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs, &w, &ys, &err);
+  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs, &w, &ys, &err, slices_of_mode(mode) == 0);
   if (rc) return fail(rc, err);
   return su2g::run_work_once(std::move(w), mode, stream);
 }
@@ -365,7 +368,8 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
   if (slices_of_mode(mode) < 0) return fail(SU2G_EINVAL, "plan_create: unknown mode");
   su2g::HeffWork w;
   std::string err;
-  const int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err);
+  const int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err,
+                                       slices_of_mode(mode) == 0);
   if (rc) return fail(rc, err);
   return plan_from_work(std::move(w), mode, plan);
 }
@@ -411,7 +415,7 @@ int su2g_env_validate(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const
   su2g::HeffWork w;
   std::vector<su2g::Struct> ys;
   std::string err;
-  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs.data(), &w, &ys, &err);
+  int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs.data(), &w, &ys, &err, S == 0);
   if (rc) return fail(rc, err);
   int64_t bytes = w.scratch_len * (int64_t)sizeof(double);
   if (S > 0) {
@@ -433,7 +437,7 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
   if (S < 0) return fail(SU2G_EINVAL, "plan_validate: unknown mode");
   su2g::HeffWork w;
   std::string err;
-  int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err);
+  int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err, S == 0);
   if (rc) return fail(rc, err);
   int64_t bytes = w.scratch_len * (int64_t)sizeof(double);
   if (S > 0) {

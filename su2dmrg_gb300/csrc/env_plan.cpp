@@ -129,7 +129,7 @@ Buckets bucket(const Struct& s, int l1, int l2 = -1) {
 
 int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int njobs, const su2g_env_job* jobs,
                     int nslots, double* const* outs, HeffWork* out, std::vector<Struct>* slot_structs,
-                    std::string* err) {
+                    std::string* err, bool fp64_tiles) {
   HeffWork& w = *out;
   w = HeffWork();
   slot_structs->clear();
@@ -442,7 +442,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
       g.alpha = 1.0;
       const int seg0 = (int)w.seg1.size();
       w.seg1.push_back(g);
-      add_tiles(w.tile1, w.scratch_len, (int64_t)Ap * C, kBufScratch, Ap, Ap, C, seg0, 1, A);
+      if (fp64_tiles) add_tiles(w.tile1, w.scratch_len, (int64_t)Ap * C, kBufScratch, Ap, Ap, C, seg0, 1, A);
       w.blk1.push_back(OutBlock{w.scratch_len, (int64_t)Ap * C, kBufScratch, Ap, Ap, C, seg0, 1});
       w.scratch_len += (int64_t)Ap * C;
       w.flops += 2.0 * A * (double)Ap * C;
@@ -489,7 +489,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
     }
     const int64_t yoff = abs_off(yb[sl], Y.offset[m] + (int64_t)C * os);
     const int64_t ylen = (int64_t)C * ms * Cp - (int64_t)C * os;
-    add_tiles(w.tile2, yoff, ylen, kBufAbs, C * ms, C, Cp, seg0, (int)w.seg2.size() - seg0, kwork);
+    if (fp64_tiles) add_tiles(w.tile2, yoff, ylen, kBufAbs, C * ms, C, Cp, seg0, (int)w.seg2.size() - seg0, kwork);
     w.blk2.push_back(OutBlock{yoff, ylen, kBufAbs, C * ms, C, Cp, seg0, (int)w.seg2.size() - seg0});
   }
   auto heavier = [](const GemmTile& x, const GemmTile& y) { return x.kwork > y.kwork; };
@@ -499,7 +499,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
 }
 
 int build_input_vector(const su2g_tensor& ul, const su2g_tensor& ur, const double* urt, double* out, Struct* vec,
-                       HeffWork* w, std::string* err) {
+                       HeffWork* w, std::string* err, bool fp64_tiles) {
   Struct L, R;
   uintptr_t lb = 0, rb = 0;
   int rc = parse_dev(ul, 3, &L, &lb, "input vector: ul", err, out != nullptr);
@@ -575,7 +575,7 @@ int build_input_vector(const su2g_tensor& ul, const su2g_tensor& ur, const doubl
             w->seg2.push_back(g);
             const int64_t coff = abs_off(ob, V.offset[vb] + row + (int64_t)col * ldc);
             const int64_t clen = (int64_t)(nr - 1) * ldc + ml;
-            add_tiles(w->tile2, coff, clen, kBufAbs, ldc, ml, nr, seg0, 1, dc);
+            if (fp64_tiles) add_tiles(w->tile2, coff, clen, kBufAbs, ldc, ml, nr, seg0, 1, dc);
             w->blk2.push_back(OutBlock{coff, clen, kBufAbs, ldc, ml, nr, seg0, 1});
             w->flops += 2.0 * ml * (double)nr * dc;
             w->max_k = std::max<int64_t>(w->max_k, dc);

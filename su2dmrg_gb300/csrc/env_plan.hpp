@@ -16,7 +16,7 @@ namespace su2g {
 // read on the host.
 int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int njobs, const su2g_env_job* jobs,
                     int nslots, double* const* outs, HeffWork* out, std::vector<Struct>* slot_structs,
-                    std::string* err);
+                    std::string* err, bool fp64_tiles = true);
 
 // The initial two-site vector of a step (dmrg_su2::prepare_input_vector,
 // dmrg_su2_omp.cpp:229-254) from ul = uu[il] and ur = uu[ir]: *vec gets the
@@ -27,7 +27,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
 // rows, at ur's offsets).  Output elements no product reaches are not
 // written (the caller zeroes them).
 int build_input_vector(const su2g_tensor& ul, const su2g_tensor& ur, const double* urt, double* out, Struct* vec,
-                       HeffWork* w, std::string* err);
+                       HeffWork* w, std::string* err, bool fp64_tiles = true);
 
 // Runs a work list on absolute addresses once (plan, apply, wait, status,
 // release); SU2G_OK at once for an empty list.

@@ -104,7 +104,7 @@ void add_tiles(std::vector<GemmTile>& tiles, int64_t c_off, int64_t c_len, int c
 
 int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                     const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, HeffWork* out,
-                    std::string* err) {
+                    std::string* err, bool fp64_tiles) {
   HeffWork& w = *out;
   w = HeffWork();
   if (!psi_desc) {
@@ -242,7 +242,7 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         g.alpha = 1.0;
         const int seg0 = (int)w.seg1.size();
         w.seg1.push_back(g);
-        add_tiles(w.tile1, T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1, a);
+        if (fp64_tiles) add_tiles(w.tile1, T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1, a);
         w.blk1.push_back(OutBlock{T.off, (int64_t)b * ms * c, kBufScratch, b, b, ms * c, seg0, 1});
         w.scratch_len += (int64_t)b * ms * c;
         w.flops += 2.0 * a * b * (double)ms * c;
@@ -335,7 +335,8 @@ int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const 
         w.max_k = std::max<int64_t>(w.max_k, g.K);
       }
     }
-    add_tiles(w.tile2, P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
+    if (fp64_tiles)
+      add_tiles(w.tile2, P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0, kwork);
     w.blk2.push_back(OutBlock{P.offset[m], (int64_t)c * d, kBufY, c, c, d, seg0, (int)w.seg2.size() - seg0});
   }
 
@@ -387,17 +388,49 @@ int check_list(const std::vector<GemmTile>& tiles, const std::vector<GemmSeg>& s
   }
   return SU2G_OK;
 }
+
+// every output block (M x N, leading dimension ldc) and every product it sums:
+// the accesses of all its tiles, whichever engine cuts them (a block's tiles
+// reach its first and last rows and columns, and no further)
+int check_blocks(const std::vector<OutBlock>& blks, const std::vector<GemmSeg>& segs, const HeffWork& w,
+                 const char* phase, std::string* err) {
+  for (const OutBlock& b : blks) {
+    if (b.M <= 0 || b.N <= 0) continue;  // no tile
+    if (!within(b.c, b.c_len, b.c_buf, w) || last_index(0, b.M, 0, b.N, b.ldc) >= b.c_len || b.ldc < b.M ||
+        b.seg0 < 0 || b.nseg < 0 || b.seg0 + b.nseg > (int)segs.size()) {
+      *err = std::string(phase) + ": block out of bounds";
+      return SU2G_EINVAL;
+    }
+    for (int s = b.seg0; s < b.seg0 + b.nseg; ++s) {
+      const GemmSeg& g = segs[s];
+      if (g.K <= 0 || !within(g.a, g.a_len, g.a_buf, w) || !within(g.b, g.b_len, g.b_buf, w)) {
+        *err = std::string(phase) + ": segment out of bounds";
+        return SU2G_EINVAL;
+      }
+      const int64_t alast = g.transA ? last_index(0, g.K, 0, b.M, g.lda) : last_index(0, b.M, 0, g.K, g.lda);
+      const int64_t blast = last_index(0, g.K, 0, b.N, g.ldb);
+      const bool lda_ok = g.transA ? g.lda >= g.K : g.lda >= b.M;
+      if (alast >= g.a_len || blast >= g.b_len || !lda_ok || g.ldb < g.K) {
+        *err = std::string(phase) + ": operand access beyond its block";
+        return SU2G_EINVAL;
+      }
+    }
+  }
+  return SU2G_OK;
+}
 }  // namespace
 
 int validate_heff_work(const HeffWork& w, std::string* err) {
-  int rc = check_list(w.tile1, w.seg1, w, "phase 1", err);
+  int rc = check_blocks(w.blk1, w.seg1, w, "phase 1", err);
+  if (!rc) rc = check_blocks(w.blk2, w.seg2, w, "phase 2", err);
+  if (!rc) rc = check_list(w.tile1, w.seg1, w, "phase 1", err);
+  if (!rc) rc = check_list(w.tile2, w.seg2, w, "phase 2", err);
   if (rc) return rc;
-  rc = check_list(w.tile2, w.seg2, w, "phase 2", err);
-  if (rc) return rc;
-  // the output tiles cover y exactly (each element written once)
+  // the output blocks cover y exactly (each element written once; the FP64
+  // tiles partition the blocks)
   int64_t written = 0;
-  for (const GemmTile& t : w.tile2)
-    if (t.c_buf == kBufY) written += (int64_t)t.mlen * t.nlen;
+  for (const OutBlock& b : w.blk2)
+    if (b.c_buf == kBufY && b.M > 0 && b.N > 0) written += (int64_t)b.M * b.N;
   if (written != w.psi.total) {
     *err = "phase 2 tiles do not cover y exactly";
     return SU2G_EINVAL;

@@ -52,14 +52,17 @@ struct HeffWork {
   int64_t max_k = 0;        // largest segment K
 };
 
-// Returns SU2G_OK or SU2G_EINVAL with *err set.
+// Returns SU2G_OK or SU2G_EINVAL with *err set.  fp64_tiles: also cut the
+// blocks into the FP64 engine's tiles (the split engine plans its own tiles
+// from the blocks and products).
 int build_heff_work(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                     const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, HeffWork* out,
-                    std::string* err);
+                    std::string* err, bool fp64_tiles = true);
 
 // Checks every element access the kernels will make against the extent of
 // the block it belongs to (and the block against its buffer for psi, y and
-// scratch).  Returns SU2G_OK or SU2G_EINVAL with *err set.
+// scratch): every output block with every product it sums, and every FP64
+// tile when they were built.  Returns SU2G_OK or SU2G_EINVAL with *err set.
 int validate_heff_work(const HeffWork& w, std::string* err);
 
 }  // namespace su2g

@@ -7,9 +7,8 @@
 
 #include <algorithm>
 #include <cstring>
-#include <map>
-#include <queue>
 #include <tuple>
+#include <unordered_map>
 
 namespace su2g {
 namespace oz {
@@ -17,10 +16,27 @@ namespace {
 
 using Key = std::tuple<int, int64_t, int64_t, int64_t, int, int, int, uint64_t>;
 
+struct KeyHash {
+  size_t operator()(const Key& k) const {
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    auto mix = [&](uint64_t x) { h ^= x + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2); };
+    mix((uint64_t)std::get<0>(k));
+    mix((uint64_t)std::get<1>(k));
+    mix((uint64_t)std::get<2>(k));
+    mix((uint64_t)std::get<3>(k));
+    mix((uint64_t)std::get<4>(k));
+    mix((uint64_t)std::get<5>(k));
+    mix((uint64_t)std::get<6>(k));
+    mix(std::get<7>(k));
+    return (size_t)h;
+  }
+};
+
 struct Builder {
   int S;
   OzWork* w;
-  std::map<Key, std::pair<int, int>> index;  // key -> (class, job index)
+  // key -> (class, job index); lookups only: jobs are numbered in order of first use
+  std::unordered_map<Key, std::pair<int, int>, KeyHash> index;
   std::vector<PackJob>* lists[3];
 
   // class 0 = operator (packed once), 1 = from psi, 2 = from the phase-1 intermediates
@@ -258,26 +274,37 @@ void schedule_tiles(std::vector<OzTile>* tiles, const std::vector<OzSeg>& segs, 
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  using Load = std::pair<int64_t, int>;  // (load, cta)
-  std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-  for (int b = 0; b < grid; ++b) heap.push({0, b});
-  std::vector<std::vector<int>> lists(grid);
+  // Longest first to the least-loaded CTA (the lower CTA on equal loads): a
+  // binary min-heap on (load, cta), whose top takes each tile's cost and
+  // sinks; every (load, cta) key is distinct, so the choices are those of any
+  // exact min-queue.
+  std::vector<std::pair<int64_t, int>> heap(grid);  // (load, cta)
+  for (int b = 0; b < grid; ++b) heap[b] = {0, b};
+  std::vector<int> count(grid, 0);
+  std::vector<int64_t> slot(n);  // position of tile i in the schedule: cta + k * grid
   for (int i : order) {
-    const Load l = heap.top();
-    heap.pop();
-    lists[l.second].push_back(i);
-    heap.push({l.first + cost[i], l.second});
+    const int b = heap[0].second;
+    slot[i] = b + (int64_t)count[b]++ * grid;
+    heap[0].first += cost[i];
+    for (int p = 0;;) {  // sink the top
+      const int l = 2 * p + 1, r = l + 1;
+      int m = p;
+      if (l < grid && heap[l] < heap[m]) m = l;
+      if (r < grid && heap[r] < heap[m]) m = r;
+      if (m == p) break;
+      std::swap(heap[p], heap[m]);
+      p = m;
+    }
   }
-  size_t kmax = 0;
-  for (const auto& l : lists) kmax = std::max(kmax, l.size());
+  int kmax = 0;
+  for (int c : count) kmax = std::max(kmax, c);
   OzTile pad{};
   pad.c_buf = kBufAbs;
   pad.ldc = 1;
   pad.rowmax = -1;
   pad.rms = 1;
   std::vector<OzTile> out((size_t)grid * kmax, pad);
-  for (int b = 0; b < grid; ++b)
-    for (size_t k = 0; k < lists[b].size(); ++k) out[b + k * grid] = (*tiles)[lists[b][k]];
+  for (int i = 0; i < n; ++i) out[slot[i]] = (*tiles)[i];
   tiles->swap(out);
 }
 
@@ -301,11 +328,11 @@ int build_ozaki_work(const HeffWork& hw, int S, OzWork* out, std::string* err) {
   // (i+1)*rms - 1, all block rows), the phase-1 tiles leave the row maxima
   // and the pack skips its own pass over the block.
   {
-    std::map<int64_t, std::vector<int>> by_src;
+    std::unordered_map<int64_t, std::vector<int>> by_src;
     for (int j = 0; j < (int)w.jobs[2].size(); ++j)
       if (w.jobs[2][j].src_buf == kBufScratch) by_src[w.jobs[2][j].src].push_back(j);
     w.rowmax_base = w.exp_len;
-    std::map<int64_t, std::pair<int64_t, int>> slots;  // block origin -> (slots, rms)
+    std::unordered_map<int64_t, std::pair<int64_t, int>> slots;  // block origin -> (slots, rms)
     for (const OutBlock& ob : hw.blk1) {
       auto it = by_src.find(ob.c);
       if (ob.c_buf != kBufScratch || it == by_src.end() || it->second.size() != 1) continue;

@@ -335,7 +335,7 @@ extern "C" int su2g_prepare_input_vector(su2g_tensor ul, su2g_tensor ur, double*
     e = launch_transposes(items, st);
   }
   if (e == cudaSuccess) {
-    rc = su2g::build_input_vector(ul, ur, urt, out, &v, &w, &err);
+    rc = su2g::build_input_vector(ul, ur, urt, out, &v, &w, &err, mode == SU2G_MODE_F64);
     if (rc) rc = fail(rc, err);
     else rc = su2g::run_work_once(std::move(w), mode, stream);
   }
