@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(256) canonical_signs_kernel(double* z, int row
     for (int i = threadIdx.x; i < rows; i += blockDim.x) col[i] = -col[i];
 }
 
-// Per-device resources kept across calls: lanes (one stream and one pair of
-// cuBLAS / cuSOLVER handles each; creating handles costs milliseconds), lent
+// Per-device resources kept across calls: lanes (one stream and one cuSOLVER
+// handle each; creating a handle costs milliseconds), lent
 // to a call for each sector it processes and returned after it, so calls from
 // several host threads (independent solves) run at the same time; and a
 // library-private memory pool whose freed blocks stay reserved (stream-ordered
