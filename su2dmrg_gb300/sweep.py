@@ -46,8 +46,9 @@ class Dmrg(Warmup):
             raise MemoryError(f"clone: {host / 1e9:.1f} GB of host-resident block tensors do not fit the host")
         d = Dmrg(self.lat, mode=self.mode if mode is None else mode, mlanc=self.mlanc)
         d.offload, d.host_fraction = self.offload, self.host_fraction
-        if hasattr(self, "host_bytes"):
-            d.host_bytes, d.host_cap, d._device = 2 * self.host_bytes, self.host_cap, getattr(self, "_device", None)
+        if hasattr(self, "_host"):  # the copies count against the same cap
+            self._host["used"] += host
+            d._host, d._device = self._host, getattr(self, "_device", None)
         d.ran_state = self.ran_state
         d.uu = [cp(t) for t in self.uu]
         d.hh = [cp(t) for t in self.hh]

@@ -291,6 +291,11 @@ class Warmup:
     offload = False
     host_fraction = 0.5
 
+    @property
+    def host_bytes(self) -> int:
+        """Bytes of block tensors this run (and its clones) hold in host memory."""
+        return self._host["used"] if hasattr(self, "_host") else 0
+
     def _position_slots(self, p: int):
         """(list, index) of every block tensor slot of position p."""
         ns = self.lat.ns
@@ -303,7 +308,7 @@ class Warmup:
         for lst, k in self._position_slots(p):
             t = lst[k]
             if t is not None and not t[1].is_cuda:
-                self.host_bytes -= t[1].numel() * t[1].element_size()
+                self._host["used"] -= t[1].numel() * t[1].element_size()
                 lst[k] = (t[0], t[1].to(self._device))
 
     def _evict(self, p: int) -> None:
@@ -312,20 +317,19 @@ class Warmup:
             return
         import torch
 
-        if not hasattr(self, "host_bytes"):
-            self.host_bytes = 0
-            self.host_cap = int(self.host_fraction * host_available_bytes())
+        if not hasattr(self, "_host"):  # shared with clones: one cap for all of them
+            self._host = {"cap": int(self.host_fraction * host_available_bytes()), "used": 0}
         moved = 0
         for lst, k in self._position_slots(p):
             t = lst[k]
             if t is None or not t[1].is_cuda:
                 continue
             nb = t[1].numel() * t[1].element_size()
-            if self.host_bytes + nb > self.host_cap:
+            if self._host["used"] + nb > self._host["cap"]:
                 continue
             self._device = t[1].device
             lst[k] = (t[0], t[1].to("cpu"))
-            self.host_bytes += nb
+            self._host["used"] += nb
             moved += nb
         if moved:
             torch.cuda.empty_cache()  # the freed blocks return to the device for the library's own pool
@@ -341,11 +345,24 @@ class Warmup:
         carry = L.fll if lr == 0 else L.frr
         for k in range(L.ns):
             if carry[p][k] == 1:
-                self.opr[p][k] = None
-        self.hh[p] = None
+                self._drop(self.opr[p], k)
+        self._drop(self.hh, p)
         for j in range(L.ns):
             if L.plqflg[p][j]:
-                self.plq[p][j] = self.plq[p][j + L.ns] = None
+                self._drop(self.plq[p], j)
+                self._drop(self.plq[p], j + L.ns)
+
+    def _put(self, lst, k: int, t) -> None:
+        """Stores a block tensor in a slot (a host-resident one it replaces leaves the host count)."""
+        self._drop(lst, k)
+        lst[k] = t
+
+    def _drop(self, lst, k: int) -> None:
+        """Empties a block tensor slot (a host-resident tensor leaves the host count)."""
+        t = lst[k]
+        if t is not None and not t[1].is_cuda:
+            self._host["used"] -= t[1].numel() * t[1].element_size()
+        lst[k] = None
 
     # ---------------------------------------------------- site updates
     def site_left(self, i: int, u, release: bool = False):
@@ -356,8 +373,8 @@ class Warmup:
         if i == 0:
             b = _Jobs()
             b.add(("opr", 0), "init", site1=L.sigma[0])
-            self.opr[0][0] = self._run(u, 0, b)[("opr", 0)]
-            self.hh[0] = None
+            self._put(self.opr[0], 0, self._run(u, 0, b)[("opr", 0)])
+            self._drop(self.hh, 0)
             return
         if release:
             self._release(i + 1, 1)
@@ -402,12 +419,12 @@ class Warmup:
                 elif p[j][1] < i < p[j][2] or p[j][2] < i < p[j][3]:
                     b.add(("plq", m), "transform", x=prev)
         out = self._run(u, 0, b)
-        self.hh[i] = out.get("hh")
+        self._put(self.hh, i, out.get("hh"))
         for name, t in out.items():
             if isinstance(name, tuple) and name[0] == "opr":
-                self.opr[i][name[1]] = t
+                self._put(self.opr[i], name[1], t)
             elif isinstance(name, tuple):
-                self.plq[i][name[1]] = t
+                self._put(self.plq[i], name[1], t)
         if release:
             self._evict(i - 1)
 
@@ -419,8 +436,8 @@ class Warmup:
         if i == ns - 1:
             b = _Jobs()
             b.add(("opr", i), "init", site1=L.sigma[1])
-            self.opr[i][i] = self._run(u, 1, b)[("opr", i)]
-            self.hh[i] = None
+            self._put(self.opr[i], i, self._run(u, 1, b)[("opr", i)])
+            self._drop(self.hh, i)
             return
         if release:
             self._release(i - 1, 0)
@@ -466,12 +483,12 @@ class Warmup:
                 elif p[j][1] < i < p[j][2] or p[j][0] < i < p[j][1]:
                     b.add(("plq", m), "transform", x=prev)
         out = self._run(u, 1, b)
-        self.hh[i] = out.get("hh")
+        self._put(self.hh, i, out.get("hh"))
         for name, t in out.items():
             if isinstance(name, tuple) and name[0] == "opr":
-                self.opr[i][name[1]] = t
+                self._put(self.opr[i], name[1], t)
             elif isinstance(name, tuple):
-                self.plq[i][name[1]] = t
+                self._put(self.plq[i], name[1], t)
         if release:
             self._evict(i + 1)
 

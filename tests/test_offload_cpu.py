@@ -33,6 +33,9 @@ class _FakeDeviceTensor:
     def to(self, where):
         return _FakeDeviceTensor(self.n, "cpu" if str(where) == "cpu" else "cuda")
 
+    def clone(self):
+        return _FakeDeviceTensor(self.n, self.where)
+
 
 def _warmup():
     from su2dmrg_gb300.warmup import Lattice, Warmup
@@ -116,3 +119,44 @@ def test_refused_allocation_is_retried_once_after_freeing_the_cache():
 
     with pytest.raises(capi.Su2gError):
         Warmup._freeing(always_refused, 1)
+
+
+def test_released_host_tensors_leave_the_host_count():
+    w = _warmup()
+    w.offload = True
+    L = w.lat
+    p = 4
+    ks = [k for k in range(L.ns) if L.fll[p][k] == 1]
+    assert ks
+    for k in ks:
+        w.opr[p][k] = ("s", _FakeDeviceTensor(10))
+    w.hh[p] = ("s", _FakeDeviceTensor(5))
+    w._evict(p)
+    assert w.host_bytes == 8 * (10 * len(ks) + 5)
+    w._release(p, 0)
+    assert w.host_bytes == 0 and w.hh[p] is None and all(w.opr[p][k] is None for k in ks)
+
+
+def test_replaced_host_tensors_leave_the_host_count():
+    w = _warmup()
+    w.offload = True
+    w.opr[3][1] = ("s", _FakeDeviceTensor(10))
+    w._evict(3)
+    assert w.host_bytes == 80
+    w._put(w.opr[3], 1, ("s", _FakeDeviceTensor(4)))  # a site update's new result
+    assert w.host_bytes == 0 and w.opr[3][1][1].is_cuda
+
+
+def test_clone_shares_the_host_budget():
+    from su2dmrg_gb300.sweep import Dmrg
+
+    w = _warmup()
+    d = Dmrg(w.lat)
+    d.offload = True
+    d.opr[2][1] = ("s", _FakeDeviceTensor(10))
+    d._evict(2)
+    c = d.clone()
+    assert not c.opr[2][1][1].is_cuda and c.offload
+    assert d.host_bytes == c.host_bytes == 160  # the original's tensor and the clone's copy
+    c._fetch(2)
+    assert d.host_bytes == 80
