@@ -447,16 +447,26 @@ class _EnvJobs:
 
 def env_layout(uu, xu, vv, xv, flag: int, jobs, slot: int = 0) -> Su2Struct:
     """Structure of output slot `slot` of an env batch (host only)."""
+    return env_layouts(uu, xu, vv, xv, flag, jobs, [slot])[0]
+
+
+def env_layouts(uu, xu, vv, xv, flag: int, jobs, slots) -> list:
+    """Structures of the output slots `slots` of an env batch (host only): the
+    job array and the output buffers are built once for all of them."""
     keep = []
     J = _EnvJobs(jobs)
+    tu, tv = _tensor(uu, xu, keep), _tensor(vv, xv, keep)
     desc = np.zeros(4 + 3 * (2 + 2 * 64), np.int32)
     flags = np.zeros(64 ** 3, np.int32)
     n = ctypes.c_int64()
-    check(lib().su2g_env_layout(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, int(slot),
-                                ptr(desc), len(desc), ptr(flags), len(flags), ctypes.addressof(n)))
-    out = _parse_desc(desc)
-    out.flag = flags[: out.nten].copy()
-    return out
+    res = []
+    for slot in slots:
+        check(lib().su2g_env_layout(tu, tv, int(flag), J.n, J.ptr, int(slot), ptr(desc), len(desc), ptr(flags),
+                                    len(flags), ctypes.addressof(n)))
+        out = _parse_desc(desc)
+        out.flag = flags[: out.nten].copy()
+        res.append(out)
+    return res
 
 
 def env_run(uu, xu, vv, xv, flag: int, jobs, outs, mode: int = capi.MODE_F64, stream=None) -> None:
@@ -489,10 +499,8 @@ def env_batch(uu, xu, vv, xv, flag: int, jobs, mode: int = capi.MODE_F64, stream
 
     nslots = 1 + max(int(j.get("slot", 0)) for j in jobs)
     dev = xu.device if hasattr(xu, "device") else torch.device("cuda")
-    res = []
-    for s in range(nslots):
-        st = env_layout(uu, xu, vv, xv, flag, jobs, s)
-        res.append((st, torch.empty(max(1, st.size()), dtype=torch.float64, device=dev)))
+    res = [(st, torch.empty(max(1, st.size()), dtype=torch.float64, device=dev))
+           for st in env_layouts(uu, xu, vv, xv, flag, jobs, range(nslots))]
     env_run(uu, xu, vv, xv, flag, jobs, [r[1] for r in res], mode, stream)
     return res
 
