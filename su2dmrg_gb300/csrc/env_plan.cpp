@@ -21,8 +21,8 @@
 
 #include <algorithm>
 #include <cmath>
-#include <map>
 #include <tuple>
+#include <unordered_map>
 
 namespace su2g {
 namespace {
@@ -418,7 +418,14 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
     }
   }
   // ---- phase 1: T = X_s^T U per (job, X block, U block, slice) ----
-  std::map<std::tuple<int, int, int>, int64_t> tpos;  // (job, X block, U block) -> slice-0 T offset
+  struct TKeyHash {
+    size_t operator()(const std::tuple<int, int, int>& k) const {
+      const uint64_t a = (uint32_t)std::get<0>(k), b = (uint32_t)std::get<1>(k), c = (uint32_t)std::get<2>(k);
+      return (size_t)((a * 0x9e3779b97f4a7c15ull) ^ (b * 0xc2b2ae3d27d4eb4full) ^ (c * 0x165667b19e3779f9ull));
+    }
+  };
+  // (job, X block, U block) -> slice-0 T offset; lookups only (offsets follow contribution order)
+  std::unordered_map<std::tuple<int, int, int>, int64_t, TKeyHash> tpos;
   for (const Contrib& c : cs) {
     if (c.xj < 0 || tpos.count({c.job, c.xj, c.k})) continue;
     const Job& jb = J[c.job];
@@ -450,15 +457,23 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
     }
   }
   // ---- phase 2: out(c, s, c') = sum w T_s^T V (or w U^T V), per block and slice ----
-  std::map<std::tuple<int, int, int>, std::vector<int>> by_out;  // (slot, block, slice) -> contributions
-  for (int q = 0; q < (int)cs.size(); ++q) by_out[{J[cs[q].job].slot, cs[q].m, cs[q].os}].push_back(q);
-  for (auto& kv : by_out) {
-    const int sl = std::get<0>(kv.first), m = std::get<1>(kv.first), os = std::get<2>(kv.first);
+  // contributions grouped by (slot, block, slice) in ascending order, each
+  // group in contribution order
+  using OutKey = std::tuple<int, int, int>;
+  std::vector<std::pair<OutKey, int>> by_out(cs.size());
+  for (int q = 0; q < (int)cs.size(); ++q) by_out[q] = {OutKey{J[cs[q].job].slot, cs[q].m, cs[q].os}, q};
+  std::stable_sort(by_out.begin(), by_out.end(),
+                   [](const std::pair<OutKey, int>& x, const std::pair<OutKey, int>& y) { return x.first < y.first; });
+  for (size_t g0 = 0; g0 < by_out.size();) {
+    size_t g1 = g0;
+    while (g1 < by_out.size() && by_out[g1].first == by_out[g0].first) ++g1;
+    const int sl = std::get<0>(by_out[g0].first), m = std::get<1>(by_out[g0].first), os = std::get<2>(by_out[g0].first);
     const Struct& Y = (*slot_structs)[sl];
     const int C = Y.block_dim(m, 0), Cp = Y.block_dim(m, Y.nbond - 1), ms = Y.nbond == 3 ? Y.block_dim(m, 1) : 1;
     const int seg0 = (int)w.seg2.size();
     int64_t kwork = 0;
-    for (int q : kv.second) {
+    for (size_t gi = g0; gi < g1; ++gi) {
+      const int q = by_out[gi].second;
       const Contrib& c = cs[q];
       const Job& jb = J[c.job];
       GemmSeg g;
@@ -491,6 +506,7 @@ int build_env_batch(const su2g_tensor& uu, const su2g_tensor& vv, int flag, int 
     const int64_t ylen = (int64_t)C * ms * Cp - (int64_t)C * os;
     if (fp64_tiles) add_tiles(w.tile2, yoff, ylen, kBufAbs, C * ms, C, Cp, seg0, (int)w.seg2.size() - seg0, kwork);
     w.blk2.push_back(OutBlock{yoff, ylen, kBufAbs, C * ms, C, Cp, seg0, (int)w.seg2.size() - seg0});
+    g0 = g1;
   }
   auto heavier = [](const GemmTile& x, const GemmTile& y) { return x.kwork > y.kwork; };
   std::stable_sort(w.tile1.begin(), w.tile1.end(), heavier);
