@@ -106,7 +106,8 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
       ids.push_back({ja, jb});
       bufs.push_back({g.a_buf, g.b_buf});
     }
-    // runs of products within the bounds of one tile (one run: the whole block)
+    // runs of products within the bounds of one tile (one run: the whole
+    // block, also when no product reaches it)
     std::vector<std::pair<int, int>> runs;  // (first product, count) relative to ob.seg0
     {
       int r0 = 0;
@@ -124,7 +125,7 @@ int build_phase(Builder& B, const std::vector<GemmSeg>& segs, const std::vector<
         }
         k += ks;
       }
-      if (ob.nseg > 0) runs.push_back({r0, ob.nseg - r0});
+      runs.push_back({r0, ob.nseg - r0});  // a block no product reaches: one tile of zeros
     }
     if (runs.size() > 1 && !may_split) {
       *err = "split mode: more than 2^17 contracted values or 1024 products feed one intermediate block";

@@ -125,13 +125,16 @@ def test_term_coefficients_and_missing_blocks(torch_cuda, oracle):
     assert _rel(y.cpu().numpy(), ref) <= TOL
 
 
-def test_empty_plan_writes_zeros(torch_cuda, oracle):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_empty_plan_writes_zeros(torch_cuda, oracle, mode):
+    """Output blocks no product reaches are written as zeros (FP64 tiles and
+    split tiles without segments alike)."""
     from su2dmrg_gb300.su2 import HeffPlan
     from su2dmrg_gb300.workloads import synthetic_heff
 
     torch = torch_cuda
     w = synthetic_heff(D=30, nspin1=0, seed=1, spin0=False)
-    plan = HeffPlan(w.psi, [])
+    plan = HeffPlan(w.psi, [], mode=mode)
     psi = _dev(torch, w.psi_data)
     y = torch.full_like(psi, 7.0)
     plan.apply(psi, y)
