@@ -861,8 +861,11 @@ def run_serve(args):
     (su2dmrg_gb300.serve.Server: --slots solves in flight, admission by
     device footprint, Lanczos solves in shared launches), then the first
     --seq-requests of the same requests one after another on the plain
-    per-solve path; their results must be identical.  Wall-clock seconds on
-    the host, every library call blocking."""
+    per-solve path.  Solves that converged (energy change below 1e-6) in both
+    runs must agree to 1e-10 in energy; unconverged early sweeps amplify
+    rounding differences between a solve that shared the GPU and one that ran
+    alone, so they are reported but not compared.  Wall-clock seconds on the
+    host, every library call blocking."""
     import copy
 
     import torch
