@@ -29,6 +29,14 @@ step instead, on workloads.synthetic_site_step at the same D, through its C
 ABI call with arguments prepared once (each call blocks; its host planning is
 inside the timed region), with L2 flushed before every call; same JSON keys,
 its own metric.
+
+--row sweep runs whole DMRG sweeps of an lx x ly cylinder (--lattice, --D,
+--delta, --qdelta, --seed; --converge or --sweeps-before), then the next sweep
+in split and in FP64 precision from the same state (--skip-fp64: split only);
+--offload keeps the block tensors of passed positions in host memory and
+--step-log prints one stderr line per two-site step.  --row serve runs the
+serving stream (--requests, --rate, --slots, --no-batch, --seq-requests);
+--row tune measures the FP64 engine's tile table (--table-out).
 """
 from __future__ import annotations
 
