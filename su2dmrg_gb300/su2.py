@@ -317,7 +317,7 @@ def hamiltonian_vector_multiplication(vec: Su2Struct, vec_data, op1: Su2Struct, 
 
 
 def _parse_desc(d):
-    d = [int(v) for v in d]
+    d = d.tolist() if isinstance(d, np.ndarray) else [int(v) for v in d]
     nb, loc, p = d[0], d[1], 2
     bonds = []
     for _ in range(nb):
