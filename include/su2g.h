@@ -112,6 +112,14 @@ int su2g_heff_plan_create(const int* psi_desc, const int* psi_flag, int nterms, 
 int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
                             const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
                             double* flops, int64_t* scratch_bytes);
+/* Host-only digest of every field of the work lists su2g_heff_plan_create
+ * would build for `mode` (they fix every sum's order: equal digests, equal
+ * results bit for bit).  Absolute operand addresses enter it: pass the same
+ * data pointers to compare two builds.  No counterpart in the reference; it
+ * pins the planner in tests. */
+int su2g_heff_plan_digest(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                          uint64_t* digest);
 /* Reads and clears the plan's device error word (the split-precision kernels
  * record a bounded wait that gave up there).  SU2G_ETIMEOUT if one did. */
 int su2g_heff_plan_status(su2g_heff_plan* plan, int* code);
@@ -296,6 +304,10 @@ int su2g_env_run(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g
  * flops and the device scratch it needs. */
 int su2g_env_validate(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
                       int mode, double* flops, int64_t* scratch_bytes);
+/* Host-only digest of the work lists su2g_env_run would build (as
+ * su2g_heff_plan_digest; the output addresses enter it too). */
+int su2g_env_digest(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                    double* const* outs, int mode, uint64_t* digest);
 
 /* Recoupling factors of the site updates, computed on first use from the
  * Clebsch-Gordan contractions the reference tabulates (dmrg_su2.cpp:776-1019):

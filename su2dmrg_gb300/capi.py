@@ -71,6 +71,7 @@ _PROTOS = {
     "su2g_fac_operator_transformation": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "su2g_heff_plan_create": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp]),
     "su2g_heff_plan_validate": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp, _vp]),
+    "su2g_heff_plan_digest": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _d, _i, _vp]),
     "su2g_heff_plan_status": (_i, [_vp, _vp]),
     "su2g_heff_plan_mark_failed": (_i, [_vp, _i]),
     "su2g_f64_tile_table": (_i, [_vp, _i, _vp, _i, _vp]),
@@ -100,6 +101,7 @@ _PROTOS = {
     "su2g_env_layout": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
     "su2g_env_run": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _vp, _i, _vp]),
     "su2g_env_validate": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _i, _vp, _vp]),
+    "su2g_env_digest": (_i, [Tensor, Tensor, _i, _i, _vp, _i, _vp, _i, _vp]),
     "su2g_fac_table": (_i, [_i, _i, _i, _i, _i, _i, _i, _vp]),
     "su2g_svd": (_i, [_vp, _vp, _vp, _vp, _d, _vp, _d, _i, _vp, _i, _vp, _i, _vp, _vp, _i64, _vp, _i64, _vp]),
     "su2g_vectran_layout": (_i, [Tensor, _i, _vp, _i, _vp, _i, _vp]),

@@ -451,6 +451,125 @@ int su2g_heff_plan_validate(const int* psi_desc, const int* psi_flag, int nterms
   return SU2G_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// FNV-style digest of every field of the work lists a mode builds (the
+// lists fix every sum's order, so equal digests mean bit-identical results)
+struct Digest {
+  uint64_t h = 1469598103934665603ull;
+  void add(int64_t x) {
+    h ^= (uint64_t)x;
+    h *= 1099511628211ull;
+    h ^= h >> 29;
+  }
+  void add(double x) {
+    int64_t b;
+    std::memcpy(&b, &x, 8);
+    add(b);
+  }
+};
+
+void digest_work(const su2g::HeffWork& w, const su2g::oz::OzWork* oz, Digest& d) {
+  for (const auto* v : {&w.seg1, &w.seg2}) {
+    d.add((int64_t)v->size());
+    for (const su2g::GemmSeg& g : *v) {
+      d.add(g.a), d.add((int64_t)g.a_buf), d.add(g.a_len), d.add(g.b), d.add((int64_t)g.b_buf), d.add(g.b_len);
+      d.add((int64_t)g.lda), d.add((int64_t)g.ldb), d.add((int64_t)g.K), d.add((int64_t)g.transA), d.add(g.alpha);
+    }
+  }
+  for (const auto* v : {&w.blk1, &w.blk2}) {
+    d.add((int64_t)v->size());
+    for (const su2g::OutBlock& b : *v) {
+      d.add(b.c), d.add(b.c_len), d.add((int64_t)b.c_buf), d.add((int64_t)b.ldc), d.add((int64_t)b.M);
+      d.add((int64_t)b.N), d.add((int64_t)b.seg0), d.add((int64_t)b.nseg);
+    }
+  }
+  for (const auto* v : {&w.tile1, &w.tile2}) {
+    d.add((int64_t)v->size());
+    for (const su2g::GemmTile& t : *v) {
+      d.add(t.c), d.add(t.c_len), d.add((int64_t)t.c_buf), d.add((int64_t)t.ldc), d.add((int64_t)t.m0);
+      d.add((int64_t)t.n0), d.add((int64_t)t.mlen), d.add((int64_t)t.nlen), d.add((int64_t)t.seg0);
+      d.add((int64_t)t.nseg), d.add(t.kwork), d.add((int64_t)t.cls);
+    }
+  }
+  d.add(w.scratch_len), d.add(w.flops), d.add(w.max_k), d.add(w.psi.total);
+  if (!oz) return;
+  const su2g::oz::OzWork& o = *oz;
+  for (const auto* v : {&o.seg1, &o.seg2}) {
+    d.add((int64_t)v->size());
+    for (const su2g::oz::OzSeg& z : *v) d.add(z.a_unit), d.add(z.b_unit), d.add(z.a_exp), d.add(z.b_exp), d.add(z.a_tmax), d.add((int64_t)z.nks);
+  }
+  for (const auto* v : {&o.tile1, &o.tile2}) {
+    d.add((int64_t)v->size());
+    for (const su2g::oz::OzTile& t : *v) {
+      d.add(t.c), d.add((int64_t)t.c_buf), d.add((int64_t)t.ldc), d.add((int64_t)t.m0), d.add((int64_t)t.n0);
+      d.add((int64_t)t.mlen), d.add((int64_t)t.nlen), d.add((int64_t)t.seg0), d.add((int64_t)t.nseg), d.add(t.work);
+      d.add(t.rowmax), d.add((int64_t)t.rms);
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    d.add((int64_t)o.jobs[c].size());
+    for (const su2g::oz::PackJob& j : o.jobs[c]) {
+      d.add(j.src), d.add((int64_t)j.src_buf), d.add((int64_t)j.R), d.add((int64_t)j.K), d.add(j.ld_r), d.add(j.ld_k);
+      d.add((int64_t)j.rt), d.add((int64_t)j.nrt), d.add((int64_t)j.nkt), d.add(j.alpha), d.add(j.dst), d.add(j.exp);
+      d.add(j.texp), d.add(j.rowmax);
+    }
+    d.add((int64_t)o.units[c].size());
+    for (const su2g::oz::Unit& u : o.units[c]) d.add((int64_t)u.job), d.add((int64_t)u.rt);
+    d.add((int64_t)o.max_nkt[c]), d.add((int64_t)o.rows_pass[c]);
+  }
+  d.add((int64_t)o.red2.size());
+  for (const su2g::oz::RedTile& r : o.red2) {
+    d.add(r.c), d.add((int64_t)r.c_buf), d.add((int64_t)r.ldc), d.add((int64_t)r.m0), d.add((int64_t)r.n0);
+    d.add((int64_t)r.mlen), d.add((int64_t)r.nlen), d.add((int64_t)r.nparts), d.add(r.part);
+  }
+  d.add(o.packed_bytes), d.add(o.exp_len), d.add(o.rowmax_base), d.add(o.rowmax_len), d.add(o.scratch_base);
+  d.add(o.partial_len);
+}
+
+int digest_of(su2g::HeffWork& w, int S, uint64_t* digest) {
+  Digest d;
+  std::string err;
+  if (S > 0) {
+    su2g::oz::OzWork oz;
+    const int rc = su2g::oz::build_ozaki_work(w, S, &oz, &err);
+    if (rc) return fail(rc, err);
+    digest_work(w, &oz, d);
+  } else {
+    digest_work(w, nullptr, d);
+  }
+  *digest = d.h;
+  return SU2G_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int su2g_heff_plan_digest(const int* psi_desc, const int* psi_flag, int nterms, const su2g_term* terms,
+                          const su2g_tensor* hl, double hl_coef, const su2g_tensor* hr, double hr_coef, int mode,
+                          uint64_t* digest) {
+  const int S = slices_of_mode(mode);
+  if (S < 0 || !digest) return fail(SU2G_EINVAL, "plan_digest: bad arguments");
+  su2g::HeffWork w;
+  std::string err;
+  const int rc = su2g::build_heff_work(psi_desc, psi_flag, nterms, terms, hl, hl_coef, hr, hr_coef, &w, &err, S == 0);
+  if (rc) return fail(rc, err);
+  return digest_of(w, S, digest);
+}
+
+int su2g_env_digest(su2g_tensor uu, su2g_tensor vv, int flag, int njobs, const su2g_env_job* jobs, int nslots,
+                    double* const* outs, int mode, uint64_t* digest) {
+  const int S = slices_of_mode(mode);
+  if (S < 0 || !digest || nslots < 0 || (nslots > 0 && !outs)) return fail(SU2G_EINVAL, "env_digest: bad arguments");
+  su2g::HeffWork w;
+  std::vector<su2g::Struct> ys;
+  std::string err;
+  const int rc = su2g::build_env_batch(uu, vv, flag, njobs, jobs, nslots, outs, &w, &ys, &err, S == 0);
+  if (rc) return fail(rc, err);
+  return digest_of(w, S, digest);
+}
+
 int su2g_heff_plan_launches(const su2g_heff_plan* p, int* n) {
   if (!p || !n) return fail(SU2G_EINVAL, "plan_launches: bad arguments");
   int c = 0;

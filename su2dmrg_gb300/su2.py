@@ -193,6 +193,15 @@ class HeffPlan:
             check(lib().su2g_heff_plan_validate(*a.args, int(mode), ctypes.addressof(fl), ctypes.addressof(sb)))
         return {"flops": fl.value, "scratch_bytes": sb.value}
 
+    @staticmethod
+    def digest(psi: Su2Struct, terms, hl=None, hr=None, mode: int = capi.MODE_F64) -> int:
+        """Host-only digest of every field of the work lists of `mode`
+        (su2g_heff_plan_digest); operand addresses enter it."""
+        dg = ctypes.c_uint64()
+        with _PlanArgs(psi, terms, hl, hr) as a:
+            check(lib().su2g_heff_plan_digest(*a.args, int(mode), ctypes.addressof(dg)))
+        return dg.value
+
     def status(self) -> int:
         """Device error word (0 = no bounded wait gave up); raises on time-out."""
         code = ctypes.c_int()
@@ -491,6 +500,18 @@ def env_validate(uu, xu, vv, xv, flag: int, jobs, mode: int = capi.MODE_F64) -> 
     check(lib().su2g_env_validate(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, nslots,
                                   int(mode), ctypes.addressof(flops), ctypes.addressof(scratch)))
     return {"flops": flops.value, "scratch_bytes": scratch.value}
+
+
+def env_digest(uu, xu, vv, xv, flag: int, jobs, outs, mode: int = capi.MODE_F64) -> int:
+    """Host-only digest of the work lists of an env batch (su2g_env_digest);
+    operand and output addresses enter it."""
+    keep = []
+    J = _EnvJobs(jobs)
+    optr = (ctypes.c_void_p * max(1, len(outs)))(*[ptr(o) for o in outs])
+    dg = ctypes.c_uint64()
+    check(lib().su2g_env_digest(_tensor(uu, xu, keep), _tensor(vv, xv, keep), int(flag), J.n, J.ptr, len(outs),
+                                ctypes.addressof(optr), int(mode), ctypes.addressof(dg)))
+    return dg.value
 
 
 def env_batch(uu, xu, vv, xv, flag: int, jobs, mode: int = capi.MODE_F64, stream=None):
